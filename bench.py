@@ -1,0 +1,362 @@
+"""Benchmark: TOF-SSS scatter-point x detector-pair x TOF-bin throughput.
+
+Workload (one "step"): a full TOF single scatter simulation of the plain
+single-instance configuration — 64x64x48 voxels of 6 mm, 760-crystal x
+80-ring scanner (820 mm diameter) sampled as 16 rings x 48 crystals, 13 TOF
+bins of 39 mm, 214 ps FWHM, scatter points every 2nd voxel with mu > 0.
+Inputs are a seeded synthetic water cylinder with lung insert and six hot
+spheres (no public dataset is used).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  For N > 1 (launched by torch.distributed.run)
+every rank runs an independent replica on its own GPU ("replicas only": the
+path does not shard), the time is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TOF-SSS scatter-pt x det-pair x TOF-bin / s"
+UNIT = "units/s"
+
+
+def _att_table():
+    return np.load(os.path.join(ROOT, "tests", "golden", "tables.npz"))["att_table"]
+
+
+def _pairs(nru, ndu):
+    return nru * nru * ndu * (ndu - 1) // 2 + ndu * nru * (nru - 1)
+
+
+def _workload():
+    from opensss_gb300 import workloads as W
+
+    return W.config2(seed=0)
+
+
+def _config(pr, extra=None):
+    c = {"workload": pr.name, "volume": list(pr.grid), "voxel_mm": 6.0,
+         "scanner": "760 crystals x 80 rings, 820 mm", "sampled_rings": pr.nr_rings_used,
+         "sampled_crystals": pr.nr_detectors_used, "tof_bins": pr.nr_bins,
+         "tof_fwhm_ps": pr.tof_resolution, "sample_step": [int(s) for s in pr.sample_step],
+         "l2": "flushed between timed steps (256 MiB write); leg lists also exceed L2",
+         "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU side
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_sample(pr, att, points, threads):
+    """FP64 C restatement of the reference on the first `points` scatter points."""
+    from oracle import build_oracle
+    from oracle import oracle as O
+
+    build_oracle.build_oracle()
+    t0 = time.perf_counter()
+    out = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                        pr.scanner.normals, pr.scanner.detector_size_mm, att, pr.energy_resolution,
+                        pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step,
+                        pr.tof_resolution, pr.tof_range, pr.nr_bins, sp_end=points, nthreads=threads)
+    return out, time.perf_counter() - t0
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    pr = _workload()
+    att = _att_table()
+    threads = cpu_threads()
+    P = _pairs(pr.nr_rings_used, pr.nr_detectors_used)
+    points = args.ref_points
+    units = points * P * pr.nr_bins
+    times = []
+    for i in range(args.warmup + args.steps):
+        _, dt = oracle_sample(pr, att, points, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    t = max(times) if times else float("nan")
+    v = units / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": _config(pr, {"sample_points": points}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"first {points} scatter points of the workload "
+                                       f"({units:.3e} units per step)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from opensss_gb300 import TofSSS, _lib
+    from opensss_gb300.engine import fortran_flat, leg_pair_to_compact
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    pr = _workload()
+    att = _att_table()
+    L = _lib.lib()
+    eng = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
+                 pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used,
+                 pr.sample_step, pr.tof_resolution, pr.tof_range, pr.nr_bins, device=dev)
+    act = torch.from_numpy(np.ascontiguousarray(pr.activity)).to(dev)
+    mu = torch.from_numpy(np.ascontiguousarray(pr.attenuation)).to(dev)
+    P = _pairs(pr.nr_rings_used, pr.nr_detectors_used)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # scatter points of this workload
+    act_f, mu_f = fortran_flat(act, dev), fortran_flat(mu, dev)
+    p = eng.problem(act_f, mu_f, pr.grid, pr.image_size)
+    pts, counts = eng.scatter_points(p)
+    nsp = int(counts.sum())
+    units = nsp * P * pr.nr_bins
+
+    L.sss_set_timing(1)
+    out = torch.empty((pr.nr_bins, eng.nl, eng.nl), dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        eng.run(act, mu, pr.image_size, out=out)
+    stage = np.zeros(6)
+    step_ms = []
+    pair_ms = []
+    leg_ms = []
+    launches = 0
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        torch.cuda.synchronize(dev)
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.run(act, mu, pr.image_size, out=out, check=False)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            L.sss_get_timing(stage.ctypes.data_as(C.c_void_p))
+            leg_ms.append(stage[0])
+            pair_ms.append(stage[1])
+            launches += 1 + int(stage[2])  # scatter-point kernel + per-wave leg and pair kernels
+        torch.cuda.synchronize(dev)
+        barrier()
+    _lib.check_status(int(eng._status.item()))
+    clocks = clk.summary()
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * units * args.steps / total_s
+
+    # ---- end to end through the public API, host buffers, copies inside
+    act_h = torch.from_numpy(np.ascontiguousarray(pr.activity)).pin_memory()
+    mu_h = torch.from_numpy(np.ascontiguousarray(pr.attenuation)).pin_memory()
+    res_h = torch.empty((pr.nr_bins, eng.nl, eng.nl), dtype=torch.float32).pin_memory()
+    e2e_s = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        a = act_h.to(dev, non_blocking=True)
+        m = mu_h.to(dev, non_blocking=True)
+        r = eng.run(a, m, pr.image_size, out=out, check=False)
+        res_h.copy_(r, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        if i >= args.warmup:
+            e2e_s.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_s)
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * units * args.steps / e2e_total
+    h2d = act_h.numel() * 4 + mu_h.numel() * 4
+    d2h = res_h.numel() * 4
+    L.sss_set_timing(0)
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (pair kernel: SFU-bound 2^x per voxel-bin)
+    pair_s = statistics.mean(pair_ms) / 1e3
+    ex2_per_launch = stage[4] if stage[4] > 0 else None
+    peak = _sfu_peak(clocks)
+    roof = {"bound": "sfu", "unit": "Gex2/s", "kernel": "pair_kernel",
+            "achieved": (ex2_per_launch / pair_s / 1e9) if ex2_per_launch else None,
+            "peak": peak["value"], "peak_source": peak["source"], "traffic": _traffic()}
+    roof["frac"] = (roof["achieved"] / roof["peak"]) if roof["achieved"] and roof["peak"] else None
+
+    # ---- CPU baseline (oracle port on the host cores) and error vs FP64 on the same sample
+    cpu = None
+    err = None
+    if world == 1 and not args.no_cpu:
+        threads = cpu_threads()
+        ref, dt = oracle_sample(pr, att, args.ref_points, threads)
+        u = args.ref_points * P * pr.nr_bins
+        cpu = {"value": u / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {args.ref_points} scatter points of the workload ({u:.3e} units)"}
+        sub = eng.run(act, mu, pr.image_size, max_points=args.ref_points).cpu().numpy()
+        got = leg_pair_to_compact(sub, pr.nr_rings_used, pr.nr_detectors_used)
+        err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+
+    ms = 1e3 * total_s / args.steps
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 ray walk)",
+            "data": "synthetic", "config": _config(pr, {"scatter_points": nsp,
+                                                        "detector_pairs": P,
+                                                        "units_per_step": units}),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "path": "TofSSS.run on pinned host volumes, compact result copied back"},
+            "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+            "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
+            "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def _sfu_peak(clocks):
+    """SFU 2^x peak measured in this process (sss_probe_ex2_rate: every SM
+    issuing independent ex2 chains), else 152 SMs x 16 results/clk x max clock."""
+    import torch
+
+    from opensss_gb300 import _lib
+
+    v = C.c_double(0.0)
+    st = torch.cuda.current_stream()
+    if _lib.lib().sss_probe_ex2_rate(C.byref(v), C.c_void_p(st.cuda_stream)) == 0 and v.value > 0:
+        return {"value": v.value, "source": "measured (sss_probe_ex2_rate)"}
+    mhz = clocks.get("sm_max_mhz") or 2070.0
+    return {"value": 152 * 16 * mhz * 1e6 / 1e9, "source": "nominal 152 SM x 16/clk x max clock"}
+
+
+def _traffic():
+    path = os.path.join(ROOT, "profiles", "pair_kernel_c2.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-points", type=int, default=48,
+                    help="scatter points in the bounded CPU sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+/*
+ * sss300 — C ABI of the GB300 (sm_103a) TOF single-scatter-simulation engine.
+ *
+ * Plain C: integers, doubles and raw pointers.  "device" pointers are CUDA
+ * global-memory addresses on the current device (e.g. torch.Tensor.data_ptr()),
+ * "host" pointers are ordinary process memory.  `stream` is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream).  Every call returns 0 on
+ * success or an SSS_ERR_* code and never throws; sss_last_error() gives a
+ * thread-local message.  Kernels report data-dependent failures by OR-ing bits
+ * into a caller-owned device status word (int32, zeroed by the caller); map it
+ * with sss_status_code() after synchronising the stream.
+ *
+ * Each entry point cites the reference interface it replaces
+ * (openSSS v1.0, paths relative to the reference project root).
+ */
+#ifndef SSS300_H
+#define SSS300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SSS300_ABI_VERSION 1
+
+enum {
+    SSS_OK = 0,
+    SSS_ERR_INVALID = 1,    /* bad argument (shape, null pointer, range) */
+    SSS_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    SSS_ERR_OVERRUN = 3,    /* a ray walked past Nx+Ny+Nz voxels; the reference raises
+                               IndexError there (Python/openSSS/RayTracing3DTOF.py:162) */
+    SSS_ERR_TOF_RANGE = 4,  /* TOF offset beyond the 8001-entry table; the reference raises
+                               IndexError (SingleScatterSimulationTOF.py:521,527) */
+    SSS_ERR_ENERGY = 5,     /* scattered energy row outside the 2000-row tables */
+    SSS_ERR_VOXEL = 6,      /* linear voxel index outside the volume (only if Nx != Ny) */
+    SSS_ERR_WORKSPACE = 7,  /* workspace too small */
+    SSS_ERR_CAPACITY = 8    /* an output capacity was too small */
+};
+
+/* Thread-local text of the last error. */
+const char *sss_last_error(void);
+/* SSS300_ABI_VERSION of the loaded library. */
+int sss_abi_version(void);
+/* Map a device status word to an SSS_ERR_* code (and set the message). */
+int sss_status_code(int32_t device_status);
+
+/* ---------------------------------------------------------------------------
+ * Ray tracing.  Replaces RayTracing3DTOF (Python/openSSS/RayTracing3DTOF.py:29-180)
+ * and the MEX tracers Matlab/RayTracing3DTOF.cpp:51 (variant 0) and
+ * Matlab/RayTracing3D.cpp:51 (variant 1: float lengths, eps 1e-23, no samples),
+ * batched: ray i is lines[6*i .. 6*i+5] = x1 y1 z1 x2 y2 z2 (device, f64).
+ * Outputs are [n_rays][capacity] (device), capacity >= Nx+Ny+Nz:
+ *   counts[i]            voxels crossed (0 = miss, -1 = the reference would overrun)
+ *   lengths / lengths_f32  segment lengths (variant 0 / 1; the other may be NULL)
+ *   indices              1-based linear voxel indices, X + (Y-1)*Ny + (Z-1)*Ny*Nx
+ *   samples              running half-length samples (variant 0; may be NULL)
+ * A ray that overruns sets SSS_ERR_OVERRUN in *status. */
+int sss_raytrace(const int32_t grid[3], const double bounds[6], const double *lines,
+                 int64_t n_rays, int32_t variant, int32_t capacity, int32_t *counts,
+                 double *lengths, float *lengths_f32, int32_t *indices, double *samples,
+                 int32_t *status, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * TOF single scatter simulation.  Replaces SingleScatterSimulationTOF
+ * (Python/openSSS/SingleScatterSimulationTOF.py:36-208 with bodySSS :301-559).
+ * The non-TOF SingleScatterSimulation (Matlab/SingleScatterSimulation.m:44) is
+ * nbins = 1 with a TOF kernel wide enough that every weight is 1. */
+typedef struct sss_tof_problem {
+    int32_t nx, ny, nz;            /* volume shape */
+    const float *activity;         /* device, [nx*ny*nz] Fortran order (x fastest) */
+    const float *attenuation;      /* device, cm^-1, same layout */
+    double image_size[6];          /* xMin yMin zMin xMax yMax zMax, cm */
+    int32_t nr, nd;                /* scanner rings, crystals per ring */
+    const double *geometry;        /* device, [nr][nd][3] crystal centres, cm */
+    const double *normals;         /* device, [nr][nd][3] face normals */
+    double detector_size[2];       /* crystal face, mm */
+    int32_t nru, ndu;              /* sampled rings, sampled crystals per ring */
+    const int32_t *rings;          /* device, [nru] ring numbers (:153) */
+    const int32_t *detectors;      /* device, [ndu] crystal numbers (:159-167) */
+    int32_t sample_step[3];        /* scatter-point lattice step, voxels */
+    int32_t nbins;                 /* TOF bins, 1..64 */
+    double tof_bin_width;          /* ps, 2*TOFRange/NrBins */
+    double tof_resolution;         /* ps FWHM */
+    const float *tof_log2w;        /* device, [8001][2]: log2 of the largest normalised TOF
+                                      weight at offset t-4000 ps and its bin (as float);
+                                      -inf where the reference's column is all zero */
+    const float *efficiency;       /* device, [2000]: eff(E)*eff(511 keV); exact 0 where the
+                                      FP64 product is 0 (:505-509) */
+    const float *atten_ratio;      /* device, [2000]: water mu(E)/mu(511) (:117-120) */
+} sss_tof_problem;
+
+/* Scatter points on the SampleStep lattice with mu > 0, z-slice major, in the
+ * reference's order (:182, :381-394).  points (device) receives [count][4]
+ * (x, y, z, lattice z index) for up to `capacity` points; slice_counts (host,
+ * may be NULL) receives the number of points of each sampled z-slice
+ * (ceil(nz/step_z) entries).  Synchronises `stream`; *count (host) is the
+ * total even when it exceeds capacity (then SSS_ERR_CAPACITY). */
+int sss_scatter_points(const sss_tof_problem *p, double *points, int64_t capacity,
+                       int64_t *count, int64_t *slice_counts, void *stream);
+
+/* Bytes of device workspace sss_tof_run needs for waves of at most
+ * wave_points scatter points (a wave always holds whole z-slices). */
+size_t sss_tof_workspace_size(const sss_tof_problem *p, int64_t wave_points);
+
+/* Run the simulation for the points [0, n_points) (whole slices as given by
+ * slice_counts, host, n_slices entries).  out (device) receives the sampled
+ * scatter sinogram in leg-pair layout [nbins][NL][NL], NL = nru*ndu, leg
+ * l = ring_index*ndu + det_index: element [b][l1][l2] is the reference's
+ * Scatters[b, Radial, Angular, ri2 + ri1*nru] for the crystal pair
+ * (detectors[di1], detectors[di2]), defined for di1 < di2 and for di1 == di2
+ * with ri1 != ri2, zero elsewhere.  Asynchronous on `stream`. */
+int sss_tof_run(const sss_tof_problem *p, const double *points, int64_t n_points,
+                const int64_t *slice_counts, int64_t n_slices, int64_t wave_points,
+                void *workspace, size_t workspace_bytes, float *out, int32_t *status,
+                void *stream);
+
+/* Expand the leg-pair output to the reference's dense layout
+ * [nbins][nd+1][nd/2][nru*nru] (SingleScatterSimulationTOF.py:171).  lor
+ * (device) is LORCoordinates int16 [nd][nd][2] (Python/openSSS/Sinogram.py:121-122).
+ * dense must be zeroed by the caller. */
+int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
+                    const int16_t *lor, const int32_t *detectors, float *dense, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Stage timing (no reference counterpart: instrumentation for benchmarks).
+ * When enabled, sss_tof_run records CUDA events around its kernels on the
+ * caller's stream; sss_get_timing waits for them and returns, for the last
+ * run on this thread, out[0] = leg-stage ms, out[1] = pair-stage ms,
+ * out[2] = kernel launches, out[3] = waves, out[4] = TOF weights evaluated
+ * (voxel x bin), out[5] = detector pairs evaluated (all scatter points).
+ * The workspace of that run must still be alive. */
+void sss_set_timing(int enable);
+int sss_get_timing(double out[6]);
+
+/* Measured rate of the SFU 2^x instruction on the current device, in 1e9
+ * results/s (no reference counterpart: the roofline denominator of the pair
+ * stage).  Synchronises `stream`. */
+int sss_probe_ex2_rate(double *gex2_per_s, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SSS300_H */

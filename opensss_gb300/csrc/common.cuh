@@ -1,0 +1,41 @@
+// Shared definitions for the sm_103a TOF-SSS engine (libsss300.so).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sss300.h"
+
+namespace sss {
+
+// Device-side error bits, OR-ed into the caller's status word; the host maps
+// them to the SSS_ERR_* codes of sss300.h after the stream is synchronised.
+enum DeviceError : int32_t {
+    kErrOverrun = 1 << 0,    // traversal would pass Nx+Ny+Nz voxels (reference: IndexError)
+    kErrTofRange = 1 << 1,   // TOF table index above 8000 (reference: IndexError)
+    kErrEnergy = 1 << 2,     // scattered-energy row outside the 2000-row tables
+    kErrVoxel = 1 << 3,      // linear voxel index outside the volume (Nx != Ny case)
+    kErrCapacity = 1 << 4,   // an internal list capacity was exceeded
+};
+
+constexpr int kTofEntries = 8001;  // -4000..4000 ps, SingleScatterSimulationTOF.py:145-147
+constexpr int kTimeRange = 4000;
+
+__device__ __forceinline__ void raise_error(int32_t* status, int32_t bits)
+{
+    if (status) atomicOr(status, bits);
+}
+
+// 2^x with the SFU (ex2.approx.ftz.f32, max rel. error about 2^-22).
+__device__ __forceinline__ float ex2(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+}  // namespace sss
+
+// Host helpers shared by the entry points (defined in api.cu).
+int sss_set_error(int code, const char* fmt, ...);
+int sss_check_launch(const char* what);

@@ -1,0 +1,780 @@
+// Fused TOF single scatter simulation on sm_103a.
+//
+// Pipeline per wave of whole z-slices (reference: SingleScatterSimulationTOF.py
+// :82-208 and bodySSS :301-559):
+//   1. scatter_points_kernel — ordered lattice compaction of mu > 0 points.
+//   2. leg_kernel   — one thread per (scatter point, sampled crystal): FP64
+//      Amanatides-Woo walk (bit-identical voxel sequence), FP32 integrals of
+//      mu and activity, incidence term, and the activity-weighted voxel list
+//      (act*len, TOF sample offset) written voxel-major so that the 32 lanes
+//      of a warp read 32 neighbouring legs in one coalesced access.
+//   3. pair_kernel  — persistent warps pull (slice, leg-1, 32-leg-2 chunk)
+//      tasks; each lane owns one detector pair, loops over the slice's
+//      scatter points, evaluates the Klein-Nishina x efficiency x attenuation
+//      factors once per pair and the Gaussian TOF weights per voxel and bin
+//      with the SFU (2^x), accumulates the slice numerator and count in
+//      registers and adds numerator/count to the output (per-slice
+//      normalisation, :555-557).
+// Nothing per voxel or per pair reaches HBM except the leg lists themselves.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "trace.cuh"
+
+namespace {
+
+using namespace sss;
+
+constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
+constexpr int kMaxWaveSlices = 256;
+constexpr int kPairWarps = 8;  // warps per pair-kernel block
+
+struct LatticeDims {
+    int lx, ly, lz;     // lattice points per axis
+    int sx, sy, sz;     // steps
+};
+
+LatticeDims lattice(const sss_tof_problem& p)
+{
+    LatticeDims L;
+    L.sx = p.sample_step[0];
+    L.sy = p.sample_step[1];
+    L.sz = p.sample_step[2];
+    L.lx = (p.nx + L.sx - 1) / L.sx;
+    L.ly = (p.ny + L.sy - 1) / L.sy;
+    L.lz = (p.nz + L.sz - 1) / L.sz;
+    return L;
+}
+
+// ---------------------------------------------------------------- 1. points
+
+// Single block, 1024 threads: walks the lattice in the reference's order
+// (z, then y, then x: :182, :387, :391) in chunks of 1024, block-scans the
+// mu > 0 flags and writes the points in order.  Coordinates follow :176-179,
+// :381, :389, :394 in FP64.
+__global__ void __launch_bounds__(1024) scatter_points_kernel(
+    const float* __restrict__ mu, int nx, int ny, int nz, LatticeDims L, double radius,
+    double zstart, double zvox, double* __restrict__ out, int64_t capacity,
+    unsigned long long* __restrict__ total, unsigned long long* __restrict__ slice_counts)
+{
+    __shared__ int warp_sums[32];
+    __shared__ unsigned long long base;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) base = 0;
+    __syncthreads();
+    const long long npts = (long long)L.lx * L.ly * L.lz;
+    for (long long c0 = 0; c0 < npts; c0 += 1024) {
+        long long i = c0 + tid;
+        int flag = 0, ix = 0, iy = 0, iz = 0;
+        if (i < npts) {
+            ix = (int)(i % L.lx);
+            iy = (int)((i / L.lx) % L.ly);
+            iz = (int)(i / ((long long)L.lx * L.ly));
+            int x = ix * L.sx, y = iy * L.sy, z = iz * L.sz;
+            flag = mu[x + (long long)nx * (y + (long long)ny * z)] > 0.0f;
+        }
+        unsigned ball = __ballot_sync(0xffffffffu, flag);
+        int pre = __popc(ball & ((1u << lane) - 1u));
+        if (lane == 0) warp_sums[warp] = __popc(ball);
+        __syncthreads();
+        if (warp == 0) {
+            int v = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            warp_sums[lane] = v;  // inclusive
+        }
+        __syncthreads();
+        int wbase = warp ? warp_sums[warp - 1] : 0;
+        if (flag) {
+            unsigned long long pos = base + wbase + pre;
+            int x = ix * L.sx, y = iy * L.sy, z = iz * L.sz;
+            if ((long long)pos < capacity) {
+                double xs = sub64(div64(mul64((double)((x + 1) * 2), radius), (double)nx), radius);
+                double ys = sub64(div64(mul64((double)((y + 1) * 2), radius), (double)ny), radius);
+                double zs = add64(zstart, mul64((double)z, zvox));
+                out[4 * pos + 0] = xs;
+                out[4 * pos + 1] = ys;
+                out[4 * pos + 2] = zs;
+                out[4 * pos + 3] = (double)z;
+            }
+            atomicAdd(&slice_counts[iz], 1ull);
+        }
+        __syncthreads();
+        if (tid == 0) base += warp_sums[31];
+        __syncthreads();
+    }
+    if (tid == 0) *total = base;
+}
+
+// ---------------------------------------------------------------- 2. legs
+
+struct LegParams {
+    Grid g;
+    const float* act;
+    const float* mu;
+    const double* geom;
+    const double* normals;
+    const int32_t* rings;
+    const int32_t* dets;
+    int nd, nru, ndu, nl, cap;
+    long long nvox;
+    const double* points;  // wave's first point, [n][4]
+    int npts;
+    float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
+    float4* legB;   // [npts][nl]: unit vector to the crystal, voxel-list length (int bits)
+    float2* vox;    // [npts][cap][nl]: act*len, 2*sample/c (ps)
+    int32_t* status;
+};
+
+__global__ void __launch_bounds__(128) leg_kernel(LegParams P)
+{
+    long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)P.npts * P.nl) return;
+    const int s = (int)(gid / P.nl), l = (int)(gid % P.nl);
+    const int ri = l / P.ndu, di = l % P.ndu;
+    const int ring = P.rings[ri], det = P.dets[di];
+    const double* dp = P.geom + 3 * ((long long)ring * P.nd + det);
+    const double zD = P.geom[3 * ((long long)ring * P.nd) + 2];  // :402 (crystal 0's z)
+    const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
+    double lc[6] = {xS, yS, zS, dp[0], dp[1], zD};
+
+    // incidence angle term |cos a| (:424-430, :533-535) and distance (:442-444)
+    const double vx = dp[0] - xS, vy = dp[1] - yS, vz = zD - zS;
+    const double* nv = P.normals + 3 * ((long long)ring * P.nd + det);
+    const double vn = sqrt(vx * vx + vy * vy + vz * vz);
+    const double nn = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+    const double cosa = fabs((vx * nv[0] + vy * nv[1] + vz * nv[2]) / (nn * vn));
+    const float sv = (float)vn;
+
+    float asum = 0.f, musum = 0.f;
+    int nlist = 0;
+    Ray r;
+    if (ray_setup(P.g, lc, 1e-20, r)) {
+        const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
+        const float inv_c = (float)(1.0 / kLightCmPerPs);
+        const double t0 = r.tmin;
+        float2* out = P.vox + (long long)s * P.cap * P.nl + l;
+        int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
+            long long v = lin - 1;
+            if (v < 0 || v >= P.nvox) {
+                raise_error(P.status, kErrVoxel);
+                return;
+            }
+            float len = vlen * (float)(tb - ta);
+            float a = __ldg(P.act + v) * len;
+            musum = fmaf(__ldg(P.mu + v), len, musum);
+            asum += a;
+            if (a != 0.f) {
+                // sample = half the distance walked to the voxel's exit (:155-156)
+                float rho = vlen * (float)(tb - t0) * inv_c;
+                out[(long long)nlist * P.nl] = make_float2(a, rho);
+                ++nlist;
+            }
+        });
+        if (c < 0) raise_error(P.status, kErrOverrun);
+    }
+    const long long o = (long long)s * P.nl + l;
+    // exp(-I) underflows to 0 in FP64 above ~745.13 (the skip at :451 / :483)
+    const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
+    P.legA[o] = make_float4(sv, asum, ilog2, (float)(cosa / (vn * vn)));
+    const float inv = (float)(1.0 / vn);
+    P.legB[o] = make_float4((float)vx * inv, (float)vy * inv, (float)vz * inv,
+                            __int_as_float(nlist));
+}
+
+// ---------------------------------------------------------------- 3. pairs
+
+struct PairParams {
+    int nru, ndu, nl, nd, cap;
+    int nbins;
+    float s0, w;            // first bin centre offset (ps) and bin width (ps)
+    float kappa2w, gamma;   // 2*kappa*w and kappa*w^2, kappa = 4/R^2 (log2 units)
+    float geo_c;            // (ds0*ds1*1e-2)^2 / (4 pi)
+    float gamma_kn;         // E/(m_e c^2) of the reference's KleinNishina
+    const float* tof_log2w; // [8001][2]
+    const float* eff;       // [2000]
+    const float* ratio;     // [2000]
+    const double* geom;
+    const int32_t* rings;
+    const int32_t* dets;
+    const double* points;   // wave's first point
+    const float4* legA;
+    const float4* legB;
+    const float2* vox;
+    const int2* chunks;     // (l1, chunk) per chunk task
+    int nchunks;
+    int nslices;
+    int slice_first[kMaxWaveSlices];   // first point of slice j within the wave
+    int slice_count[kMaxWaveSlices];
+    unsigned int* counter;
+    unsigned long long* work;  // [0] voxel lists walked per pair, [1] pairs evaluated
+    float* out;             // [nbins][nl][nl]
+    int32_t* status;
+};
+
+// Energy row of a pair exactly as the reference computes it in FP64
+// (:442-444, :474-475, :495-501), used when the FP32 estimate lies within
+// 1e-3 keV of a rounding boundary.
+__device__ __noinline__ int energy_row_fp64(const PairParams& P, int s, int ri1, int di1, int ri2,
+                                            int di2)
+{
+    const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
+    const int r1 = P.rings[ri1], r2 = P.rings[ri2], d1 = P.dets[di1], d2 = P.dets[di2];
+    const double* p1 = P.geom + 3 * ((long long)r1 * P.nd + d1);
+    const double* p2 = P.geom + 3 * ((long long)r2 * P.nd + d2);
+    const double z1 = P.geom[3 * ((long long)r1 * P.nd) + 2];
+    const double z2 = P.geom[3 * ((long long)r2 * P.nd) + 2];
+    double sv1 = __dsqrt_rn(add64(add64(mul64(sub64(p1[0], xS), sub64(p1[0], xS)),
+                                      mul64(sub64(p1[1], yS), sub64(p1[1], yS))),
+                                 mul64(sub64(z1, zS), sub64(z1, zS))));
+    double sv2 = __dsqrt_rn(add64(add64(mul64(sub64(p2[0], xS), sub64(p2[0], xS)),
+                                      mul64(sub64(p2[1], yS), sub64(p2[1], yS))),
+                                 mul64(sub64(z2, zS), sub64(z2, zS))));
+    double lor = add64(add64(mul64(sub64(p1[0], p2[0]), sub64(p1[0], p2[0])),
+                           mul64(sub64(p1[1], p2[1]), sub64(p1[1], p2[1]))),
+                      mul64(sub64(z1, z2), sub64(z1, z2)));
+    double a = mul64(sv1, sv1), b = mul64(sv2, sv2);
+    double q = div64(sub64(add64(a, b), lor), mul64(2.0, __dsqrt_rn(mul64(a, b))));
+    double th = sub64(180.0, mul64(acos(q), 180.0 / 3.141592653589793));
+    double cth = cos(mul64(th, 3.141592653589793 / 180.0));
+    double es = floor(add64(div64(511.0, add64(1.0, mul64(1.0, sub64(1.0, cth)))), 0.5));
+    return (int)mul64(es, 2.0) - 1;
+}
+
+template <int BP>
+__device__ __forceinline__ void accumulate_voxel(float (&acc)[BP], int nbins, float ca, float x,
+                                                 const float* sY, const unsigned char* sN,
+                                                 const PairParams& P, bool& tof_bad)
+{
+    // t = floor(x) with x in [-2^22, 2^22]: round-down add of 1.5*2^23
+    float y = __fadd_rd(x, 12582912.0f);
+    int t = __float_as_int(y) - 0x4B400000;
+    if (t < 0) t += kTofEntries;  // numpy negative index wraps (:521, :527)
+    if ((unsigned)t >= (unsigned)kTofEntries) {
+        tof_bad = true;
+        return;
+    }
+    const float Y = sY[t];
+    const float n = (float)sN[t];
+    const float off = (float)(t - kTimeRange);
+    const float delta = off - fmaf(n, P.w, P.s0);
+    const float beta = P.kappa2w * delta;
+#pragma unroll
+    for (int b = 0; b < BP; ++b) {
+        if (b < nbins) {
+            const float d = n - (float)b;
+            const float e = fmaf(-d, fmaf(P.gamma, d, beta), Y);
+            acc[b] = fmaf(ca, ex2(e), acc[b]);
+        }
+    }
+}
+
+template <int BP>
+__global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_constant__ PairParams P)
+{
+    extern __shared__ float smem[];
+    float* sY = smem;
+    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
+    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
+        sY[i] = P.tof_log2w[2 * i];
+        sN[i] = (unsigned char)P.tof_log2w[2 * i + 1];
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const long long ntasks = (long long)P.nslices * P.nchunks;
+    const float inv_c = (float)(1.0 / kLightCmPerPs);
+    bool tof_bad = false, energy_bad = false;
+    unsigned long long walked = 0, npairs = 0;
+
+    for (;;) {
+        long long task = 0;
+        if (lane == 0) task = atomicAdd(P.counter, 1u);
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= ntasks) break;
+        const int slice = (int)(task / P.nchunks);
+        const int2 ch = P.chunks[task % P.nchunks];
+        const int l1 = ch.x;
+        const int ri1 = l1 / P.ndu, di1 = l1 % P.ndu;
+        // valid second legs of l1 in order: rings ri2 < ri1 with di2 >= di1,
+        // ring ri1 with di2 > di1, rings ri2 > ri1 with di2 >= di1 (:464-470)
+        const int m = P.ndu - di1;
+        const int nvalid = P.nru * m - 1;
+        const int q = ch.y * 32 + lane;
+        const bool lane_ok = q < nvalid;
+        int ri2, di2;
+        if (q < ri1 * m) {
+            ri2 = q / m;
+            di2 = di1 + q % m;
+        } else if (q < ri1 * m + m - 1) {
+            ri2 = ri1;
+            di2 = di1 + 1 + (q - ri1 * m);
+        } else {
+            const int q2 = q - ri1 * m - (m - 1);
+            ri2 = ri1 + 1 + q2 / m;
+            di2 = di1 + q2 % m;
+        }
+        const int l2 = lane_ok ? ri2 * P.ndu + di2 : l1;
+
+        float acc[BP];
+#pragma unroll
+        for (int b = 0; b < BP; ++b) acc[b] = 0.f;
+        float cnt = 0.f;
+
+        const int sfirst = P.slice_first[slice], scount = P.slice_count[slice];
+        for (int s = sfirst; s < sfirst + scount; ++s) {
+            const long long lo = (long long)s * P.nl;
+            const float4 A1 = P.legA[lo + l1], B1 = P.legB[lo + l1];
+            const float4 A2 = P.legA[lo + l2], B2 = P.legB[lo + l2];
+            bool ok = lane_ok && A1.z != INFINITY && A2.z != INFINITY &&
+                      !(A1.y == 0.f && A2.y == 0.f);
+            float c1 = 0.f, c2 = 0.f;
+            if (ok) {
+                // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
+                float qc = fmaf(B1.x, B2.x, fmaf(B1.y, B2.y, B1.z * B2.z));
+                qc = fminf(1.f, fmaxf(-1.f, qc));
+                const float e = 511.0f / (2.0f + qc);
+                const float eh = e + 0.5f;
+                const float fr = eh - floorf(eh);
+                int row;
+                if (fr < 1e-3f || fr > 1.0f - 1e-3f)
+                    row = energy_row_fp64(P, sfirst + (s - sfirst), ri1, di1, ri2, di2);
+                else
+                    row = 2 * (int)floorf(eh) - 1;
+                if (row < 0 || row >= 2000) {
+                    energy_bad = true;
+                    ok = false;
+                } else {
+                    const float effp = __ldg(P.eff + row);
+                    if (effp == 0.f) {
+                        ok = false;  // :508-509 (before the count is added)
+                    } else {
+                        const float rr = __ldg(P.ratio + row);
+                        // Klein-Nishina with cos(theta) = -qc (:239-258)
+                        const float ratio = 1.0f / (1.0f + P.gamma_kn * (1.0f + qc));
+                        const float sin2 = 1.0f - qc * qc;
+                        const float kn = ratio * ratio * (ratio + 1.0f / ratio - sin2);
+                        // geometry (:533-536): (ds)^2 |cos a1||cos a2| / (4 pi sv1^2 sv2^2)
+                        const float f = P.geo_c * A1.w * A2.w * effp * kn;
+                        const float m1 = ex2(-A1.z), m2 = ex2(-A2.z);
+                        const float m1r = ex2(-rr * A1.z), m2r = ex2(-rr * A2.z);
+                        if (A1.y != 0.f) c1 = f * m1 * m2r;  // :540
+                        if (A2.y != 0.f) c2 = f * m2 * m1r;
+                        cnt += (A1.y != 0.f && A2.y != 0.f) ? 2.f : 1.f;  // :485-488
+                        npairs += 1;
+                        walked += (c1 != 0.f ? __float_as_int(B1.w) : 0) +
+                                  (c2 != 0.f ? __float_as_int(B2.w) : 0);
+                    }
+                }
+            }
+            // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
+            const float u = fmaf(A1.x - A2.x, inv_c, 4000.5f);
+            const float2* v1 = P.vox + (long long)s * P.cap * P.nl + l1;
+            if (__any_sync(0xffffffffu, c1 != 0.f)) {
+                const int n1 = __float_as_int(B1.w);
+                for (int k = 0; k < n1; ++k) {
+                    const float2 v = v1[(long long)k * P.nl];
+                    if (c1 != 0.f)
+                        accumulate_voxel<BP>(acc, P.nbins, c1 * v.x, u - v.y, sY, sN, P, tof_bad);
+                }
+            }
+            const int n2 = c2 != 0.f ? __float_as_int(B2.w) : 0;
+            const int n2max = __reduce_max_sync(0xffffffffu, n2);
+            const float2* v2 = P.vox + (long long)s * P.cap * P.nl + l2;
+            for (int k = 0; k < n2max; ++k) {
+                if (k < n2) {
+                    const float2 v = v2[(long long)k * P.nl];
+                    accumulate_voxel<BP>(acc, P.nbins, c2 * v.x, u + v.y, sY, sN, P, tof_bad);
+                }
+            }
+        }
+        if (lane_ok && cnt > 0.f) {
+            float* o = P.out + (long long)l1 * P.nl + l2;
+            const long long plane = (long long)P.nl * P.nl;
+#pragma unroll
+            for (int b = 0; b < BP; ++b)
+                if (b < P.nbins) atomicAdd(o + b * plane, acc[b] / cnt);
+        }
+    }
+    if (tof_bad) raise_error(P.status, kErrTofRange);
+    if (energy_bad) raise_error(P.status, kErrEnergy);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        walked += __shfl_xor_sync(0xffffffffu, walked, o);
+        npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
+    }
+    if (lane == 0 && P.work) {
+        atomicAdd(P.work, walked);
+        atomicAdd(P.work + 1, npairs);
+    }
+}
+
+template <int BP>
+int launch_pairs(const PairParams& P, cudaStream_t st)
+{
+    const size_t smem = kTofEntries * sizeof(float) + kTofEntries;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(pair_kernel<BP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr_set = true;
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pair_kernel<BP>, kPairWarps * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    long long ntasks = (long long)P.nslices * P.nchunks;
+    long long blocks = std::min<long long>((long long)sms * per_sm,
+                                           (ntasks + kPairWarps - 1) / kPairWarps);
+    if (blocks < 1) blocks = 1;
+    pair_kernel<BP><<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(P);
+    return sss_check_launch("pair_kernel");
+}
+
+int dispatch_pairs(const PairParams& P, cudaStream_t st)
+{
+    const int b = P.nbins;
+    if (b <= 1) return launch_pairs<1>(P, st);
+    if (b <= 8) return launch_pairs<8>(P, st);
+    if (b <= 16) return launch_pairs<16>(P, st);
+    if (b <= 24) return launch_pairs<24>(P, st);
+    if (b <= 40) return launch_pairs<40>(P, st);
+    return launch_pairs<64>(P, st);
+}
+
+// ---------------------------------------------------------------- densify
+
+__global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, int nd,
+                               const int16_t* __restrict__ lor, const int32_t* __restrict__ dets,
+                               float* __restrict__ dense)
+{
+    const int nl = nru * ndu;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)nbins * nl * nl;
+    if (i >= total) return;
+    const int l2 = (int)(i % nl);
+    const int l1 = (int)((i / nl) % nl);
+    const int b = (int)(i / ((long long)nl * nl));
+    const int ri1 = l1 / ndu, di1 = l1 % ndu, ri2 = l2 / ndu, di2 = l2 % ndu;
+    if (di1 > di2 || (di1 == di2 && ri1 == ri2)) return;
+    const int d1 = dets[di1], d2 = dets[di2];
+    const int ang = lor[2 * ((long long)d1 * nd + d2)];
+    const int rad = lor[2 * ((long long)d1 * nd + d2) + 1];
+    const int nang = nd / 2, nsino = nru * nru;
+    dense[(((long long)b * (nd + 1) + rad) * nang + ang) * nsino + ri2 + ri1 * nru] = cmp[i];
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Optional stage timing (events recorded on the caller's stream).
+struct StageTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;  // pairs: leg start/end, pair start/end per wave
+    int launches = 0, waves = 0, nbins = 0;
+    const unsigned long long* work = nullptr;  // device counters of the last run
+    cudaEvent_t get()
+    {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ev.push_back(e);
+        return e;
+    }
+    void clear()
+    {
+        for (auto e : ev) cudaEventDestroy(e);
+        ev.clear();
+        launches = waves = 0;
+    }
+};
+thread_local StageTimer g_timer;
+
+struct WsLayout {
+    size_t legA, legB, vox, chunks, counter, total;
+};
+
+WsLayout ws_layout(const sss_tof_problem& p, long long wave_points, long long nchunks)
+{
+    const long long nl = (long long)p.nru * p.ndu;
+    const long long cap = (long long)p.nx + p.ny + p.nz;
+    WsLayout w;
+    size_t off = 0;
+    w.legA = off;
+    off = align_up(off + sizeof(float4) * wave_points * nl);
+    w.legB = off;
+    off = align_up(off + sizeof(float4) * wave_points * nl);
+    w.vox = off;
+    off = align_up(off + sizeof(float2) * wave_points * cap * nl);
+    w.chunks = off;
+    off = align_up(off + sizeof(int2) * nchunks);
+    w.counter = off;
+    off = align_up(off + 256);
+    w.total = off;
+    return w;
+}
+
+long long chunk_count(const sss_tof_problem& p)
+{
+    long long n = 0;
+    for (int di1 = 0; di1 < p.ndu; ++di1) {
+        long long nvalid = (long long)p.nru * (p.ndu - di1) - 1;
+        n += (long long)p.nru * ((nvalid + 31) / 32);
+    }
+    return n;
+}
+
+int validate(const sss_tof_problem* p)
+{
+    if (!p) return sss_set_error(SSS_ERR_INVALID, "null problem");
+    if (p->nx < 1 || p->ny < 1 || p->nz < 1) return sss_set_error(SSS_ERR_INVALID, "bad volume shape");
+    if (!p->activity || !p->attenuation || !p->geometry || !p->normals || !p->rings ||
+        !p->detectors || !p->tof_log2w || !p->efficiency || !p->atten_ratio)
+        return sss_set_error(SSS_ERR_INVALID, "null array in problem");
+    if (p->nr < 1 || p->nd < 2 || p->nru < 1 || p->ndu < 1 || p->nru > p->nr || p->ndu > p->nd)
+        return sss_set_error(SSS_ERR_INVALID, "bad scanner / sampling sizes");
+    if (p->sample_step[0] < 1 || p->sample_step[1] < 1 || p->sample_step[2] < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sample_step must be >= 1");
+    if (p->nbins < 1 || p->nbins > 64) return sss_set_error(SSS_ERR_INVALID, "nbins must be 1..64");
+    if (!(p->image_size[3] > p->image_size[0] && p->image_size[4] > p->image_size[1] &&
+          p->image_size[5] > p->image_size[2]))
+        return sss_set_error(SSS_ERR_INVALID, "image_size must satisfy max > min");
+    long long nl = (long long)p->nru * p->ndu;
+    if (nl * nl * p->nbins > (1ll << 40)) return sss_set_error(SSS_ERR_INVALID, "output too large");
+    return SSS_OK;
+}
+
+}  // namespace
+
+extern "C" int sss_scatter_points(const sss_tof_problem* p, double* points, int64_t capacity,
+                                  int64_t* count, int64_t* slice_counts, void* stream)
+{
+    int rc = validate(p);
+    if (rc) return rc;
+    if (!count) return sss_set_error(SSS_ERR_INVALID, "sss_scatter_points: null count");
+    if (capacity > 0 && !points) return sss_set_error(SSS_ERR_INVALID, "sss_scatter_points: null points");
+    cudaStream_t st = (cudaStream_t)stream;
+    LatticeDims L = lattice(*p);
+    const double* IS = p->image_size;
+    double zvox = (IS[5] - IS[2]) / p->nz;  // :87
+    double zstart = zvox / 2 - (-IS[2]);    // :176, :179
+    double radius = -IS[0];                 // :177
+    unsigned long long* dbuf = nullptr;
+    size_t nbuf = 1 + (size_t)L.lz;
+    if (cudaMallocAsync(&dbuf, nbuf * sizeof(unsigned long long), st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_scatter_points: allocation failed");
+    cudaMemsetAsync(dbuf, 0, nbuf * sizeof(unsigned long long), st);
+    scatter_points_kernel<<<1, 1024, 0, st>>>(p->attenuation, p->nx, p->ny, p->nz, L, radius,
+                                               zstart, zvox, points, capacity, dbuf, dbuf + 1);
+    rc = sss_check_launch("scatter_points_kernel");
+    std::vector<unsigned long long> h(nbuf);
+    if (!rc && cudaMemcpyAsync(h.data(), dbuf, nbuf * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        rc = sss_set_error(SSS_ERR_CUDA, "sss_scatter_points: copy failed");
+    cudaFreeAsync(dbuf, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && !rc)
+        rc = sss_set_error(SSS_ERR_CUDA, "sss_scatter_points: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc) return rc;
+    *count = (int64_t)h[0];
+    if (slice_counts)
+        for (int i = 0; i < L.lz; ++i) slice_counts[i] = (int64_t)h[1 + i];
+    if ((int64_t)h[0] > capacity)
+        return sss_set_error(SSS_ERR_CAPACITY, "sss_scatter_points: %lld points > capacity %lld",
+                             (long long)h[0], (long long)capacity);
+    return SSS_OK;
+}
+
+extern "C" size_t sss_tof_workspace_size(const sss_tof_problem* p, int64_t wave_points)
+{
+    if (validate(p)) return 0;
+    return ws_layout(*p, wave_points, chunk_count(*p)).total;
+}
+
+extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64_t n_points,
+                           const int64_t* slice_counts, int64_t n_slices, int64_t wave_points,
+                           void* workspace, size_t workspace_bytes, float* out, int32_t* status,
+                           void* stream)
+{
+    int rc = validate(p);
+    if (rc) return rc;
+    if (!out || (n_points > 0 && (!points || !slice_counts)))
+        return sss_set_error(SSS_ERR_INVALID, "sss_tof_run: null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long nl = (long long)p->nru * p->ndu;
+    const long long cap = (long long)p->nx + p->ny + p->nz;
+    const long long nchunks = chunk_count(*p);
+    long long maxslice = 0, tot = 0;
+    for (int64_t i = 0; i < n_slices; ++i) {
+        maxslice = std::max<long long>(maxslice, slice_counts[i]);
+        tot += slice_counts[i];
+    }
+    if (tot != n_points) return sss_set_error(SSS_ERR_INVALID, "slice_counts do not sum to n_points");
+    if (wave_points < maxslice)
+        return sss_set_error(SSS_ERR_INVALID, "wave_points %lld < largest slice %lld",
+                             (long long)wave_points, maxslice);
+    WsLayout w = ws_layout(*p, wave_points, nchunks);
+    if (!workspace || workspace_bytes < w.total)
+        return sss_set_error(SSS_ERR_WORKSPACE, "sss_tof_run: workspace %zu < %zu bytes",
+                             workspace_bytes, w.total);
+    char* ws = (char*)workspace;
+    if (cudaMemsetAsync(out, 0, sizeof(float) * p->nbins * nl * nl, st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_tof_run: memset failed");
+    if (n_points == 0) return SSS_OK;
+
+    // chunk table (l1, chunk), l1-major
+    std::vector<int2> chunks;
+    chunks.reserve(nchunks);
+    for (int l1 = 0; l1 < nl; ++l1) {
+        int di1 = l1 % p->ndu;
+        long long nvalid = (long long)p->nru * (p->ndu - di1) - 1;
+        for (int c = 0; c < (nvalid + 31) / 32; ++c) chunks.push_back(make_int2(l1, c));
+    }
+    if (cudaMemcpyAsync(ws + w.chunks, chunks.data(), sizeof(int2) * chunks.size(),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_tof_run: chunk upload failed");
+
+    LegParams LP;
+    LP.g.nx = p->nx;
+    LP.g.ny = p->ny;
+    LP.g.nz = p->nz;
+    for (int k = 0; k < 6; ++k) LP.g.b[k] = p->image_size[k];
+    LP.act = p->activity;
+    LP.mu = p->attenuation;
+    LP.geom = p->geometry;
+    LP.normals = p->normals;
+    LP.rings = p->rings;
+    LP.dets = p->detectors;
+    LP.nd = p->nd;
+    LP.nru = p->nru;
+    LP.ndu = p->ndu;
+    LP.nl = (int)nl;
+    LP.cap = (int)cap;
+    LP.nvox = (long long)p->nx * p->ny * p->nz;
+    LP.legA = (float4*)(ws + w.legA);
+    LP.legB = (float4*)(ws + w.legB);
+    LP.vox = (float2*)(ws + w.vox);
+    LP.status = status;
+
+    PairParams PP;
+    PP.nru = p->nru;
+    PP.ndu = p->ndu;
+    PP.nl = (int)nl;
+    PP.nd = p->nd;
+    PP.cap = (int)cap;
+    PP.nbins = p->nbins;
+    const double wbin = p->tof_bin_width;
+    const double kappa = 4.0 / (p->tof_resolution * p->tof_resolution);
+    PP.s0 = (float)((1.0 - (p->nbins + 1) / 2.0) * wbin);  // :282
+    PP.w = (float)wbin;
+    PP.kappa2w = (float)(2.0 * kappa * wbin);
+    PP.gamma = (float)(kappa * wbin * wbin);
+    const double ds = p->detector_size[0] * p->detector_size[1] * 1e-2;
+    PP.geo_c = (float)(ds * ds / (4.0 * 3.141592653589793));
+    PP.gamma_kn = (float)(511.0E3 * 1.6E-19 / (9.10938356E-31 * (299792458.0 * 299792458.0)));
+    PP.tof_log2w = p->tof_log2w;
+    PP.eff = p->efficiency;
+    PP.ratio = p->atten_ratio;
+    PP.geom = p->geometry;
+    PP.rings = p->rings;
+    PP.dets = p->detectors;
+    PP.legA = LP.legA;
+    PP.legB = LP.legB;
+    PP.vox = LP.vox;
+    PP.chunks = (const int2*)(ws + w.chunks);
+    PP.nchunks = (int)nchunks;
+    PP.counter = (unsigned int*)(ws + w.counter);
+    PP.work = (unsigned long long*)(ws + w.counter + 8);
+    PP.out = out;
+    cudaMemsetAsync(ws + w.counter, 0, 256, st);
+    PP.status = status;
+
+    g_timer.clear();
+    g_timer.work = PP.work;
+    g_timer.nbins = p->nbins;
+    // waves of whole slices
+    long long first = 0;
+    int64_t si = 0;
+    while (si < n_slices) {
+        long long npts = 0;
+        int nsl = 0;
+        PP.nslices = 0;
+        while (si < n_slices && nsl < kMaxWaveSlices && npts + slice_counts[si] <= wave_points) {
+            if (slice_counts[si] > 0) {
+                PP.slice_first[PP.nslices] = (int)npts;
+                PP.slice_count[PP.nslices] = (int)slice_counts[si];
+                PP.nslices++;
+            }
+            npts += slice_counts[si];
+            ++nsl;
+            ++si;
+        }
+        if (npts > 0) {
+            LP.points = points + 4 * first;
+            LP.npts = (int)npts;
+            long long threads = npts * nl;
+            if (g_timer.on) cudaEventRecord(g_timer.get(), st);
+            leg_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(LP);
+            if ((rc = sss_check_launch("leg_kernel"))) return rc;
+            if (g_timer.on) cudaEventRecord(g_timer.get(), st);
+            PP.points = LP.points;
+            cudaMemsetAsync(PP.counter, 0, sizeof(unsigned int), st);
+            if (g_timer.on) cudaEventRecord(g_timer.get(), st);
+            if ((rc = dispatch_pairs(PP, st))) return rc;
+            if (g_timer.on) cudaEventRecord(g_timer.get(), st);
+            g_timer.launches += 2;
+            g_timer.waves += 1;
+        }
+        first += npts;
+    }
+    return SSS_OK;
+}
+
+extern "C" void sss_set_timing(int enable)
+{
+    g_timer.clear();
+    g_timer.work = nullptr;
+    g_timer.on = enable != 0;
+}
+
+extern "C" int sss_get_timing(double out[6])
+{
+    if (!out) return sss_set_error(SSS_ERR_INVALID, "sss_get_timing: null output");
+    double leg = 0, pair = 0;
+    for (size_t i = 0; i + 3 < g_timer.ev.size(); i += 4) {
+        float a = 0, b = 0;
+        if (cudaEventSynchronize(g_timer.ev[i + 3]) != cudaSuccess ||
+            cudaEventElapsedTime(&a, g_timer.ev[i], g_timer.ev[i + 1]) != cudaSuccess ||
+            cudaEventElapsedTime(&b, g_timer.ev[i + 2], g_timer.ev[i + 3]) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_get_timing: event query failed");
+        leg += a;
+        pair += b;
+    }
+    out[0] = leg;
+    out[1] = pair;
+    out[2] = g_timer.launches;
+    out[3] = g_timer.waves;
+    unsigned long long h[2] = {0, 0};
+    if (g_timer.work && g_timer.on) {
+        if (cudaMemcpy(h, g_timer.work, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_get_timing: counter copy failed");
+    }
+    out[4] = (double)h[0] * g_timer.nbins;  // 2^x evaluations (voxel x bin)
+    out[5] = (double)h[1];                  // detector-pair evaluations
+    return SSS_OK;
+}
+
+extern "C" int sss_tof_densify(const float* compact, int32_t nbins, int32_t nru, int32_t ndu,
+                               int32_t nd, const int16_t* lor, const int32_t* detectors,
+                               float* dense, void* stream)
+{
+    if (!compact || !lor || !detectors || !dense || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
+        return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify: bad argument");
+    long long nl = (long long)nru * ndu;
+    long long total = (long long)nbins * nl * nl;
+    densify_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        compact, nbins, nru, ndu, nd, lor, detectors, dense);
+    return sss_check_launch("densify_kernel");
+}

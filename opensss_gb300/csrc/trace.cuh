@@ -1,0 +1,188 @@
+// Amanatides-Woo voxel traversal in IEEE FP64, operation for operation as in
+// the reference tracer (Python/openSSS/RayTracing3DTOF.py:29-180 with
+// BoxIntersectTest :204-269; Matlab/RayTracing3DTOF.cpp:51-341).  Every FP64
+// operation is an explicit round-to-nearest intrinsic, so no multiply-add is
+// fused whatever the compile flags, and the voxel sequence is bit-identical
+// to the reference's.
+#pragma once
+
+#include "common.cuh"
+
+namespace sss {
+
+__device__ __forceinline__ double mul64(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add64(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub64(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double div64(double a, double b) { return __ddiv_rn(a, b); }
+// Python's built-in min/max: the first argument wins unless the second
+// compares strictly smaller / larger (RayTracing3DTOF.py:53-54, 77-78).
+__device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double pymax(double a, double b) { return (b > a) ? b : a; }
+
+struct Grid {
+    int nx, ny, nz;
+    double b[6];  // xMin yMin zMin xMax yMax zMax
+};
+
+// Parametric state of one ray after set-up.
+struct Ray {
+    double tmin, tmax;
+    double xv, yv, zv;          // direction (end - start)
+    double xt, yt, zt;          // next crossing parameter per axis
+    double xd, yd, zd;          // parametric step per axis
+    int X, Y, Z;                // current voxel, 1-based
+    int xe, ye, ze;             // final voxel, 1-based
+    int xs, ys, zs;             // step directions
+};
+
+// BoxIntersectTest; eps = 1e-20 (RayTracing3DTOF.py:225) or 1e-23 for the
+// non-TOF MEX variant (Matlab/RayTracing3D.cpp:267).
+__device__ __forceinline__ bool box_intersect(const Grid& g, const double* lc, double eps,
+                                              double& rtmin, double& rtmax)
+{
+    double tmin, tmax, a, b;
+    double xdiv = div64(1.0, add64(sub64(lc[3], lc[0]), eps));
+    if (xdiv >= 0) {
+        tmin = mul64(sub64(g.b[0], lc[0]), xdiv);
+        tmax = mul64(sub64(g.b[3], lc[0]), xdiv);
+    } else {
+        tmin = mul64(sub64(g.b[3], lc[0]), xdiv);
+        tmax = mul64(sub64(g.b[0], lc[0]), xdiv);
+    }
+    double ydiv = div64(1.0, add64(sub64(lc[4], lc[1]), eps));
+    if (ydiv >= 0) {
+        a = mul64(sub64(g.b[1], lc[1]), ydiv);
+        b = mul64(sub64(g.b[4], lc[1]), ydiv);
+    } else {
+        a = mul64(sub64(g.b[4], lc[1]), ydiv);
+        b = mul64(sub64(g.b[1], lc[1]), ydiv);
+    }
+    if (tmin > b || a > tmax) return false;
+    if (a > tmin) tmin = a;
+    if (b < tmax) tmax = b;
+    double zdiv = div64(1.0, add64(sub64(lc[5], lc[2]), eps));
+    if (zdiv >= 0) {
+        a = mul64(sub64(g.b[2], lc[2]), zdiv);
+        b = mul64(sub64(g.b[5], lc[2]), zdiv);
+    } else {
+        a = mul64(sub64(g.b[5], lc[2]), zdiv);
+        b = mul64(sub64(g.b[2], lc[2]), zdiv);
+    }
+    if (tmin > b || a > tmax) return false;
+    if (a > tmin) tmin = a;
+    if (b < tmax) tmax = b;
+    if ((tmin >= 1 && tmax >= 1) || (tmin <= 0 && tmax <= 0)) return false;
+    rtmin = tmin;
+    rtmax = tmax;
+    return true;
+}
+
+// Per-axis set-up (RayTracing3DTOF.py:77-123).  `start`/`end` are the grid
+// entry/exit coordinates, n the voxel count on the axis.
+__device__ __forceinline__ void axis_setup(double lo, double vs, double n, double v,
+                                           double start, double end, double tmin, double tmax,
+                                           bool int_first, int& X, int& Xe, int& st, double& tn,
+                                           double& td)
+{
+    double c0 = ceil(div64(sub64(start, lo), vs));
+    double c1 = ceil(div64(sub64(end, lo), vs));
+    double x, xe;
+    if (!int_first) {
+        x = pymax(1.0, pymin(n, c0));
+        xe = pymax(1.0, pymin(n, c1));
+    } else {  // z: int() before the clamp (RayTracing3DTOF.py:109-110)
+        x = pymin(pymax(1.0, c0), n);
+        xe = pymin(pymax(1.0, c1), n);
+    }
+    if (v > 0) {
+        st = 1;
+        td = div64(vs, v);
+        tn = add64(tmin, div64(sub64(add64(lo, mul64(x, vs)), start), v));
+    } else if (v < 0) {
+        st = -1;
+        td = div64(vs, -v);
+        tn = add64(tmin, div64(sub64(add64(lo, mul64(sub64(x, 1.0), vs)), start), v));
+    } else {
+        st = 0;
+        tn = tmax;
+        td = tmax;
+    }
+    X = (int)x;
+    Xe = (int)xe;
+}
+
+// Ray set-up; returns false on a miss (the reference returns empty arrays).
+__device__ __forceinline__ bool ray_setup(const Grid& g, const double* lc, double eps, Ray& r)
+{
+    double tmin, tmax;
+    if (!box_intersect(g, lc, eps, tmin, tmax)) return false;
+    tmin = pymax(tmin, 0.0);
+    tmax = pymin(tmax, 1.0);
+    const double nx = (double)g.nx, ny = (double)g.ny, nz = (double)g.nz;
+    double vx = div64(sub64(g.b[3], g.b[0]), nx);
+    double vy = div64(sub64(g.b[4], g.b[1]), ny);
+    double vz = div64(sub64(g.b[5], g.b[2]), nz);
+    r.xv = sub64(lc[3], lc[0]);
+    r.yv = sub64(lc[4], lc[1]);
+    r.zv = sub64(lc[5], lc[2]);
+    double xs = add64(lc[0], mul64(r.xv, tmin)), ys = add64(lc[1], mul64(r.yv, tmin)),
+           zs = add64(lc[2], mul64(r.zv, tmin));
+    double xe = add64(lc[0], mul64(r.xv, tmax)), ye = add64(lc[1], mul64(r.yv, tmax)),
+           ze = add64(lc[2], mul64(r.zv, tmax));
+    axis_setup(g.b[0], vx, nx, r.xv, xs, xe, tmin, tmax, false, r.X, r.xe, r.xs, r.xt, r.xd);
+    axis_setup(g.b[1], vy, ny, r.yv, ys, ye, tmin, tmax, false, r.Y, r.ye, r.ys, r.yt, r.yd);
+    axis_setup(g.b[2], vz, nz, r.zv, zs, ze, tmin, tmax, true, r.Z, r.ze, r.zs, r.zt, r.zd);
+    r.tmin = tmin;
+    r.tmax = tmax;
+    return true;
+}
+
+// sub2ind (RayTracing3DTOF.py:182-202): X + (Y-1)*Ny + (Z-1)*Ny*Nx, 1-based.
+// Ny is the x stride, as in the reference; this is the true Fortran index
+// only when Nx == Ny.
+__device__ __forceinline__ int64_t sub2ind(const Grid& g, int X, int Y, int Z)
+{
+    return (int64_t)X + (int64_t)(Y - 1) * g.ny + (int64_t)(Z - 1) * g.ny * g.nx;
+}
+
+// Walk the voxels.  For voxel k (0-based) the visitor receives
+// (k, 1-based linear index, t at entry, t at exit).  Returns the voxel
+// count, or -1 if the reference would overrun its Nx+Ny+Nz storage
+// (RayTracing3DTOF.py:71-75, 162) — the visitor has then seen `cap` voxels.
+template <class Visit>
+__device__ __forceinline__ int ray_walk(const Grid& g, Ray& r, int cap, Visit&& visit)
+{
+    int64_t cur = sub2ind(g, r.X, r.Y, r.Z);
+    double tprev = r.tmin;
+    int n = 1;
+    while (r.X != r.xe || r.Y != r.ye || r.Z != r.ze) {
+        if (n >= cap) return -1;
+        double t;
+        if (r.xt < r.yt) {
+            if (r.xt < r.zt) { r.X += r.xs; t = r.xt; r.xt = add64(r.xt, r.xd); }
+            else { r.Z += r.zs; t = r.zt; r.zt = add64(r.zt, r.zd); }
+        } else {
+            if (r.yt < r.zt) { r.Y += r.ys; t = r.yt; r.yt = add64(r.yt, r.yd); }
+            else { r.Z += r.zs; t = r.zt; r.zt = add64(r.zt, r.zd); }
+        }
+        visit(n - 1, cur, tprev, t);
+        tprev = t;
+        cur = sub2ind(g, r.X, r.Y, r.Z);
+        n += 1;
+    }
+    visit(n - 1, cur, tprev, r.tmax);
+    return n;
+}
+
+// Segment length exactly as the reference evaluates it:
+// sqrt((xv*t0 - xv*t1)^2 + (yv*t0 - yv*t1)^2 + (zv*t0 - zv*t1)^2)
+// (RayTracing3DTOF.py:152-154, with the grid start replaced by xv*tMin at :127).
+__device__ __forceinline__ double ref_length(const Ray& r, double t0, double t1)
+{
+    double dx = sub64(mul64(r.xv, t0), mul64(r.xv, t1));
+    double dy = sub64(mul64(r.yv, t0), mul64(r.yv, t1));
+    double dz = sub64(mul64(r.zv, t0), mul64(r.zv, t1));
+    return __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+}
+
+}  // namespace sss

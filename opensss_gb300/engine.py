@@ -1,0 +1,194 @@
+"""Host side of the TOF-SSS engine: device buffers (torch), tables and the
+calls into ``libsss300.so``.
+
+``TofSSS`` keeps the scanner, sampling and tables resident on the device;
+``run`` takes the activity and attenuation volumes (numpy or CUDA tensors)
+and returns the sampled scatter sinogram in the engine's leg-pair layout
+``[B, NL, NL]`` (see ``include/sss300.h``) as a CUDA tensor.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib, geometry, tables
+
+WS_BUDGET_BYTES = 24 << 30  # default cap on the leg-list workspace per run
+
+
+def _require_cuda(device):
+    if not torch.cuda.is_available():
+        raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
+    return torch.device(device)
+
+
+def as_device(a, dtype, device):
+    """numpy / tensor -> contiguous CUDA tensor of dtype."""
+    if isinstance(a, torch.Tensor):
+        return a.to(device=device, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device=device, dtype=dtype).contiguous()
+
+
+def fortran_flat(vol, device):
+    """[Nx, Ny, Nz] volume -> flat float32 CUDA tensor in Fortran order (x fastest),
+    the reference's ``flatten(order="F")`` (SingleScatterSimulationTOF.py:187-188)."""
+    if isinstance(vol, torch.Tensor):
+        return vol.to(device=device, dtype=torch.float32).permute(2, 1, 0).contiguous().reshape(-1)
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(vol, dtype=np.float32).transpose(2, 1, 0))
+                            ).reshape(-1).to(device)
+
+
+def _ptr(t: torch.Tensor | None):
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+class TofSSS:
+    """A configured TOF-SSS problem with scanner, sampling and tables on the GPU."""
+
+    def __init__(self, Geometry, NormalVectors, DetectorSize, AttenuationTable, EnergyResolution,
+                 EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution,
+                 TOFRange, NrBins, device="cuda"):
+        self.device = _require_cuda(device)
+        _lib.lib()
+        geom = np.asarray(Geometry, dtype=np.float64)
+        self.nr, self.nd = geom.shape[:2]
+        self.nru, self.ndu = int(NrRingsUsed), int(NrDetectorsUsed)
+        self.nl = self.nru * self.ndu
+        self.nbins = int(NrBins)
+        if not 1 <= self.nbins <= 64:
+            raise ValueError("NrBins must be 1..64")
+        self.sample_step = [int(s) for s in np.asarray(SampleStep).reshape(-1)[:3]]
+        self.detector_size = [float(x) for x in np.asarray(DetectorSize).reshape(-1)[:2]]
+        self.tof_resolution = float(TOFResolution)
+        self.tof_range = float(TOFRange)
+        att = np.asarray(AttenuationTable, dtype=np.float64)
+        self.rings_np = geometry.sampled_rings(self.nr, self.nru)
+        self.dets_np = geometry.sampled_detectors(self.nd, self.ndu)
+        dev = self.device
+        self.geometry = as_device(geom, torch.float64, dev)
+        self.normals = as_device(np.asarray(NormalVectors, dtype=np.float64), torch.float64, dev)
+        self.rings = as_device(self.rings_np, torch.int32, dev)
+        self.dets = as_device(self.dets_np, torch.int32, dev)
+        self.tof_log2w = as_device(tables.tof_log2_table(self.nbins, self.tof_range,
+                                                         self.tof_resolution), torch.float32, dev)
+        self.eff = as_device(tables.pair_efficiency_f32(att, float(EnergyThreshold),
+                                                        float(EnergyResolution)), torch.float32, dev)
+        self.ratio = as_device(tables.attenuation_ratio(att), torch.float32, dev)
+        self._ws = None
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    # ------------------------------------------------------------------
+    def problem(self, act_flat, mu_flat, shape, image_size) -> _lib.TofProblem:
+        p = _lib.TofProblem()
+        p.nx, p.ny, p.nz = (int(s) for s in shape)
+        p.activity = act_flat.data_ptr()
+        p.attenuation = mu_flat.data_ptr()
+        for i, v in enumerate(np.asarray(image_size, dtype=np.float64).reshape(-1)[:6]):
+            p.image_size[i] = float(v)
+        p.nr, p.nd = self.nr, self.nd
+        p.geometry = self.geometry.data_ptr()
+        p.normals = self.normals.data_ptr()
+        p.detector_size[0], p.detector_size[1] = self.detector_size
+        p.nru, p.ndu = self.nru, self.ndu
+        p.rings = self.rings.data_ptr()
+        p.detectors = self.dets.data_ptr()
+        for i in range(3):
+            p.sample_step[i] = self.sample_step[i]
+        p.nbins = self.nbins
+        p.tof_bin_width = 2 * self.tof_range / self.nbins
+        p.tof_resolution = self.tof_resolution
+        p.tof_log2w = self.tof_log2w.data_ptr()
+        p.efficiency = self.eff.data_ptr()
+        p.atten_ratio = self.ratio.data_ptr()
+        return p
+
+    def scatter_points(self, p, stream=None):
+        """(points [n, 4] float64 CUDA tensor, per-slice counts numpy int64)."""
+        L = _lib.lib()
+        lz = -(-p.nz // self.sample_step[2])
+        cap = (-(-p.nx // self.sample_step[0])) * (-(-p.ny // self.sample_step[1])) * lz
+        pts = torch.empty((max(cap, 1), 4), dtype=torch.float64, device=self.device)
+        count = C.c_int64(0)
+        counts = np.zeros(lz, dtype=np.int64)
+        st = C.c_void_p(stream.cuda_stream if stream is not None
+                        else torch.cuda.current_stream(self.device).cuda_stream)
+        _lib.check(L.sss_scatter_points(C.byref(p), _ptr(pts), cap, C.byref(count),
+                                        counts.ctypes.data_as(C.c_void_p), st))
+        return pts[:count.value], counts
+
+    def run(self, ActivityMap, AttenuationMap, ImageSize, max_points: int | None = None,
+            wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
+            check: bool = True) -> torch.Tensor:
+        """Sampled scatter sinogram, leg-pair layout [B, NL, NL] float32 (CUDA).
+
+        ``max_points`` restricts the run to the first scatter points in
+        lattice order (a partial last slice is normalised over its points,
+        like the oracle's bounded samples)."""
+        dev = self.device
+        shape = tuple(int(s) for s in (ActivityMap.shape if not isinstance(ActivityMap, torch.Tensor)
+                                       else ActivityMap.shape))
+        act = fortran_flat(ActivityMap, dev)
+        mu = fortran_flat(AttenuationMap, dev)
+        p = self.problem(act, mu, shape, ImageSize)
+        st = stream if stream is not None else torch.cuda.current_stream(dev)
+        pts, counts = self.scatter_points(p, st)
+        if max_points is not None:
+            keep = np.minimum(counts, np.maximum(0, max_points - np.concatenate([[0], np.cumsum(counts)[:-1]])))
+            counts = keep
+            pts = pts[: int(counts.sum())]
+        n = int(counts.sum())
+        if out is None:
+            out = torch.empty((self.nbins, self.nl, self.nl), dtype=torch.float32, device=dev)
+        wave = self.plan_wave(p, counts, wave_points)
+        L = _lib.lib()
+        need = L.sss_tof_workspace_size(C.byref(p), wave)
+        ws = self.workspace(need)
+        self._status.zero_()
+        _lib.check(L.sss_tof_run(C.byref(p), _ptr(pts), n, counts.ctypes.data_as(C.c_void_p),
+                                 len(counts), wave, _ptr(ws), need, _ptr(out), _ptr(self._status),
+                                 C.c_void_p(st.cuda_stream)))
+        # keep the inputs alive until the stream has consumed them
+        self._last = (act, mu, pts)
+        if check:
+            st.synchronize()
+            _lib.check_status(int(self._status.item()))
+        return out
+
+    def plan_wave(self, p, counts, wave_points=None) -> int:
+        if wave_points is not None:
+            return int(max(wave_points, counts.max(initial=0), 1))
+        L = _lib.lib()
+        per_point = L.sss_tof_workspace_size(C.byref(p), 2) - L.sss_tof_workspace_size(C.byref(p), 1)
+        budget = min(WS_BUDGET_BYTES, int(torch.cuda.mem_get_info(self.device)[0] * 0.5))
+        fit = max(1, budget // max(per_point, 1))
+        total = int(counts.sum())
+        return int(max(min(fit, total), counts.max(initial=0), 1))
+
+    def workspace(self, nbytes: int) -> torch.Tensor:
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = None
+            self._ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    # ------------------------------------------------------------------
+    def densify(self, compact: torch.Tensor, lor) -> torch.Tensor:
+        """Leg-pair layout -> reference layout [B, ND+1, ND//2, NRU^2] (CUDA)."""
+        dev = self.device
+        lor_t = as_device(np.asarray(lor, dtype=np.int16), torch.int16, dev)
+        dense = torch.zeros((self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru),
+                            dtype=torch.float32, device=dev)
+        st = torch.cuda.current_stream(dev)
+        _lib.check(_lib.lib().sss_tof_densify(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd,
+                                              _ptr(lor_t), _ptr(self.dets), _ptr(dense),
+                                              C.c_void_p(st.cuda_stream)))
+        return dense
+
+
+def leg_pair_to_compact(lp: np.ndarray, nru: int, ndu: int) -> np.ndarray:
+    """[B, NL, NL] leg-pair layout -> [B, NRU*NRU, NDU, NDU] (sino = ri1*NRU+ri2)."""
+    b = lp.shape[0]
+    x = lp.reshape(b, nru, ndu, nru, ndu).transpose(0, 1, 3, 2, 4)
+    return x.reshape(b, nru * nru, ndu, ndu)

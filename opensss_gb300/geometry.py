@@ -1,0 +1,121 @@
+"""Geometry-time lookup tables (host, computed once per scanner / sampling).
+
+These are the reference's set-up tables, not per-call work: sinogram
+coordinates of every crystal pair, the ring-pair slice order, the sampled
+rings/crystals of the SSS, and the nearest-neighbour source tables the
+upsampling gathers through.  The hot paths that consume them run on the GPU.
+"""
+
+from __future__ import annotations
+
+import functools
+
+import numpy as np
+
+
+def SinogramCoordinates(NrSectorsTrans: int, NrSectorsAxial: int, NrModulesAxial: int,
+                        NrModulesTrans: int, NrCrystalsTrans: int, NrCrystalsAxial: int,
+                        MinSectorDifference: int = 0, ID_Shidt: bool = True):
+    """Sinogram coordinates of every crystal pair and slice index of every
+    ring pair; same arguments and outputs as the reference
+    (``Python/openSSS/Sinogram.py:27-141``), evaluated with array operations.
+
+    Returns ``(LORCoordinates int16 [N, N, 2] (angular, radial),
+    SinogramIndex int16 [NR, NR], DetectorShift int)``.
+    """
+    nr = NrSectorsAxial * NrModulesAxial * NrCrystalsAxial
+    n = NrSectorsTrans * NrModulesTrans * NrCrystalsTrans
+    min_diff = MinSectorDifference * NrModulesTrans * NrCrystalsTrans
+    radial_size = n - 2 * (min_diff - 1) - 1
+    shift = (NrModulesTrans * NrCrystalsTrans) // 2 if ID_Shidt else 0
+
+    cid = np.arange(n, dtype=np.int64) % n - shift
+    cid[cid < 0] += n
+    c1 = cid[:, None]
+    c2 = cid[None, :]
+    ida = np.where(c1 < c2, c1, c2)
+    idb = np.where(c1 < c2, c2, c1)
+    s = ida + idb
+    diff = idb - ida
+    outer = (s >= (3 * n) // 2) | (s < n // 2)
+    rad_outer = np.where(ida == idb, (-n) // 2, ((diff - 1) // 2) - ((n - (diff + 1)) // 2))
+    rad_inner = np.where(ida == idb, n // 2, ((n - (diff + 1)) // 2) - ((diff - 1) // 2))
+    radial = np.where(outer, rad_outer, rad_inner)
+    angular = np.where(s < n // 2, (2 * ida + n + radial) // 2,
+                       np.where(s >= (3 * n) // 2, (2 * ida - n + radial) // 2,
+                                (2 * ida - radial) // 2))
+    lor = np.full((n, n, 2), -1, dtype=np.int64)
+    ok = diff >= min_diff
+    lor[..., 0] = np.where(ok, angular, -1)
+    lor[..., 1] = np.where(ok, radial + radial_size // 2, -1)
+
+    r1 = np.arange(nr)[:, None]
+    r2 = np.arange(nr)[None, :]
+    d = np.abs(r1 - r2)
+    below = (2 * d - 1) * nr - d * (d - 1) + r2
+    above = (2 * d - 1) * nr - d * (d - 1) + (nr - d) + r1
+    sino = np.where(r1 == r2, r1, np.where(r2 < r1, below, above))
+    return lor.astype(np.int16), sino.astype(np.int16), int(shift)
+
+
+def sampled_rings(nr_rings: int, nr_rings_used: int) -> np.ndarray:
+    """Rings the SSS simulates (``SingleScatterSimulationTOF.py:153``)."""
+    return np.floor(np.linspace(0, nr_rings - 1, nr_rings_used) + 0.5).astype(np.int64)
+
+
+def sampled_detectors(nr_detectors: int, nr_detectors_used: int) -> np.ndarray:
+    """Crystals the SSS simulates per ring (``SingleScatterSimulationTOF.py:159-167``):
+    accumulated floor with step ND/NDU starting at crystal 0."""
+    step = nr_detectors / nr_detectors_used
+    det = np.zeros(nr_detectors_used, dtype=np.int64)
+    for d in range(1, nr_detectors_used):
+        det[d] = int(np.floor(det[d - 1] + step))
+    return det
+
+
+@functools.lru_cache(maxsize=16)
+def _upsample_source_cached(lor_bytes: bytes, nd: int, det_key: tuple):
+    lor = np.frombuffer(lor_bytes, dtype=np.int16).reshape(nd, nd, 2)
+    return _upsample_source(lor, nd, np.array(det_key, dtype=np.int64))
+
+
+def _upsample_source(lor, nd, det):
+    # The reference fills each full sinogram from the sampled crystal pairs
+    # with scipy's nearest-neighbour griddata (Interpolation.py:122-131); the
+    # point set is the same for every ring pair because every ring uses the
+    # same crystals.  Asking the same interpolator for point numbers instead of
+    # values reproduces its choices, including its tie-breaking.
+    from scipy.interpolate import NearestNDInterpolator
+
+    ndu = len(det)
+    rad = lor[np.ix_(det, det, [1])][:, :, 0]
+    ang = lor[np.ix_(det, det, [0])][:, :, 0]
+    points = np.array([(y, x) for y, x in zip(rad.flatten(), ang.flatten())])
+    gx, gy = np.mgrid[0:nd + 1, 0:nd // 2]
+    src = NearestNDInterpolator(points, np.arange(ndu * ndu))((gx, gy))
+    return np.ascontiguousarray(src.astype(np.int32))
+
+
+def upsample_source(lor: np.ndarray, detectors: np.ndarray) -> np.ndarray:
+    """int32 [ND+1, ND/2]: griddata point number p = a*NDU + b (a, b = sampled
+    crystal indices of the two rings) whose value fills each full-sinogram bin."""
+    lor = np.ascontiguousarray(lor, dtype=np.int16)
+    nd = lor.shape[0]
+    return _upsample_source_cached(lor.tobytes(), nd, tuple(int(d) for d in detectors))
+
+
+def ring_nearest(nr_rings: int, rings: np.ndarray) -> np.ndarray:
+    """Index of the sampled ring each ring copies from: RegularGridInterpolator
+    'nearest' over the sampled ring numbers, ties to the lower ring
+    (Interpolation.py:256)."""
+    rings = np.asarray(rings, dtype=np.float64)
+    out = np.zeros(nr_rings, dtype=np.int32)
+    for r in range(nr_rings):
+        i = int(np.searchsorted(rings, r, side="right") - 1)
+        i = min(max(i, 0), len(rings) - 2) if len(rings) > 1 else 0
+        if len(rings) == 1:
+            out[r] = 0
+            continue
+        frac = (r - rings[i]) / (rings[i + 1] - rings[i])
+        out[r] = i if frac <= 0.5 else i + 1
+    return out

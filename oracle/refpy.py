@@ -1,0 +1,46 @@
+"""Loader for the reference openSSS Python package (test infrastructure only).
+
+ORACLE — this module is part of the checker, never of the product.  It imports
+the unmodified reference modules from the reference checkout (default
+``/root/reference/Python``, override with ``OPENSSS_REFERENCE``) with a
+pass-through ``numba`` stub first on ``sys.path``.  It is used only by
+``tests/golden/make_golden.py`` in the build container to produce the golden
+fixtures committed under ``tests/golden``; nothing on a GPU machine imports it.
+"""
+
+import os
+import sys
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE_PY = os.environ.get("OPENSSS_REFERENCE", "/root/reference/Python")
+
+
+def available() -> bool:
+    return os.path.isdir(os.path.join(REFERENCE_PY, "openSSS"))
+
+
+def load():
+    """Import and return the reference modules as a namespace dict."""
+    if not available():
+        raise RuntimeError(f"reference package not found at {REFERENCE_PY}")
+    stub = os.path.join(_HERE, "numba_stub")
+    for p in (stub, REFERENCE_PY):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    # the stub must shadow any real numba
+    sys.path.remove(stub)
+    sys.path.insert(0, stub)
+    import importlib
+
+    mods = {}
+    for name in (
+        "RayTracing3DTOF",
+        "SingleScatterSimulationTOF",
+        "Interpolation",
+        "TailsMask",
+        "BackProjection",
+        "Sinogram",
+        "Support",
+    ):
+        mods[name] = importlib.import_module(f"openSSS.{name}")
+    return mods

@@ -1,0 +1,387 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the unmodified openSSS v1.0 Python modules (interpreted, through the
+pass-through numba stub in ``oracle/numba_stub``) and the reference's MEX ray
+tracers compiled from source (``oracle/_ref``), on seeded synthetic inputs,
+and stores inputs + outputs as compressed ``.npz`` fixtures.  It needs the
+reference checkout (``OPENSSS_REFERENCE``, default ``/root/reference/Python``)
+and is run by hand in the build container:
+
+    python tests/golden/make_golden.py [--only name,...]
+
+The fixtures are then used by the CPU tests (oracle pinning) and the GPU
+parity tests, which never need the reference checkout.
+"""
+
+from __future__ import annotations
+
+import argparse
+import hashlib
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from oracle import refpy  # noqa: E402
+from opensss_gb300 import workloads as W  # noqa: E402
+
+ATT_TABLE = os.path.join(refpy.REFERENCE_PY, "openSSS", "AttenuationTable_AttenuationTable.npy")
+
+
+def _save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+def _sino(R, nd, nr):
+    return R["Sinogram"].SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+
+
+# ---------------------------------------------------------------- rays
+
+
+def ray_cases(seed=7):
+    """Seeded rays on several grids, with the edge cases the tracer has:
+    axis-parallel rays, rays along voxel planes and through voxel corners,
+    rays starting or ending inside the grid, misses and rays that only touch
+    a face."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    grids = [
+        (np.array([12, 12, 6]), np.array([-12.0, -12.0, -6.0, 12.0, 12.0, 6.0])),
+        (np.array([40, 40, 20]), np.array([-20.0, -20.0, -10.0, 20.0, 20.0, 10.0])),
+        (np.array([16, 16, 16]), np.array([-3.2, -3.2, -3.2, 3.2, 3.2, 3.2])),
+        (np.array([10, 14, 7]), np.array([-5.0, -7.0, -3.5, 5.0, 7.0, 3.5])),  # Nx != Ny
+    ]
+    for grid, gb in grids:
+        ext = gb[3:] - gb[:3]
+        n = 600
+        a = rng.uniform(gb[:3] - 0.8 * ext, gb[3:] + 0.8 * ext, size=(n, 3))
+        b = rng.uniform(gb[:3] - 0.8 * ext, gb[3:] + 0.8 * ext, size=(n, 3))
+        lines = np.concatenate([a, b], axis=1)
+        # axis-parallel in one or two coordinates
+        lines[0:40, 3] = lines[0:40, 0]
+        lines[40:80, 4] = lines[40:80, 1]
+        lines[80:120, 5] = lines[80:120, 2]
+        lines[120:150, 3:5] = lines[120:150, 0:2]
+        # endpoints inside the grid
+        lines[150:200, 0:3] = rng.uniform(gb[:3], gb[3:], size=(50, 3))
+        lines[200:230, 3:6] = rng.uniform(gb[:3], gb[3:], size=(30, 3))
+        # points on the voxel lattice (corner and plane crossings, ties)
+        vox = ext / grid
+        k = rng.integers(-2, grid.max() + 3, size=(120, 6))
+        lat = np.concatenate([gb[:3] + k[:, :3] * vox, gb[:3] + k[:, 3:] * vox], axis=1)
+        lines[230:350] = lat
+        # exact diagonals through corners
+        lines[350:360, 0:3] = gb[:3] - vox
+        lines[350:360, 3:6] = gb[3:] + vox * rng.integers(0, 3, size=(10, 1))
+        # lines along a face plane (touching only)
+        lines[360:380, 0] = gb[0]
+        lines[360:380, 3] = gb[0]
+        cases.append((grid, gb, lines))
+    return cases
+
+
+def gen_rays(R):
+    RT = R["RayTracing3DTOF"].RayTracing3DTOF
+    tof = O.RefTracer(True)
+    non = O.RefTracer(False)
+    out = {}
+    for ci, (grid, gb, lines) in enumerate(ray_cases()):
+        cap = int(grid.sum())
+        n = lines.shape[0]
+        cnt = np.zeros(n, np.int32)
+        ln = np.zeros((n, cap))
+        ix = np.zeros((n, cap), np.int32)
+        sm = np.zeros((n, cap))
+        cnt3 = np.zeros(n, np.int32)
+        ln3 = np.zeros((n, cap), np.float32)
+        ix3 = np.zeros((n, cap), np.int32)
+        mex_mismatch = 0
+        raised = 0
+        for i in range(n):
+            try:
+                a, b, c = RT(grid, gb, lines[i])
+            except IndexError:
+                # the traversal overran its Nx+Ny+Nz storage: the reference
+                # raises here (and the MEX build would keep stepping)
+                cnt[i] = -1
+                cnt3[i] = -1
+                raised += 1
+                continue
+            k = len(a)
+            cnt[i] = k
+            ln[i, :k], ix[i, :k], sm[i, :k] = a, b, c
+            ma, mb, mc = tof(grid, gb, lines[i])
+            if len(ma) != k or not np.array_equal(mb, b):
+                mex_mismatch += 1
+            na, nb_, _ = non(grid, gb, lines[i])
+            cnt3[i] = len(na)
+            ln3[i, :len(na)] = na
+            ix3[i, :len(na)] = nb_
+        print(f"rays case {ci}: {n} rays, {int((cnt > 0).sum())} hits, {raised} overruns, "
+              f"MEX/Python index mismatches {mex_mismatch}")
+        out[f"grid{ci}"] = grid
+        out[f"bounds{ci}"] = gb
+        out[f"lines{ci}"] = lines
+        out[f"count{ci}"] = cnt
+        out[f"len{ci}"] = ln
+        out[f"idx{ci}"] = ix
+        out[f"samples{ci}"] = sm
+        out[f"count_nontof{ci}"] = cnt3
+        out[f"len_nontof{ci}"] = ln3
+        out[f"idx_nontof{ci}"] = ix3
+    out["ncases"] = np.array(len(ray_cases()))
+    _save("rays", **out)
+
+
+# ---------------------------------------------------------------- SSS
+
+
+def _run_sss(R, pr, LC):
+    AT = np.load(ATT_TABLE)
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.time()
+        dense = R["SingleScatterSimulationTOF"].SingleScatterSimulationTOF(
+            pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry, LC,
+            pr.scanner.normals, pr.scanner.detector_size_mm, AT, pr.energy_resolution,
+            pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step,
+            pr.tof_resolution, pr.tof_range, pr.nr_bins, d)
+        dt = time.time() - t0
+    return dense, dt
+
+
+def _compact_from_dense(dense, LC, nd, nru, ndu):
+    det = W.sampled_detectors(nd, ndu)
+    a, b = np.triu_indices(ndu)
+    ang = LC[det[a], det[b], 0].astype(np.int64)
+    rad = LC[det[a], det[b], 1].astype(np.int64)
+    cmp = np.zeros((dense.shape[0], nru * nru, ndu, ndu), np.float32)
+    for s in range(nru * nru):
+        cmp[:, s, a, b] = dense[:, rad, ang, s]
+    # everything else in the dense output must be zero
+    check = dense.copy()
+    for s in range(nru * nru):
+        check[:, rad, ang, s] = 0
+    assert not check.any(), "reference wrote outside the sampled detector pairs"
+    return cmp
+
+
+def _problem_arrays(pr):
+    return dict(activity=pr.activity, attenuation=pr.attenuation, image_size=pr.image_size,
+                geometry=pr.scanner.geometry, normals=pr.scanner.normals,
+                detector_size=pr.scanner.detector_size_mm,
+                params=np.array([pr.nr_rings_used, pr.nr_detectors_used, pr.nr_bins,
+                                 *pr.sample_step]),
+                fparams=np.array([pr.energy_resolution, pr.energy_threshold, pr.tof_resolution,
+                                  pr.tof_range]))
+
+
+def gen_sss(R, which):
+    problems = []
+    if "tiny" in which:
+        problems += [("sss_tiny_b1", W.tiny_problem(1, seed=3)),
+                     ("sss_tiny_b3", W.tiny_problem(3, seed=4)),
+                     ("sss_tiny_b5", W.tiny_problem(5, seed=5, shape=(14, 14, 8), nd=64, nr=8,
+                                                    nru=4, ndu=10, voxel_cm=1.7))]
+    if "c1" in which:
+        problems.append(("sss_c1", W.config1(seed=0)))
+    for name, pr in problems:
+        nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
+        LC, SI, _ = _sino(R, nd, nr)
+        dense, dt = _run_sss(R, pr, LC)
+        cmp = _compact_from_dense(dense, LC, nd, pr.nr_rings_used, pr.nr_detectors_used)
+        print(f"{name}: reference SSS {dt:.1f} s, {int((cmp != 0).sum())} non-zero cells")
+        _save(name, **_problem_arrays(pr), compact=cmp, ref_seconds=np.array(dt),
+              ref_cores=np.array(os.cpu_count()))
+
+
+# ---------------------------------------------------------------- tables / LUTs
+
+
+def gen_tables(R):
+    S = R["SingleScatterSimulationTOF"]
+    AT = np.load(ATT_TABLE)
+    out = {}
+    for tag, nb, rng_ps, res in (("b1", 1, 1000.0, 1.0e6), ("b13", 13, None, 214.0),
+                                 ("b33", 33, None, 214.0), ("b6", 6, 1000.0, 214.0)):
+        if rng_ps is None:
+            rng_ps, _ = W.tof_bins(nb, 3.9 if nb == 13 else 1.5)
+        bw = 2 * rng_ps / nb
+        import warnings
+
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            T = S.TOFEfficiencyTable(np.arange(-4000, 4001), bw, nb, res)
+        out[f"tof_{tag}"] = T[:, ::3]  # every 3rd offset keeps the fixture small
+        out[f"tof_{tag}_params"] = np.array([nb, rng_ps, res])
+    from scipy.special import erf
+
+    eff = 0.5 * (1 - erf((435.0 - AT[:, 0]) / (511 * 0.12 / 2 / np.sqrt(np.log(2)))))
+    out["eff_435_012"] = eff
+    out["att_table"] = AT
+    _save("tables", **out)
+
+    lc48, si6, _ = _sino(R, 48, 6)
+    lc64, si10, _ = _sino(R, 64, 10)
+    lc760, si80, _ = _sino(R, 760, 80)
+    digest = hashlib.sha256(np.ascontiguousarray(lc760).tobytes()).hexdigest()
+    _save("sinogram", lor48=lc48, sino6=si6, lor64=lc64, sino10=si10, sino80=si80,
+          lor760_sha256=np.array(digest), lor760_row0=lc760[0], lor760_row379=lc760[379],
+          lor760_diag=np.stack([lc760[i, i] for i in range(760)]))
+
+
+def gen_upsample_luts(R):
+    """For the 760-crystal scanner, the nearest-neighbour source cell that the
+    reference's radial/angular fill picks for every full-sinogram bin, found
+    by running Interpolation.interpolate_radial_angular on a sinogram whose
+    cells hold their own (rad, ang) code."""
+    I = R["Interpolation"]
+    lc760, _, _ = _sino(R, 760, 80)
+    out = {}
+    code = (np.arange(761)[:, None] * 1000 + np.arange(380)[None, :]).astype(np.float32)
+    gx, gy = np.mgrid[0:761, 0:380]
+    for ndu in (32, 48, 96):
+        det = np.tile(W.sampled_detectors(760, ndu), (80, 1))
+        F = I.interpolate_radial_angular(code, 0, 0, lc760, det, gx, gy)
+        out[f"src_ndu{ndu}"] = F.astype(np.int32)
+        print(f"upsample LUT ndu={ndu}: {len(np.unique(F))} distinct sources")
+    _save("upsample_lut760", **out)
+
+
+def gen_upsample(R):
+    """Full InterpolateAllBins on a small geometry (NR must be a multiple of 5)."""
+    I = R["Interpolation"]
+    rng = np.random.default_rng(11)
+    cases = {}
+    for ci, (nd, nr, nru, ndu, nb) in enumerate(((48, 10, 3, 8, 2), (64, 10, 4, 12, 1))):
+        lc, si, _ = _sino(R, nd, nr)
+        det = W.sampled_detectors(nd, ndu)
+        rings = W.sampled_rings(nr, nru)
+        # a sampled sinogram as the SSS writes it: values on the sampled pairs only
+        cmp = np.zeros((nb, nru * nru, ndu, ndu), np.float32)
+        a, b = np.triu_indices(ndu)
+        for s in range(nru * nru):
+            r1, r2 = divmod(s, nru)
+            v = rng.uniform(0.5, 2.0, size=(nb, len(a))).astype(np.float32)
+            same = (a == b) & (r1 == r2)
+            v[:, same] = 0
+            cmp[:, s, a, b] = v
+        dense = O.densify(cmp.astype(np.float64), lc, nd, nru, ndu)
+        with tempfile.TemporaryDirectory() as d:
+            Ib = I.InterpolateScatters(dense, nr, nru, nd, ndu, lc, si, d, False)
+            per_bin = [np.load(os.path.join(d, f"SSS_mashed_bin{k}.npz"))["arr_0"] for k in range(nb)]
+        cases[f"case{ci}_dims"] = np.array([nd, nr, nru, ndu, nb])
+        cases[f"case{ci}_compact"] = cmp
+        cases[f"case{ci}_sum"] = Ib
+        cases[f"case{ci}_bins"] = np.stack(per_bin)
+        cases[f"case{ci}_rings"] = rings
+        print(f"upsample case {ci}: out {Ib.shape}")
+    _save("upsample", **cases)
+
+
+# ---------------------------------------------------------------- mask / fit
+
+
+def _small_scan(nd, nr, radius=20.3, pitch=1.1):
+    # 20 cm / 1 cm would put 45-degree LORs exactly through voxel corners,
+    # where the reference tracer overruns its storage and raises
+    return W.ring_scanner(nd, nr, radius_cm=radius, ring_pitch_cm=pitch)
+
+
+def gen_mask(R):
+    T = R["TailsMask"]
+    out = {}
+    for ci, (nd, nr, shape, vox, af) in enumerate(((48, 6, (12, 12, 6), 2.0, 1),
+                                                    (64, 8, (16, 16, 8), 1.5, 3),
+                                                    (48, 6, (12, 12, 6), 2.0, 5))):
+        sc = _small_scan(nd, nr)
+        act, mu, bounds = W.cylinder_phantom(shape, vox, seed=ci, radius_cm=6.0)
+        lc, si, _ = _sino(R, nd, nr)
+        m = T.MaskGenerator(act, mu, bounds, sc.geometry, lc, si, True, af)
+        out[f"case{ci}_dims"] = np.array([nd, nr, af])
+        out[f"case{ci}_mu"] = mu
+        out[f"case{ci}_bounds"] = bounds
+        out[f"case{ci}_geometry"] = sc.geometry
+        out[f"case{ci}_mask"] = m
+        print(f"mask case {ci}: {int(m.sum())} masked bins of {m.size}")
+    _save("mask", **out)
+
+
+def gen_fit(R):
+    B = R["BackProjection"]
+    T = R["TailsMask"]
+    rng = np.random.default_rng(5)
+    out = {}
+    for ci, (nd, nr, shape, vox, fgrid, af) in enumerate(((48, 6, (12, 12, 6), 2.0, (10, 10, 6), 1),
+                                                           (64, 10, (16, 16, 8), 1.5, (12, 12, 10), 2))):
+        sc = _small_scan(nd, nr)
+        act, mu, bounds = W.cylinder_phantom(shape, vox, seed=ci, radius_cm=6.0)
+        lc, si, _ = _sino(R, nd, nr)
+        m = T.MaskGenerator(act, mu, bounds, sc.geometry, lc, si, True, af)
+        maskf = np.float32(m >= 1)
+        shp = (nd + 1, nd // 2, nr * nr)
+        scat = rng.uniform(0.2, 1.0, size=shp).astype(np.float32)
+        scat[rng.uniform(size=shp) < 0.1] = 0
+        rnd = np.full(shp, 0.1, np.float32)
+        prm = (rng.poisson(3.0, size=shp) / 1.0).astype(np.float32)
+        fit_bounds = np.array([bounds[0], bounds[1], sc.geometry[0, 0, 2] - 0.5,
+                               bounds[3], bounds[4], sc.geometry[-1, 0, 2] + 0.5])
+        order = si[:nr, :nr].T
+        scale = B.BackProjectionScatterRandFit(prm, scat, rnd, maskf, np.array(fgrid), fit_bounds,
+                                               sc.geometry, lc, order, af)
+        out[f"case{ci}_dims"] = np.array([nd, nr, af])
+        out[f"case{ci}_grid"] = np.array(fgrid)
+        out[f"case{ci}_bounds"] = fit_bounds
+        out[f"case{ci}_geometry"] = sc.geometry
+        out[f"case{ci}_mask"] = maskf
+        out[f"case{ci}_scatter"] = scat
+        out[f"case{ci}_randoms"] = rnd
+        out[f"case{ci}_prompts"] = prm
+        out[f"case{ci}_scale"] = np.asarray(scale, np.float32)
+        print(f"fit case {ci}: scale {scale}")
+    _save("fit", **out)
+
+
+ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit"]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default=",".join(ALL))
+    args = ap.parse_args()
+    which = set(args.only.split(","))
+    import warnings
+
+    warnings.simplefilter("ignore")
+    R = refpy.load()
+    from oracle import build_oracle
+
+    build_oracle.build_ref()
+    if "rays" in which:
+        gen_rays(R)
+    if "tables" in which:
+        gen_tables(R)
+    sss = [w.split("_", 1)[1] for w in which if w.startswith("sss_")]
+    if sss:
+        gen_sss(R, sss)
+    if "upsample" in which:
+        gen_upsample(R)
+    if "upsample_lut" in which:
+        gen_upsample_luts(R)
+    if "mask" in which:
+        gen_mask(R)
+    if "fit" in which:
+        gen_fit(R)
+
+
+if __name__ == "__main__":
+    main()

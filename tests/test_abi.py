@@ -1,0 +1,94 @@
+"""The C ABI library loads and exports every declared symbol (no GPU needed)."""
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"\b(sss_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from opensss_gb300 import _lib
+
+    return _lib.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert "sss_tof_run" in names and "sss_raytrace" in names
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_python_binding_covers_header():
+    from opensss_gb300 import _lib
+
+    assert set(_declared()) <= set(_lib.SIGNATURES)
+
+
+def test_abi_version(lib):
+    assert lib.sss_abi_version() == 1
+
+
+def test_invalid_arguments_fail_before_any_device_work(lib):
+    from opensss_gb300 import _lib
+
+    grid = np.array([4, 4, 4], np.int32)
+    bad = np.array([1.0, 0, 0, 0, 1, 1])  # xMax < xMin
+    rc = lib.sss_raytrace(grid.ctypes.data_as(C.c_void_p), bad.ctypes.data_as(C.c_void_p), None, 0,
+                          0, 12, C.c_void_p(8), None, None, C.c_void_p(8), None, None, None)
+    assert rc == 1
+    assert "bounds" in _lib.last_error()
+    ok = np.array([0.0, 0, 0, 1, 1, 1])
+    rc = lib.sss_raytrace(grid.ctypes.data_as(C.c_void_p), ok.ctypes.data_as(C.c_void_p), None, 0,
+                          0, 11, C.c_void_p(8), None, None, C.c_void_p(8), None, None, None)
+    assert rc == 8  # capacity below Nx+Ny+Nz
+    rc = lib.sss_raytrace(grid.ctypes.data_as(C.c_void_p), ok.ctypes.data_as(C.c_void_p), None, 0,
+                          2, 12, C.c_void_p(8), None, None, C.c_void_p(8), None, None, None)
+    assert rc == 1
+
+
+def test_status_codes(lib):
+    from opensss_gb300 import _lib
+
+    assert lib.sss_status_code(0) == 0
+    assert lib.sss_status_code(1) == 3
+    assert "IndexError" in _lib.last_error()
+    assert lib.sss_status_code(2) == 4
+    with pytest.raises(_lib.SSSError):
+        _lib.check_status(1)
+
+
+def test_problem_validation(lib):
+    from opensss_gb300 import _lib
+
+    p = _lib.TofProblem()
+    assert lib.sss_tof_workspace_size(C.byref(p), 10) == 0
+    rc = lib.sss_tof_run(C.byref(p), None, 0, None, 0, 1, None, 0, None, None, None)
+    assert rc == 1
+
+
+def test_no_cpu_fallback_without_gpu():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from opensss_gb300 import RayTracing3DTOF, _lib
+
+    with pytest.raises(_lib.EngineUnavailable):
+        RayTracing3DTOF(np.array([4, 4, 4]), np.array([0.0, 0, 0, 1, 1, 1]),
+                        np.array([-1.0, 0.5, 0.5, 2, 0.5, 0.5]))

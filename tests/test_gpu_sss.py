@@ -1,0 +1,136 @@
+"""GPU TOF-SSS (sss_tof_run) against the reference's outputs and the FP64 oracle.
+
+Tolerance: 1e-4 relative L2 over the whole sampled sinogram, the bar the
+engine is built to; the zero / non-zero pattern (which pairs and slices
+contribute) must match exactly."""
+
+import numpy as np
+import pytest
+
+from conftest import golden, problem_from_golden, rel_l2
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def _engine(pr, att):
+    from opensss_gb300 import TofSSS
+
+    return TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
+                  pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                  pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                  pr.nr_bins)
+
+
+def _gpu_compact(pr, att, **kw):
+    from opensss_gb300.engine import leg_pair_to_compact
+
+    eng = _engine(pr, att)
+    lp = eng.run(pr.activity, pr.attenuation, pr.image_size, **kw).cpu().numpy()
+    return leg_pair_to_compact(lp, pr.nr_rings_used, pr.nr_detectors_used)
+
+
+def _oracle_compact(pr, att, sp_end=-1):
+    return O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                         pr.scanner.normals, pr.scanner.detector_size_mm, att,
+                         pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                         pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                         pr.nr_bins, sp_end=sp_end)
+
+
+def _valid_mask(nru, ndu):
+    ri1 = np.arange(nru)[:, None, None, None]
+    ri2 = np.arange(nru)[None, :, None, None]
+    d1 = np.arange(ndu)[None, None, :, None]
+    d2 = np.arange(ndu)[None, None, None, :]
+    return ((d1 < d2) | ((d1 == d2) & (ri1 != ri2))).reshape(nru * nru, ndu, ndu)
+
+
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_c1"])
+def test_sss_matches_reference(cuda_ok, att_table, name):
+    g = golden(name)
+    pr = problem_from_golden(g)
+    got = _gpu_compact(pr, att_table)
+    ref = g["compact"]
+    assert np.array_equal(got != 0, ref != 0)
+    assert rel_l2(got, ref) < TOL
+    # nothing outside the valid detector pairs
+    assert not got[:, ~_valid_mask(pr.nr_rings_used, pr.nr_detectors_used)].any()
+
+
+def test_scatter_points_match_oracle(cuda_ok, att_table):
+    from opensss_gb300 import workloads as W
+
+    pr = W.config2()
+    eng = _engine(pr, att_table)
+    from opensss_gb300.engine import fortran_flat
+
+    act = fortran_flat(pr.activity, eng.device)
+    mu = fortran_flat(pr.attenuation, eng.device)
+    p = eng.problem(act, mu, pr.grid, pr.image_size)
+    pts, counts = eng.scatter_points(p)
+    xyz, sl = O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)
+    pts = pts.cpu().numpy()
+    assert len(pts) == len(xyz) == counts.sum()
+    assert np.array_equal(pts[:, :3], xyz)
+    assert np.array_equal(pts[:, 3].astype(np.int64), sl)
+
+
+@pytest.mark.parametrize("cfg,points", [("config2", 160), ("config4", 6)])
+def test_sss_large_configs_against_fp64_oracle(cuda_ok, att_table, cfg, points):
+    """Full benchmark geometry, bounded number of scatter points."""
+    from opensss_gb300 import workloads as W
+
+    pr = getattr(W, cfg)()
+    got = _gpu_compact(pr, att_table, max_points=points)
+    ref = _oracle_compact(pr, att_table, sp_end=points)
+    assert np.array_equal(got != 0, ref != 0)
+    assert rel_l2(got, ref) < TOL
+
+
+def test_waves_do_not_change_the_result(cuda_ok, att_table):
+    """Splitting the run into many waves of whole slices gives the same sums."""
+    g = golden("sss_tiny_b5")
+    pr = problem_from_golden(g)
+    a = _gpu_compact(pr, att_table)
+    b = _gpu_compact(pr, att_table, wave_points=1)  # one slice per wave
+    assert rel_l2(b, a) < 1e-6
+
+
+def test_dropin_dense_output(cuda_ok, att_table, tmp_path):
+    from opensss_gb300 import SingleScatterSimulationTOF
+    from opensss_gb300.geometry import SinogramCoordinates
+
+    g = golden("sss_tiny_b3")
+    pr = problem_from_golden(g)
+    lor, _, _ = SinogramCoordinates(1, 1, 1, 1, pr.scanner.nr_detectors, pr.scanner.nr_rings,
+                                    ID_Shidt=False)
+    out = SingleScatterSimulationTOF(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                                     lor, pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                                     pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                                     pr.nr_detectors_used, pr.sample_step, pr.tof_resolution,
+                                     pr.tof_range, pr.nr_bins, str(tmp_path))
+    ref = O.densify(g["compact"].astype(np.float64), lor, pr.scanner.nr_detectors,
+                    pr.nr_rings_used, pr.nr_detectors_used)
+    assert out.dtype == np.float32
+    assert out.shape == (pr.nr_bins, pr.scanner.nr_detectors + 1, pr.scanner.nr_detectors // 2,
+                         pr.nr_rings_used ** 2)
+    assert np.array_equal(out != 0, ref != 0)
+    assert rel_l2(out, ref) < TOL
+    assert (tmp_path / "Scatters_SSS.npz").exists()
+
+
+def test_tof_bins_sum_to_nontof(cuda_ok, att_table):
+    """TOF weights are normalised over bins: summing the TOF bins gives the
+    non-TOF estimate of the same problem (size-independent property)."""
+    from opensss_gb300 import workloads as W
+
+    pr = W.tiny_problem(5, seed=9)
+    tof = _gpu_compact(pr, att_table)
+    pr1 = W.tiny_problem(5, seed=9)
+    pr1.nr_bins, pr1.tof_resolution = 1, 1.0e6
+    non = _gpu_compact(pr1, att_table)
+    # weights only sum to one away from the table edges; the tiny scanner stays inside
+    assert rel_l2(tof.sum(axis=0), non[0]) < 1e-4

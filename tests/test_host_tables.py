@@ -1,0 +1,86 @@
+"""Host-side set-up tables of the engine against the reference's outputs."""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from opensss_gb300 import geometry as G
+from opensss_gb300 import tables as T
+
+
+@pytest.mark.parametrize("tag", ["b1", "b6", "b13", "b33"])
+def test_tof_table_matches_reference(tag):
+    g = golden("tables")
+    nb, rng, res = g[f"tof_{tag}_params"]
+    ref = g[f"tof_{tag}"]
+    assert np.array_equal(T.tof_table(int(nb), rng, res)[:, ::3], ref)
+
+
+@pytest.mark.parametrize("tag", ["b1", "b6", "b13", "b33"])
+def test_kernel_tof_weights_reproduce_table(tag):
+    """The per-bin weights the kernel rebuilds from (log2 max weight, bin)
+    agree with the reference table to FP32 storage precision."""
+    g = golden("tables")
+    nb, rng, res = g[f"tof_{tag}_params"]
+    ref = g[f"tof_{tag}"]
+    l2 = T.tof_log2_table(int(nb), rng, res)
+    w = T.tof_weights_from_log2(l2, int(nb), rng, res)[:, ::3]
+    assert np.abs(w - ref).max() < 5e-8
+    assert np.array_equal(w == 0, ref == 0) or np.abs(w[ref == 0]).max() < 1e-30
+
+
+def test_efficiency_zero_set_matches_reference():
+    g = golden("tables")
+    att = g["att_table"]
+    eff = T.efficiency(att[:, 0], 435.0, 0.12)
+    assert np.array_equal(eff, g["eff_435_012"])
+    pe = T.pair_efficiency_f32(att, 435.0, 0.12)
+    ref_prod = g["eff_435_012"] * g["eff_435_012"][1021]
+    assert np.array_equal(pe == 0, ref_prod == 0)
+
+
+@pytest.mark.parametrize("nd,nr,lk,sk", [(48, 6, "lor48", "sino6"), (64, 10, "lor64", "sino10")])
+def test_sinogram_coordinates_small(nd, nr, lk, sk):
+    g = golden("sinogram")
+    lor, si, shift = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    assert lor.dtype == np.int16 and si.dtype == np.int16 and shift == 0
+    assert np.array_equal(lor, g[lk])
+    assert np.array_equal(si, g[sk])
+
+
+def test_sinogram_coordinates_760():
+    g = golden("sinogram")
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, 760, 80, ID_Shidt=False)
+    assert hashlib.sha256(lor.tobytes()).hexdigest() == str(g["lor760_sha256"])
+    assert np.array_equal(lor[0], g["lor760_row0"])
+    assert np.array_equal(lor[379], g["lor760_row379"])
+    assert np.array_equal(si, g["sino80"])
+
+
+@pytest.mark.parametrize("ndu", [32, 48, 96])
+def test_upsample_source_matches_reference(ndu):
+    lut = golden("upsample_lut760")[f"src_ndu{ndu}"]
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, 760, 80, ID_Shidt=False)
+    det = G.sampled_detectors(760, ndu)
+    src = G.upsample_source(lor, det)
+    a, b = np.divmod(src, ndu)
+    code = lor[det[a], det[b], 1].astype(np.int64) * 1000 + lor[det[a], det[b], 0]
+    assert np.array_equal(code, lut)
+
+
+def test_ring_nearest_ties_to_lower():
+    rings = G.sampled_rings(80, 8)
+    m = G.ring_nearest(80, rings)
+    assert m[0] == 0 and m[79] == 7
+    for r in range(80):
+        d = np.abs(rings - r)
+        best = np.where(d == d.min())[0]
+        assert m[r] == best.min()
+
+
+def test_sampled_detectors_reference_rule():
+    assert G.sampled_detectors(760, 32)[:4].tolist() == [0, 23, 46, 69]
+    assert G.sampled_detectors(760, 96)[-1] == 665
+    assert G.sampled_rings(80, 16)[[0, -1]].tolist() == [0, 79]

@@ -1,0 +1,114 @@
+"""Pin the CPU oracle to the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the unmodified reference)."""
+
+import numpy as np
+import pytest
+
+from conftest import golden, problem_from_golden, rel_l2
+from oracle import oracle as O
+
+
+def _ulp_close(a, b, ulps=4):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    tol = ulps * np.spacing(np.maximum(np.abs(a), np.abs(b)))
+    return np.all(np.abs(a - b) <= tol)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_oracle_rays_match_reference(case):
+    g = golden("rays")
+    grid, gb, lines = g[f"grid{case}"], g[f"bounds{case}"], g[f"lines{case}"]
+    cnt_ref = g[f"count{case}"]
+    cnt, ln, ix, sm = O.trace_batch(grid, gb, lines, allow_overrun=True)
+    # overruns (reference IndexError) are flagged, everything else matches
+    assert np.array_equal(cnt < 0, cnt_ref < 0)
+    ok = cnt_ref >= 0
+    assert np.array_equal(cnt[ok], cnt_ref[ok])
+    for i in np.where(ok & (cnt_ref > 0))[0]:
+        n = cnt_ref[i]
+        assert np.array_equal(ix[i, :n], g[f"idx{case}"][i, :n]), i
+        # the interpreted reference squares through libm pow(); the oracle
+        # multiplies (as numba does): lengths agree to a few ulp
+        assert _ulp_close(ln[i, :n], g[f"len{case}"][i, :n]), i
+        assert _ulp_close(sm[i, :n], g[f"samples{case}"][i, :n], ulps=16), i
+
+
+def test_rays_fixture_has_edge_cases():
+    g = golden("rays")
+    allc = np.concatenate([g[f"count{c}"] for c in range(int(g["ncases"]))])
+    assert (allc == 0).sum() > 50          # misses
+    assert (allc < 0).sum() > 0            # reference overruns
+    assert (allc > 0).sum() > 1000
+
+
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5"])
+def test_oracle_sss_matches_reference(name, att_table):
+    g = golden(name)
+    pr = problem_from_golden(g)
+    cmp = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                        pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                        pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                        pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                        pr.nr_bins)
+    ref = g["compact"]
+    assert np.array_equal(cmp != 0, ref != 0)
+    # reference accumulates in float32, the oracle in FP64
+    assert rel_l2(cmp, ref) < 1e-6
+
+
+@pytest.mark.slow
+def test_oracle_sss_config1_matches_reference(att_table):
+    g = golden("sss_c1")
+    pr = problem_from_golden(g)
+    cmp = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                        pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                        pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                        pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                        pr.nr_bins)
+    ref = g["compact"]
+    assert np.array_equal(cmp != 0, ref != 0)
+    assert rel_l2(cmp, ref) < 1e-6
+
+
+@pytest.mark.parametrize("case", range(3))
+def test_oracle_mask_matches_reference(case):
+    from opensss_gb300.geometry import SinogramCoordinates
+
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    m = O.mask(g[f"case{case}_mu"], g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, si, af)
+    assert np.array_equal(m, g[f"case{case}_mask"])
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_oracle_fit_matches_reference(case):
+    from opensss_gb300.geometry import SinogramCoordinates
+
+    g = golden("fit")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    s = O.fit(g[f"case{case}_prompts"], g[f"case{case}_scatter"], g[f"case{case}_randoms"],
+              g[f"case{case}_mask"], g[f"case{case}_grid"], g[f"case{case}_bounds"],
+              g[f"case{case}_geometry"], lor, si, af)
+    ref = g[f"case{case}_scale"]
+    assert abs(float(s[0]) - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_oracle_upsample_matches_reference(case):
+    from opensss_gb300 import geometry as G
+
+    g = golden("upsample")
+    nd, nr, nru, ndu, nb = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    det = G.sampled_detectors(nd, ndu)
+    lut = G.upsample_source(lor, det)
+    rmap = G.ring_nearest(nr, G.sampled_rings(nr, nru))
+    cmp = g[f"case{case}_compact"].astype(np.float64)
+    bins = []
+    for b in range(nb):
+        bins.append(O.upsample_bin(cmp[b], nru, ndu, nr, nd, lut, rmap, si))
+    assert np.array_equal(np.stack(bins), g[f"case{case}_bins"])
+    assert np.allclose(np.sum(bins, axis=0), g[f"case{case}_sum"], rtol=1e-6, atol=0)
