@@ -198,13 +198,13 @@ def run_ours(args, rank, world, local_rank):
     act_f, mu_f = fortran_flat(act, dev), fortran_flat(mu, dev)
     p = eng.problem(act_f, mu_f, pr.grid, pr.image_size)
     pts, counts = eng.scatter_points(p)
-    nsp = int(counts.sum())
+    nsp = int(counts.sum()) if args.max_points is None else min(int(counts.sum()), args.max_points)
     units = nsp * P * pr.nr_bins
 
     L.sss_set_timing(1)
     out = torch.empty((pr.nr_bins, eng.nl, eng.nl), dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
-        eng.run(act, mu, pr.image_size, out=out)
+        eng.run(act, mu, pr.image_size, out=out, max_points=args.max_points)
     stage = np.zeros(6)
     step_ms = []
     pair_ms = []
@@ -218,7 +218,7 @@ def run_ours(args, rank, world, local_rank):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            eng.run(act, mu, pr.image_size, out=out, check=False)
+            eng.run(act, mu, pr.image_size, out=out, check=False, max_points=args.max_points)
             e1.record(stream)
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
@@ -247,7 +247,7 @@ def run_ours(args, rank, world, local_rank):
         t0 = time.perf_counter()
         a = act_h.to(dev, non_blocking=True)
         m = mu_h.to(dev, non_blocking=True)
-        r = eng.run(a, m, pr.image_size, out=out, check=False)
+        r = eng.run(a, m, pr.image_size, out=out, check=False, max_points=args.max_points)
         res_h.copy_(r, non_blocking=True)
         torch.cuda.synchronize(dev)
         if i >= args.warmup:
@@ -334,9 +334,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--ref-points", type=int, default=48,
+    ap.add_argument("--ref-points", type=int, default=1024,
                     help="scatter points in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--max-points", type=int, default=None,
+                    help="limit each step to the first scatter points (profiling runs only)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

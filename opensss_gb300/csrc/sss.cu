@@ -126,7 +126,7 @@ struct LegParams {
     int npts;
     float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
     float4* legB;   // [npts][nl]: unit vector to the crystal, voxel-list length (int bits)
-    float2* vox;    // [npts][cap][nl]: act*len, 2*sample/c (ps)
+    float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major
     int32_t* status;
 };
 
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
         const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
         const float inv_c = (float)(1.0 / kLightCmPerPs);
         const double t0 = r.tmin;
-        float2* out = P.vox + (long long)s * P.cap * P.nl + l;
+        float2* out = P.vox + ((long long)s * P.nl + l) * P.cap;
         int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
             long long v = lin - 1;
             if (v < 0 || v >= P.nvox) {
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
             if (a != 0.f) {
                 // sample = half the distance walked to the voxel's exit (:155-156)
                 float rho = vlen * (float)(tb - t0) * inv_c;
-                out[(long long)nlist * P.nl] = make_float2(a, rho);
+                out[nlist] = make_float2(a, rho);
                 ++nlist;
             }
         });
@@ -205,8 +205,7 @@ struct PairParams {
     const float4* legA;
     const float4* legB;
     const float2* vox;
-    const int2* chunks;     // (l1, chunk) per chunk task
-    int nchunks;
+    int nchunks;            // 32-partner chunks per walking leg
     int nslices;
     int slice_first[kMaxWaveSlices];   // first point of slice j within the wave
     int slice_count[kMaxWaveSlices];
@@ -273,6 +272,15 @@ __device__ __forceinline__ void accumulate_voxel(float (&acc)[BP], int nbins, fl
     }
 }
 
+// One task = (slice, walking leg lw, chunk of 32 partner legs).  Every lane
+// pairs lw with its own partner leg lp; the pair (l1, l2) is ordered as the
+// reference orders it (crystal of l1 < crystal of l2, :469).  The task adds
+// the part of the pair's TOF sum that runs over lw's voxels (AB1 if lw is
+// l1, AB2 if lw is l2, :519-530); the other part comes from the task that
+// walks lp.  Both tasks see the same scatter points, so both divide by the
+// same per-slice count.  All lanes walk the same voxel list: one coalesced
+// 32-voxel load per 32 voxels, broadcast with shuffles, and no divergence
+// in trip count.
 template <int BP>
 __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_constant__ PairParams P)
 {
@@ -286,7 +294,8 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    const long long ntasks = (long long)P.nslices * P.nchunks;
+    const long long per_slice = (long long)P.nl * P.nchunks;
+    const long long ntasks = (long long)P.nslices * per_slice;
     const float inv_c = (float)(1.0 / kLightCmPerPs);
     bool tof_bad = false, energy_bad = false;
     unsigned long long walked = 0, npairs = 0;
@@ -296,29 +305,34 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
         if (lane == 0) task = atomicAdd(P.counter, 1u);
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= ntasks) break;
-        const int slice = (int)(task / P.nchunks);
-        const int2 ch = P.chunks[task % P.nchunks];
-        const int l1 = ch.x;
-        const int ri1 = l1 / P.ndu, di1 = l1 % P.ndu;
-        // valid second legs of l1 in order: rings ri2 < ri1 with di2 >= di1,
-        // ring ri1 with di2 > di1, rings ri2 > ri1 with di2 >= di1 (:464-470)
-        const int m = P.ndu - di1;
-        const int nvalid = P.nru * m - 1;
-        const int q = ch.y * 32 + lane;
-        const bool lane_ok = q < nvalid;
-        int ri2, di2;
-        if (q < ri1 * m) {
-            ri2 = q / m;
-            di2 = di1 + q % m;
-        } else if (q < ri1 * m + m - 1) {
-            ri2 = ri1;
-            di2 = di1 + 1 + (q - ri1 * m);
-        } else {
-            const int q2 = q - ri1 * m - (m - 1);
-            ri2 = ri1 + 1 + q2 / m;
-            di2 = di1 + q2 % m;
+        const int slice = (int)(task / per_slice);
+        const int rem = (int)(task % per_slice);
+        const int lw = rem / P.nchunks;
+        const int rw = lw / P.ndu, dw = lw % P.ndu;
+
+        // partner of this lane: legs 0..nl-1 (lw leads the pair unless its
+        // crystal is the larger), then one more entry per other ring for the
+        // same crystal in the opposite role (both orders are distinct pairs)
+        const int q = (rem % P.nchunks) * 32 + lane;
+        int lp = lw, rp = rw, dp = dw;
+        bool w_first = true, lane_ok = false;
+        if (q < P.nl) {
+            lp = q;
+            rp = q / P.ndu;
+            dp = q % P.ndu;
+            lane_ok = lp != lw;
+            w_first = dp >= dw;
+        } else if (q < P.nl + P.nru) {
+            rp = q - P.nl;
+            dp = dw;
+            lp = rp * P.ndu + dw;
+            lane_ok = rp != rw;
+            w_first = false;
         }
-        const int l2 = lane_ok ? ri2 * P.ndu + di2 : l1;
+        const int ri1 = w_first ? rw : rp, di1 = w_first ? dw : dp;
+        const int ri2 = w_first ? rp : rw, di2 = w_first ? dp : dw;
+        const int l1 = w_first ? lw : lp, l2 = w_first ? lp : lw;
+        const float sigma = w_first ? -1.f : 1.f;
 
         float acc[BP];
 #pragma unroll
@@ -328,11 +342,13 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
         const int sfirst = P.slice_first[slice], scount = P.slice_count[slice];
         for (int s = sfirst; s < sfirst + scount; ++s) {
             const long long lo = (long long)s * P.nl;
-            const float4 A1 = P.legA[lo + l1], B1 = P.legB[lo + l1];
-            const float4 A2 = P.legA[lo + l2], B2 = P.legB[lo + l2];
+            const float4 Aw = P.legA[lo + lw], Bw = P.legB[lo + lw];
+            const float4 Ap = P.legA[lo + lp], Bp = P.legB[lo + lp];
+            const float4 A1 = w_first ? Aw : Ap, A2 = w_first ? Ap : Aw;
+            const float4 B1 = w_first ? Bw : Bp, B2 = w_first ? Bp : Bw;
             bool ok = lane_ok && A1.z != INFINITY && A2.z != INFINITY &&
                       !(A1.y == 0.f && A2.y == 0.f);
-            float c1 = 0.f, c2 = 0.f;
+            float c = 0.f;
             if (ok) {
                 // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
                 float qc = fmaf(B1.x, B2.x, fmaf(B1.y, B2.y, B1.z * B2.z));
@@ -342,17 +358,14 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
                 const float fr = eh - floorf(eh);
                 int row;
                 if (fr < 1e-3f || fr > 1.0f - 1e-3f)
-                    row = energy_row_fp64(P, sfirst + (s - sfirst), ri1, di1, ri2, di2);
+                    row = energy_row_fp64(P, s, ri1, di1, ri2, di2);
                 else
                     row = 2 * (int)floorf(eh) - 1;
                 if (row < 0 || row >= 2000) {
                     energy_bad = true;
-                    ok = false;
                 } else {
                     const float effp = __ldg(P.eff + row);
-                    if (effp == 0.f) {
-                        ok = false;  // :508-509 (before the count is added)
-                    } else {
+                    if (effp != 0.f) {  // :508-509 skips before the count is added
                         const float rr = __ldg(P.ratio + row);
                         // Klein-Nishina with cos(theta) = -qc (:239-258)
                         const float ratio = 1.0f / (1.0f + P.gamma_kn * (1.0f + qc));
@@ -360,44 +373,40 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
                         const float kn = ratio * ratio * (ratio + 1.0f / ratio - sin2);
                         // geometry (:533-536): (ds)^2 |cos a1||cos a2| / (4 pi sv1^2 sv2^2)
                         const float f = P.geo_c * A1.w * A2.w * effp * kn;
-                        const float m1 = ex2(-A1.z), m2 = ex2(-A2.z);
-                        const float m1r = ex2(-rr * A1.z), m2r = ex2(-rr * A2.z);
-                        if (A1.y != 0.f) c1 = f * m1 * m2r;  // :540
-                        if (A2.y != 0.f) c2 = f * m2 * m1r;
+                        // this task's part: M1 * M2^r * AB1 or M2 * M1^r * AB2 (:540)
+                        const float mw = ex2(-Aw.z), mpr = ex2(-rr * Ap.z);
+                        if (Aw.y != 0.f) c = f * mw * mpr;
                         cnt += (A1.y != 0.f && A2.y != 0.f) ? 2.f : 1.f;  // :485-488
                         npairs += 1;
-                        walked += (c1 != 0.f ? __float_as_int(B1.w) : 0) +
-                                  (c2 != 0.f ? __float_as_int(B2.w) : 0);
                     }
                 }
             }
             // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
             const float u = fmaf(A1.x - A2.x, inv_c, 4000.5f);
-            const float2* v1 = P.vox + (long long)s * P.cap * P.nl + l1;
-            if (__any_sync(0xffffffffu, c1 != 0.f)) {
-                const int n1 = __float_as_int(B1.w);
-                for (int k = 0; k < n1; ++k) {
-                    const float2 v = v1[(long long)k * P.nl];
-                    if (c1 != 0.f)
-                        accumulate_voxel<BP>(acc, P.nbins, c1 * v.x, u - v.y, sY, sN, P, tof_bad);
-                }
-            }
-            const int n2 = c2 != 0.f ? __float_as_int(B2.w) : 0;
-            const int n2max = __reduce_max_sync(0xffffffffu, n2);
-            const float2* v2 = P.vox + (long long)s * P.cap * P.nl + l2;
-            for (int k = 0; k < n2max; ++k) {
-                if (k < n2) {
-                    const float2 v = v2[(long long)k * P.nl];
-                    accumulate_voxel<BP>(acc, P.nbins, c2 * v.x, u + v.y, sY, sN, P, tof_bad);
+            if (__any_sync(0xffffffffu, c != 0.f)) {
+                const int nw = __float_as_int(Bw.w);
+                if (c != 0.f) walked += nw;
+                const float2* vw = P.vox + (lo + lw) * P.cap;
+                for (int k0 = 0; k0 < nw; k0 += 32) {
+                    const float2 mine = (k0 + lane < nw) ? vw[k0 + lane] : make_float2(0.f, 0.f);
+                    const int jn = min(32, nw - k0);
+                    for (int j = 0; j < jn; ++j) {
+                        const float a = __shfl_sync(0xffffffffu, mine.x, j);
+                        const float r = __shfl_sync(0xffffffffu, mine.y, j);
+                        if (c != 0.f)
+                            accumulate_voxel<BP>(acc, P.nbins, c * a, fmaf(sigma, r, u), sY, sN, P,
+                                                 tof_bad);
+                    }
                 }
             }
         }
         if (lane_ok && cnt > 0.f) {
             float* o = P.out + (long long)l1 * P.nl + l2;
             const long long plane = (long long)P.nl * P.nl;
+            const float inv = 1.0f / cnt;
 #pragma unroll
             for (int b = 0; b < BP; ++b)
-                if (b < P.nbins) atomicAdd(o + b * plane, acc[b] / cnt);
+                if (b < P.nbins) atomicAdd(o + b * plane, acc[b] * inv);
         }
     }
     if (tof_bad) raise_error(P.status, kErrTofRange);
@@ -428,7 +437,7 @@ int launch_pairs(const PairParams& P, cudaStream_t st)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pair_kernel<BP>, kPairWarps * 32, smem);
     if (per_sm < 1) per_sm = 1;
-    long long ntasks = (long long)P.nslices * P.nchunks;
+    long long ntasks = (long long)P.nslices * P.nl * P.nchunks;
     long long blocks = std::min<long long>((long long)sms * per_sm,
                                            (ntasks + kPairWarps - 1) / kPairWarps);
     if (blocks < 1) blocks = 1;
@@ -494,10 +503,10 @@ struct StageTimer {
 thread_local StageTimer g_timer;
 
 struct WsLayout {
-    size_t legA, legB, vox, chunks, counter, total;
+    size_t legA, legB, vox, counter, total;
 };
 
-WsLayout ws_layout(const sss_tof_problem& p, long long wave_points, long long nchunks)
+WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
 {
     const long long nl = (long long)p.nru * p.ndu;
     const long long cap = (long long)p.nx + p.ny + p.nz;
@@ -509,22 +518,16 @@ WsLayout ws_layout(const sss_tof_problem& p, long long wave_points, long long nc
     off = align_up(off + sizeof(float4) * wave_points * nl);
     w.vox = off;
     off = align_up(off + sizeof(float2) * wave_points * cap * nl);
-    w.chunks = off;
-    off = align_up(off + sizeof(int2) * nchunks);
     w.counter = off;
     off = align_up(off + 256);
     w.total = off;
     return w;
 }
 
-long long chunk_count(const sss_tof_problem& p)
+// partner chunks per walking leg: nl legs plus nru same-crystal entries
+int chunk_count(const sss_tof_problem& p)
 {
-    long long n = 0;
-    for (int di1 = 0; di1 < p.ndu; ++di1) {
-        long long nvalid = (long long)p.nru * (p.ndu - di1) - 1;
-        n += (long long)p.nru * ((nvalid + 31) / 32);
-    }
-    return n;
+    return ((p.nru * p.ndu + p.nru) + 31) / 32;
 }
 
 int validate(const sss_tof_problem* p)
@@ -590,7 +593,7 @@ extern "C" int sss_scatter_points(const sss_tof_problem* p, double* points, int6
 extern "C" size_t sss_tof_workspace_size(const sss_tof_problem* p, int64_t wave_points)
 {
     if (validate(p)) return 0;
-    return ws_layout(*p, wave_points, chunk_count(*p)).total;
+    return ws_layout(*p, wave_points).total;
 }
 
 extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64_t n_points,
@@ -605,7 +608,6 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     cudaStream_t st = (cudaStream_t)stream;
     const long long nl = (long long)p->nru * p->ndu;
     const long long cap = (long long)p->nx + p->ny + p->nz;
-    const long long nchunks = chunk_count(*p);
     long long maxslice = 0, tot = 0;
     for (int64_t i = 0; i < n_slices; ++i) {
         maxslice = std::max<long long>(maxslice, slice_counts[i]);
@@ -615,7 +617,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     if (wave_points < maxslice)
         return sss_set_error(SSS_ERR_INVALID, "wave_points %lld < largest slice %lld",
                              (long long)wave_points, maxslice);
-    WsLayout w = ws_layout(*p, wave_points, nchunks);
+    WsLayout w = ws_layout(*p, wave_points);
     if (!workspace || workspace_bytes < w.total)
         return sss_set_error(SSS_ERR_WORKSPACE, "sss_tof_run: workspace %zu < %zu bytes",
                              workspace_bytes, w.total);
@@ -624,17 +626,6 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
         return sss_set_error(SSS_ERR_CUDA, "sss_tof_run: memset failed");
     if (n_points == 0) return SSS_OK;
 
-    // chunk table (l1, chunk), l1-major
-    std::vector<int2> chunks;
-    chunks.reserve(nchunks);
-    for (int l1 = 0; l1 < nl; ++l1) {
-        int di1 = l1 % p->ndu;
-        long long nvalid = (long long)p->nru * (p->ndu - di1) - 1;
-        for (int c = 0; c < (nvalid + 31) / 32; ++c) chunks.push_back(make_int2(l1, c));
-    }
-    if (cudaMemcpyAsync(ws + w.chunks, chunks.data(), sizeof(int2) * chunks.size(),
-                        cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return sss_set_error(SSS_ERR_CUDA, "sss_tof_run: chunk upload failed");
 
     LegParams LP;
     LP.g.nx = p->nx;
@@ -683,8 +674,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     PP.legA = LP.legA;
     PP.legB = LP.legB;
     PP.vox = LP.vox;
-    PP.chunks = (const int2*)(ws + w.chunks);
-    PP.nchunks = (int)nchunks;
+    PP.nchunks = chunk_count(*p);
     PP.counter = (unsigned int*)(ws + w.counter);
     PP.work = (unsigned long long*)(ws + w.counter + 8);
     PP.out = out;

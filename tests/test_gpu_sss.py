@@ -40,6 +40,16 @@ def _oracle_compact(pr, att, sp_end=-1):
                          pr.nr_bins, sp_end=sp_end)
 
 
+def assert_same_support(got, ref, floor=1e-25):
+    """Same set of contributing cells.  FP32 flushes TOF weights that are
+    below ~1e-38 in FP64 to zero, so cells whose reference value is that far
+    below the sinogram's peak may differ in zero-ness only."""
+    tiny = floor * float(np.abs(ref).max())
+    diff = (got != 0) != (ref != 0)
+    assert not np.any(diff & (np.abs(ref) > tiny)), int(np.sum(diff & (np.abs(ref) > tiny)))
+    assert not np.any(diff & (np.abs(got) > tiny))
+
+
 def _valid_mask(nru, ndu):
     ri1 = np.arange(nru)[:, None, None, None]
     ri2 = np.arange(nru)[None, :, None, None]
@@ -54,7 +64,7 @@ def test_sss_matches_reference(cuda_ok, att_table, name):
     pr = problem_from_golden(g)
     got = _gpu_compact(pr, att_table)
     ref = g["compact"]
-    assert np.array_equal(got != 0, ref != 0)
+    assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
     # nothing outside the valid detector pairs
     assert not got[:, ~_valid_mask(pr.nr_rings_used, pr.nr_detectors_used)].any()
@@ -86,7 +96,7 @@ def test_sss_large_configs_against_fp64_oracle(cuda_ok, att_table, cfg, points):
     pr = getattr(W, cfg)()
     got = _gpu_compact(pr, att_table, max_points=points)
     ref = _oracle_compact(pr, att_table, sp_end=points)
-    assert np.array_equal(got != 0, ref != 0)
+    assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
 
 
@@ -117,7 +127,7 @@ def test_dropin_dense_output(cuda_ok, att_table, tmp_path):
     assert out.dtype == np.float32
     assert out.shape == (pr.nr_bins, pr.scanner.nr_detectors + 1, pr.scanner.nr_detectors // 2,
                          pr.nr_rings_used ** 2)
-    assert np.array_equal(out != 0, ref != 0)
+    assert_same_support(out, ref)
     assert rel_l2(out, ref) < TOL
     assert (tmp_path / "Scatters_SSS.npz").exists()
 
