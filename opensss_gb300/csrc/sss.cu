@@ -28,7 +28,7 @@ using namespace sss;
 
 constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
 constexpr int kMaxWaveSlices = 256;
-constexpr int kPairWarps = 8;  // warps per pair-kernel block
+constexpr int kPairWarps = 4;  // warps per pair-kernel block
 
 struct LatticeDims {
     int lx, ly, lz;     // lattice points per axis
