@@ -107,7 +107,7 @@ size_t sss_tof_workspace_size(const sss_tof_problem *p, int64_t wave_points);
 /* Run the simulation for the points [0, n_points) (whole slices as given by
  * slice_counts, host, n_slices entries).  out (device) receives the sampled
  * scatter sinogram in leg-pair layout [nbins][NL][NL], NL = nru*ndu, leg
- * l = ring_index*ndu + det_index: element [b][l1][l2] is the reference's
+ * l = det_index*nru + ring_index (crystal-major): element [b][l1][l2] is the reference's
  * Scatters[b, Radial, Angular, ri2 + ri1*nru] for the crystal pair
  * (detectors[di1], detectors[di2]), defined for di1 < di2 and for di1 == di2
  * with ri1 != ri2, zero elsewhere.  Asynchronous on `stream`. */

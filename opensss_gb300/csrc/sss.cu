@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
     long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)P.npts * P.nl) return;
     const int s = (int)(gid / P.nl), l = (int)(gid % P.nl);
-    const int ri = l / P.ndu, di = l % P.ndu;
+    const int di = l / P.nru, ri = l % P.nru;  // legs are crystal-major
     const int ring = P.rings[ri], det = P.dets[di];
     const double* dp = P.geom + 3 * ((long long)ring * P.nd + det);
     const double zD = P.geom[3 * ((long long)ring * P.nd) + 2];  // :402 (crystal 0's z)
@@ -244,12 +244,18 @@ __device__ __noinline__ int energy_row_fp64(const PairParams& P, int s, int ri1,
     return (int)mul64(es, 2.0) - 1;
 }
 
+// Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
+// reference's 8001-entry TOF table, :520-528).  w_b is rebuilt from the
+// largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
+// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Two bins per
+// packed FP32x2 instruction.
 template <int BP>
-__device__ __forceinline__ void accumulate_voxel(float (&acc)[BP], int nbins, float ca, float x,
-                                                 const float* sY, const unsigned char* sN,
-                                                 const PairParams& P, bool& tof_bad)
+__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[(BP + 1) / 2], int nbins, float ca,
+                                                 float x, const float* sY,
+                                                 const unsigned char* sN, const PairParams& P,
+                                                 bool& tof_bad)
 {
-    // t = floor(x) with x in [-2^22, 2^22]: round-down add of 1.5*2^23
+    // t = floor(x) with |x| < 2^22: round-down add of 1.5*2^23
     float y = __fadd_rd(x, 12582912.0f);
     int t = __float_as_int(y) - 0x4B400000;
     if (t < 0) t += kTofEntries;  // numpy negative index wraps (:521, :527)
@@ -260,14 +266,22 @@ __device__ __forceinline__ void accumulate_voxel(float (&acc)[BP], int nbins, fl
     const float Y = sY[t];
     const float n = (float)sN[t];
     const float off = (float)(t - kTimeRange);
-    const float delta = off - fmaf(n, P.w, P.s0);
-    const float beta = P.kappa2w * delta;
+    const float beta = P.kappa2w * (off - fmaf(n, P.w, P.s0));
+    if constexpr (BP == 1) {
+        acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(P.gamma, n, beta), Y)), acc[0].x);
+    } else {
+        const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
+        const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-P.gamma, -P.gamma);
+        const float2 two = make_float2(2.f, 2.f);
+        float2 nd = make_float2(-n, 1.f - n);  // b - n for the pair (b, b+1)
 #pragma unroll
-    for (int b = 0; b < BP; ++b) {
-        if (b < nbins) {
-            const float d = n - (float)b;
-            const float e = fmaf(-d, fmaf(P.gamma, d, beta), Y);
-            acc[b] = fmaf(ca, ex2(e), acc[b]);
+        for (int k = 0; k < (BP + 1) / 2; ++k) {
+            if (2 * k < nbins) {
+                const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
+                const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
+                acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), ex2(e2.y)), acc[k]);
+            }
+            nd = __fadd2_rn(nd, two);
         }
     }
 }
@@ -308,7 +322,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
         const int slice = (int)(task / per_slice);
         const int rem = (int)(task % per_slice);
         const int lw = rem / P.nchunks;
-        const int rw = lw / P.ndu, dw = lw % P.ndu;
+        const int dw = lw / P.nru, rw = lw % P.nru;
 
         // partner of this lane: legs 0..nl-1 (lw leads the pair unless its
         // crystal is the larger), then one more entry per other ring for the
@@ -318,14 +332,14 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
         bool w_first = true, lane_ok = false;
         if (q < P.nl) {
             lp = q;
-            rp = q / P.ndu;
-            dp = q % P.ndu;
+            dp = q / P.nru;
+            rp = q % P.nru;
             lane_ok = lp != lw;
             w_first = dp >= dw;
         } else if (q < P.nl + P.nru) {
             rp = q - P.nl;
             dp = dw;
-            lp = rp * P.ndu + dw;
+            lp = dw * P.nru + rp;
             lane_ok = rp != rw;
             w_first = false;
         }
@@ -334,9 +348,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
         const int l1 = w_first ? lw : lp, l2 = w_first ? lp : lw;
         const float sigma = w_first ? -1.f : 1.f;
 
-        float acc[BP];
+        float2 acc[(BP + 1) / 2];
 #pragma unroll
-        for (int b = 0; b < BP; ++b) acc[b] = 0.f;
+        for (int k = 0; k < (BP + 1) / 2; ++k) acc[k] = make_float2(0.f, 0.f);
         float cnt = 0.f;
 
         const int sfirst = P.slice_first[slice], scount = P.slice_count[slice];
@@ -405,8 +419,10 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
             const long long plane = (long long)P.nl * P.nl;
             const float inv = 1.0f / cnt;
 #pragma unroll
-            for (int b = 0; b < BP; ++b)
-                if (b < P.nbins) atomicAdd(o + b * plane, acc[b] * inv);
+            for (int k = 0; k < (BP + 1) / 2; ++k) {
+                if (2 * k < P.nbins) atomicAdd(o + (2 * k) * plane, acc[k].x * inv);
+                if (2 * k + 1 < P.nbins) atomicAdd(o + (2 * k + 1) * plane, acc[k].y * inv);
+            }
         }
     }
     if (tof_bad) raise_error(P.status, kErrTofRange);
@@ -469,7 +485,7 @@ __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru
     const int l2 = (int)(i % nl);
     const int l1 = (int)((i / nl) % nl);
     const int b = (int)(i / ((long long)nl * nl));
-    const int ri1 = l1 / ndu, di1 = l1 % ndu, ri2 = l2 / ndu, di2 = l2 % ndu;
+    const int di1 = l1 / nru, ri1 = l1 % nru, di2 = l2 / nru, ri2 = l2 % nru;
     if (di1 > di2 || (di1 == di2 && ri1 == ri2)) return;
     const int d1 = dets[di1], d2 = dets[di2];
     const int ang = lor[2 * ((long long)d1 * nd + d2)];

@@ -188,7 +188,8 @@ class TofSSS:
 
 
 def leg_pair_to_compact(lp: np.ndarray, nru: int, ndu: int) -> np.ndarray:
-    """[B, NL, NL] leg-pair layout -> [B, NRU*NRU, NDU, NDU] (sino = ri1*NRU+ri2)."""
+    """[B, NL, NL] leg-pair layout (leg = crystal_index*NRU + ring_index) ->
+    [B, NRU*NRU, NDU, NDU] (sino = ri1*NRU + ri2, then crystal indices)."""
     b = lp.shape[0]
-    x = lp.reshape(b, nru, ndu, nru, ndu).transpose(0, 1, 3, 2, 4)
+    x = lp.reshape(b, ndu, nru, ndu, nru).transpose(0, 2, 4, 1, 3)
     return x.reshape(b, nru * nru, ndu, ndu)
