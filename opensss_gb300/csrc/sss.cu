@@ -164,7 +164,11 @@ __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
                 raise_error(P.status, kErrVoxel);
                 return;
             }
-            float len = vlen * (float)(tb - ta);
+            // |vec| * |dt|; for near-zero steps the reference's own FP64 length
+            // expression decides whether a corner-grazing segment is zero or
+            // not (that decides whether a leg carries activity, :483-488)
+            const double dt = tb - ta;
+            float len = fabs(dt) < 1e-9 ? (float)ref_length(r, ta, tb) : vlen * (float)fabs(dt);
             float a = __ldg(P.act + v) * len;
             musum = fmaf(__ldg(P.mu + v), len, musum);
             asum += a;
