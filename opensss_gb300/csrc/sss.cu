@@ -17,6 +17,7 @@
 //      normalisation, :555-557).
 // Nothing per voxel or per pair reaches HBM except the leg lists themselves.
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -28,7 +29,7 @@ using namespace sss;
 
 constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
 constexpr int kMaxWaveSlices = 256;
-constexpr int kPairWarps = 4;  // warps per pair-kernel block
+constexpr int kPairWarps = 8;  // warps per pair-kernel block
 
 struct LatticeDims {
     int lx, ly, lz;     // lattice points per axis
@@ -251,27 +252,31 @@ __device__ __noinline__ int energy_row_fp64(const PairParams& P, int s, int ri1,
 // Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
 // reference's 8001-entry TOF table, :520-528).  w_b is rebuilt from the
 // largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
-// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Two bins per
-// packed FP32x2 instruction.
-template <int BP>
-__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[(BP + 1) / 2], int nbins, float ca,
-                                                 float x, const float* sY,
-                                                 const unsigned char* sN, const PairParams& P,
-                                                 bool& tof_bad)
+// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Bins go two
+// at a time through packed FP32x2 instructions; NP = number of bin pairs.
+template <int NP, bool SINGLE>
+__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
+                                                 const float* sY, const unsigned char* sN,
+                                                 const PairParams& P, bool& tof_bad)
 {
-    // t = floor(x) with |x| < 2^22: round-down add of 1.5*2^23
-    float y = __fadd_rd(x, 12582912.0f);
+    // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
+    const float y = __fadd_rd(x, 12582912.0f);
     int t = __float_as_int(y) - 0x4B400000;
-    if (t < 0) t += kTofEntries;  // numpy negative index wraps (:521, :527)
+    float off = y - 12586912.0f;  // t - 4000, exact
     if ((unsigned)t >= (unsigned)kTofEntries) {
-        tof_bad = true;
-        return;
+        if (t < 0 && t + kTofEntries >= 0) {  // numpy negative index wraps (:521, :527)
+            t += kTofEntries;
+            off = (float)(t - kTimeRange);
+        } else {
+            tof_bad = true;
+            return;
+        }
     }
     const float Y = sY[t];
     const float n = (float)sN[t];
-    const float off = (float)(t - kTimeRange);
+    // beta = 2 kappa w (off - s_n), s_n = s0 + n w
     const float beta = P.kappa2w * (off - fmaf(n, P.w, P.s0));
-    if constexpr (BP == 1) {
+    if constexpr (SINGLE) {
         acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(P.gamma, n, beta), Y)), acc[0].x);
     } else {
         const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
@@ -279,13 +284,11 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[(BP + 1) / 2], in
         const float2 two = make_float2(2.f, 2.f);
         float2 nd = make_float2(-n, 1.f - n);  // b - n for the pair (b, b+1)
 #pragma unroll
-        for (int k = 0; k < (BP + 1) / 2; ++k) {
-            if (2 * k < nbins) {
-                const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
-                const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
-                acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), ex2(e2.y)), acc[k]);
-            }
-            nd = __fadd2_rn(nd, two);
+        for (int k = 0; k < NP; ++k) {
+            const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
+            const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
+            acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), ex2(e2.y)), acc[k]);
+            if (k + 1 < NP) nd = __fadd2_rn(nd, two);
         }
     }
 }
@@ -296,15 +299,17 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[(BP + 1) / 2], in
 // the part of the pair's TOF sum that runs over lw's voxels (AB1 if lw is
 // l1, AB2 if lw is l2, :519-530); the other part comes from the task that
 // walks lp.  Both tasks see the same scatter points, so both divide by the
-// same per-slice count.  All lanes walk the same voxel list: one coalesced
-// 32-voxel load per 32 voxels, broadcast with shuffles, and no divergence
-// in trip count.
-template <int BP>
-__global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_constant__ PairParams P)
+// same per-slice count.  All lanes walk the same voxel list: 32 voxels at a
+// time are staged in a per-warp shared buffer and read back as broadcasts,
+// so the trip count is uniform across the warp.
+template <int NP, bool SINGLE, int MINB>
+__global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
 {
     extern __shared__ float smem[];
     float* sY = smem;
     unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
+    float2* vbuf = reinterpret_cast<float2*>(smem + kTofEntries + (kTofEntries + 3) / 4 + 1) +
+                   (threadIdx.x >> 5) * 32;
     for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
         sY[i] = P.tof_log2w[2 * i];
         sN[i] = (unsigned char)P.tof_log2w[2 * i + 1];
@@ -352,9 +357,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
         const int l1 = w_first ? lw : lp, l2 = w_first ? lp : lw;
         const float sigma = w_first ? -1.f : 1.f;
 
-        float2 acc[(BP + 1) / 2];
+        float2 acc[NP];
 #pragma unroll
-        for (int k = 0; k < (BP + 1) / 2; ++k) acc[k] = make_float2(0.f, 0.f);
+        for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);
         float cnt = 0.f;
 
         const int sfirst = P.slice_first[slice], scount = P.slice_count[slice];
@@ -406,14 +411,17 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
                 if (c != 0.f) walked += nw;
                 const float2* vw = P.vox + (lo + lw) * P.cap;
                 for (int k0 = 0; k0 < nw; k0 += 32) {
-                    const float2 mine = (k0 + lane < nw) ? vw[k0 + lane] : make_float2(0.f, 0.f);
+                    __syncwarp();
+                    if (k0 + lane < nw) vbuf[lane] = vw[k0 + lane];
+                    __syncwarp();
                     const int jn = min(32, nw - k0);
-                    for (int j = 0; j < jn; ++j) {
-                        const float a = __shfl_sync(0xffffffffu, mine.x, j);
-                        const float r = __shfl_sync(0xffffffffu, mine.y, j);
-                        if (c != 0.f)
-                            accumulate_voxel<BP>(acc, P.nbins, c * a, fmaf(sigma, r, u), sY, sN, P,
-                                                 tof_bad);
+                    if (c != 0.f) {
+#pragma unroll 2
+                        for (int j = 0; j < jn; ++j) {
+                            const float2 v = vbuf[j];
+                            accumulate_voxel<NP, SINGLE>(acc, c * v.x, fmaf(sigma, v.y, u), sY, sN,
+                                                         P, tof_bad);
+                        }
                     }
                 }
             }
@@ -423,7 +431,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
             const long long plane = (long long)P.nl * P.nl;
             const float inv = 1.0f / cnt;
 #pragma unroll
-            for (int k = 0; k < (BP + 1) / 2; ++k) {
+            for (int k = 0; k < NP; ++k) {
                 if (2 * k < P.nbins) atomicAdd(o + (2 * k) * plane, acc[k].x * inv);
                 if (2 * k + 1 < P.nbins) atomicAdd(o + (2 * k + 1) * plane, acc[k].y * inv);
             }
@@ -442,38 +450,45 @@ __global__ void __launch_bounds__(kPairWarps * 32) pair_kernel(const __grid_cons
     }
 }
 
-template <int BP>
+size_t pair_smem_bytes()
+{
+    return sizeof(float) * (kTofEntries + (kTofEntries + 3) / 4 + 1) + sizeof(float2) * 32 * kPairWarps;
+}
+
+template <int NP, bool SINGLE>
 int launch_pairs(const PairParams& P, cudaStream_t st)
 {
-    const size_t smem = kTofEntries * sizeof(float) + kTofEntries;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(pair_kernel<BP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        attr_set = true;
-    }
+    constexpr int MINB = NP <= 8 ? 3 : 2;
+    auto kern = pair_kernel<NP, SINGLE, MINB>;
+    if (NP <= 8 && getenv("SSS_PAIR_MINB2")) kern = pair_kernel<NP, SINGLE, 2>;
+    const size_t smem = pair_smem_bytes();
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pair_kernel<BP>, kPairWarps * 32, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPairWarps * 32, smem);
     if (per_sm < 1) per_sm = 1;
     long long ntasks = (long long)P.nslices * P.nl * P.nchunks;
     long long blocks = std::min<long long>((long long)sms * per_sm,
                                            (ntasks + kPairWarps - 1) / kPairWarps);
     if (blocks < 1) blocks = 1;
-    pair_kernel<BP><<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(P);
+    kern<<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(P);
     return sss_check_launch("pair_kernel");
 }
 
 int dispatch_pairs(const PairParams& P, cudaStream_t st)
 {
-    const int b = P.nbins;
-    if (b <= 1) return launch_pairs<1>(P, st);
-    if (b <= 8) return launch_pairs<8>(P, st);
-    if (b <= 16) return launch_pairs<16>(P, st);
-    if (b <= 24) return launch_pairs<24>(P, st);
-    if (b <= 40) return launch_pairs<40>(P, st);
-    return launch_pairs<64>(P, st);
+    if (P.nbins == 1) return launch_pairs<1, true>(P, st);
+    switch ((P.nbins + 1) / 2) {
+#define SSS_NP(k) \
+    case k: return launch_pairs<k, false>(P, st);
+        SSS_NP(1) SSS_NP(2) SSS_NP(3) SSS_NP(4) SSS_NP(5) SSS_NP(6) SSS_NP(7) SSS_NP(8)
+        SSS_NP(9) SSS_NP(10) SSS_NP(11) SSS_NP(12) SSS_NP(13) SSS_NP(14) SSS_NP(15) SSS_NP(16)
+        SSS_NP(17) SSS_NP(18) SSS_NP(19) SSS_NP(20) SSS_NP(21) SSS_NP(22) SSS_NP(23) SSS_NP(24)
+        SSS_NP(25) SSS_NP(26) SSS_NP(27) SSS_NP(28) SSS_NP(29) SSS_NP(30) SSS_NP(31) SSS_NP(32)
+#undef SSS_NP
+    }
+    return sss_set_error(SSS_ERR_INVALID, "nbins out of range");
 }
 
 // ---------------------------------------------------------------- densify
