@@ -30,6 +30,11 @@ using namespace sss;
 constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
 constexpr int kMaxWaveSlices = 256;
 constexpr int kPairWarps = 8;  // warps per pair-kernel block
+// pair-kernel shared memory: log2 weight table (floats), bin table (bytes),
+// then 32 float2 voxels per warp starting on a 16-byte boundary
+constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
+constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
+static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
 struct LatticeDims {
     int lx, ly, lz;     // lattice points per axis
@@ -308,8 +313,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
     extern __shared__ float smem[];
     float* sY = smem;
     unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
-    float2* vbuf = reinterpret_cast<float2*>(smem + kTofEntries + (kTofEntries + 3) / 4 + 1) +
-                   (threadIdx.x >> 5) * 32;
+    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
     for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
         sY[i] = P.tof_log2w[2 * i];
         sN[i] = (unsigned char)P.tof_log2w[2 * i + 1];
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
 
 size_t pair_smem_bytes()
 {
-    return sizeof(float) * (kTofEntries + (kTofEntries + 3) / 4 + 1) + sizeof(float2) * 32 * kPairWarps;
+    return sizeof(float) * kSmemVbufFloats + sizeof(float2) * 32 * kPairWarps;
 }
 
 template <int NP, bool SINGLE>
