@@ -17,7 +17,6 @@
 //      normalisation, :555-557).
 // Nothing per voxel or per pair reaches HBM except the leg lists themselves.
 #include <algorithm>
-#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -464,7 +463,6 @@ int launch_pairs(const PairParams& P, cudaStream_t st)
 {
     constexpr int MINB = NP <= 8 ? 3 : 2;
     auto kern = pair_kernel<NP, SINGLE, MINB>;
-    if (NP <= 8 && getenv("SSS_PAIR_MINB2")) kern = pair_kernel<NP, SINGLE, 2>;
     const size_t smem = pair_smem_bytes();
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int dev = 0, sms = 0, per_sm = 0;
