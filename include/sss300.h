@@ -100,6 +100,20 @@ typedef struct sss_tof_problem {
 int sss_scatter_points(const sss_tof_problem *p, double *points, int64_t capacity,
                        int64_t *count, int64_t *slice_counts, void *stream);
 
+/* No counterpart in the reference.  sss_scatter_points without any device
+ * allocation, for callers that must not allocate: code running inside a
+ * fixed memory arena or pool it does not own, under a runtime that forbids
+ * allocation calls while it records or replays work, or in a process whose
+ * device memory is capped.  Same arguments, results and errors as
+ * sss_scatter_points; its scratch is a 32 KiB array inside the library that
+ * every GPU loading the library holds until exit.  Limit: at most 4096
+ * sampled z-slices (ceil(nz / sample_step[2])); larger problems get
+ * SSS_ERR_INVALID.  The first call on each device looks up that array's
+ * device address, so make it before any stream capture.  All calls share the
+ * array: calls whose work overlaps on the GPU race, so serialise them. */
+int sss_scatter_points_noalloc(const sss_tof_problem *p, double *points, int64_t capacity,
+                               int64_t *count, int64_t *slice_counts, void *stream);
+
 /* Bytes of device workspace sss_tof_run needs for waves of at most
  * wave_points scatter points (a wave always holds whole z-slices). */
 size_t sss_tof_workspace_size(const sss_tof_problem *p, int64_t wave_points);

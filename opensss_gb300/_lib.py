@@ -58,6 +58,8 @@ SIGNATURES = {
     "sss_status_code": (C.c_int, [_I32]),
     "sss_raytrace": (C.c_int, [_P, _P, _P, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _P]),
     "sss_scatter_points": (C.c_int, [C.POINTER(TofProblem), _P, _I64, C.POINTER(_I64), _P, _P]),
+    "sss_scatter_points_noalloc": (C.c_int, [C.POINTER(TofProblem), _P, _I64, C.POINTER(_I64), _P,
+                                             _P]),
     "sss_tof_workspace_size": (C.c_size_t, [C.POINTER(TofProblem), _I64]),
     "sss_tof_run": (C.c_int, [C.POINTER(TofProblem), _P, _I64, _P, _I64, _I64, _P, C.c_size_t,
                               _P, _P, _P]),

@@ -17,6 +17,7 @@
 //      normalisation, :555-557).
 // Nothing per voxel or per pair reaches HBM except the leg lists themselves.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -804,4 +805,94 @@ extern "C" int sss_tof_densify(const float* compact, int32_t nbins, int32_t nru,
     densify_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         compact, nbins, nru, ndu, nd, lor, detectors, dense);
     return sss_check_launch("densify_kernel");
+}
+
+// ---------------------------------------------------------------- no-allocation scatter points
+//
+// sss_scatter_points_noalloc: the same scatter-point enumeration as
+// sss_scatter_points for callers that must not allocate device memory —
+// code that runs inside a fixed memory arena or pool it does not own, under
+// a runtime that forbids allocation calls while it records or replays work,
+// or in a process whose memory is capped so that a late allocation could
+// fail mid-pipeline.  Its scratch (the running total and one counter per
+// sampled z-slice) lives in the file-scope array below instead of a
+// temporary buffer.
+namespace {
+
+// At most this many sampled z-slices (ceil(nz / sample_step_z)).
+constexpr int kNoAllocMaxSlices = 4096;
+constexpr int kNoAllocMaxDevices = 64;
+
+// [0] = total points, [1 + i] = points of sampled slice i.  32 KiB that every
+// GPU which loads this library keeps until the process exits.  All calls
+// share it: each call clears the part it uses before the kernel runs, and two
+// calls whose work overlaps on the GPU race on it.
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[1 + kNoAllocMaxSlices];
+
+std::mutex g_noalloc_lock;
+unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up once per
+// device (host code cannot use the symbol's name as an address).
+int noalloc_scratch(unsigned long long** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_scatter_points_noalloc: no current device");
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return sss_set_error(SSS_ERR_INVALID, "sss_scatter_points_noalloc: device %d not supported", dev);
+    std::lock_guard<std::mutex> guard(g_noalloc_lock);
+    if (!g_noalloc_addr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return sss_set_error(SSS_ERR_CUDA, "sss_scatter_points_noalloc: cudaGetSymbolAddress: %s",
+                                 cudaGetErrorString(e));
+        g_noalloc_addr[dev] = (unsigned long long*)ptr;
+    }
+    *out = g_noalloc_addr[dev];
+    return SSS_OK;
+}
+
+}  // namespace
+
+extern "C" int sss_scatter_points_noalloc(const sss_tof_problem* p, double* points, int64_t capacity,
+                                          int64_t* count, int64_t* slice_counts, void* stream)
+{
+    int rc = validate(p);
+    if (rc) return rc;
+    if (!count) return sss_set_error(SSS_ERR_INVALID, "sss_scatter_points_noalloc: null count");
+    if (capacity > 0 && !points)
+        return sss_set_error(SSS_ERR_INVALID, "sss_scatter_points_noalloc: null points");
+    LatticeDims L = lattice(*p);
+    if (L.lz > kNoAllocMaxSlices)
+        return sss_set_error(SSS_ERR_INVALID,
+                             "sss_scatter_points_noalloc: %d sampled z-slices exceed its limit of %d",
+                             L.lz, kNoAllocMaxSlices);
+    unsigned long long* scratch = nullptr;
+    if ((rc = noalloc_scratch(&scratch))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const double* IS = p->image_size;
+    double zvox = (IS[5] - IS[2]) / p->nz;  // :87
+    double zstart = zvox / 2 - (-IS[2]);    // :176, :179
+    double radius = -IS[0];                 // :177
+    const size_t used = (1 + (size_t)L.lz) * sizeof(unsigned long long);
+    if (cudaMemsetAsync(scratch, 0, used, st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_scatter_points_noalloc: clearing the scratch failed");
+    scatter_points_kernel<<<1, 1024, 0, st>>>(p->attenuation, p->nx, p->ny, p->nz, L, radius, zstart,
+                                               zvox, points, capacity, scratch, scratch + 1);
+    if ((rc = sss_check_launch("scatter_points_kernel"))) return rc;
+    unsigned long long total = 0;
+    if (cudaMemcpyAsync(&total, scratch, sizeof(total), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        (slice_counts && cudaMemcpyAsync(slice_counts, scratch + 1, (size_t)L.lz * sizeof(int64_t),
+                                         cudaMemcpyDeviceToHost, st) != cudaSuccess))
+        return sss_set_error(SSS_ERR_CUDA, "sss_scatter_points_noalloc: copy failed");
+    if (cudaStreamSynchronize(st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_scatter_points_noalloc: %s",
+                             cudaGetErrorString(cudaGetLastError()));
+    *count = (int64_t)total;
+    if ((int64_t)total > capacity)
+        return sss_set_error(SSS_ERR_CAPACITY, "sss_scatter_points_noalloc: %lld points > capacity %lld",
+                             (long long)total, (long long)capacity);
+    return SSS_OK;
 }
