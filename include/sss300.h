@@ -138,6 +138,47 @@ int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t nd
                     const int16_t *lor, const int32_t *detectors, float *dense, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Upsampling.  Replaces InterpolateAllBins (Python/openSSS/Interpolation.py:197-319)
+ * once its nearest-neighbour choices are known (geometry time, see
+ * opensss_gb300/geometry.py): out[cell*nslices + s] = sum over the nbins bins
+ * of max(sampled[b*bin_stride + cell_src[cell] + ring_src[s]], 0), in bin
+ * order (one bin: nbins = 1).  cell = rad*(ND/2) + ang over the full
+ * (ND+1) x ND/2 sinogram, s = full-sinogram slice.  The two offset tables
+ * (device int64) address either the reference's dense sampled layout or the
+ * leg-pair layout of sss_tof_run.  out (device) is [ncell][nslices]. */
+int sss_upsample(const float *sampled, int64_t bin_stride, int32_t nbins, const int64_t *cell_src,
+                 const int64_t *ring_src, int64_t ncell, int32_t nslices, float *out, void *stream);
+
+/* Tail mask.  Replaces MaskGenerator / MaskDetectors (Python/openSSS/TailsMask.py:84-228):
+ * every LOR (Ring1, d1, Ring2, d2) with d1, d2 multiples of af and d1 <= d2
+ * (not the same crystal) is traced through map (device float32, Fortran
+ * order; attenuation in cm^-1, or activity when use_activity) in FP64.
+ * out[cell*nr*nr + sino_index[Ring1][Ring2]] = 1 where 1/exp(-sum mu*len) == 1
+ * (attenuation) or sum act*len <= 0 (activity).  out (device uint8,
+ * [(nd+1)*(nd/2)][nr*nr]) must be zeroed by the caller. */
+int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float *map, int32_t use_activity,
+                  int32_t nr, int32_t nd, const double *geometry, const int16_t *lor,
+                  const int16_t *sino_index, int32_t af, uint8_t *out, int32_t *status, void *stream);
+
+/* Back-projection scale fit.  Replaces BackProjectionScatterRandFit
+ * (Python/openSSS/BackProjection.py:115-215) and BackProjection (:31-113).
+ * The LOR (Ring1, d1, Ring2, d2) on the af lattice reads slice
+ * sino_order[Ring1][Ring2] (the reference passes SinogramIndex.T) of the
+ * full sinograms prompts / randoms (device float32 [cell][slice]) and of the
+ * mask: mask_f32 (multiplied) or, if not NULL, mask_u8 (mask >= 1).  The
+ * scatter value is scatters[scat_cell[cell] + scat_ring[slice]] (clamped at
+ * 0 when scat_clamp), so an upsampled sinogram can be read straight from
+ * the sampled one.  images: device workspace 4 * Nx*Ny*Nz floats (P, S, R,
+ * sensitivity); sums: device 2 doubles; scale: device float, the fitted
+ * slope (reference: float32 array of shape (1,)). */
+int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
+                        const double *geometry, const int16_t *lor, const int16_t *sino_order,
+                        int32_t af, const float *prompts, const float *randoms, const float *mask_f32,
+                        const uint8_t *mask_u8, const float *scatters, const int64_t *scat_cell,
+                        const int64_t *scat_ring, int32_t scat_clamp, float *images, double *sums,
+                        float *scale, int32_t *status, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Stage timing (no reference counterpart: instrumentation for benchmarks).
  * When enabled, sss_tof_run records CUDA events around its kernels on the
  * caller's stream; sss_get_timing waits for them and returns, for the last

@@ -1,0 +1,76 @@
+"""Drop-in ``GenerateTailsMask`` / ``MaskGenerator``: the tail mask on the GPU.
+
+Same arguments and result as the reference (``Python/openSSS/TailsMask.py:28-82,165-228``):
+uint8 ``(ND+1, ND//2, NR**2)``, 1 where the LOR's attenuation correction
+factor is exactly 1 (or, with ``UseAttenuation=False``, where it sees no
+activity), for the LORs on the AccelerationFactor lattice.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import as_device, fortran_flat
+
+
+def _ptr(t):
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramIndex,
+                     AccelerationFactor=1, use_activity=False, device="cuda") -> torch.Tensor:
+    """uint8 CUDA tensor [(ND+1)*(ND//2), NR*NR]."""
+    if not torch.cuda.is_available():
+        raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
+    geom = np.asarray(Geometry, dtype=np.float64)
+    nr, nd = geom.shape[:2]
+    shape = tuple(int(s) for s in volume.shape)
+    vol = fortran_flat(volume, device)
+    g = as_device(geom, torch.float64, device)
+    lor = as_device(np.asarray(SinogramCoordinates, dtype=np.int16), torch.int16, device)
+    si = as_device(np.asarray(SinogramIndex, dtype=np.int16)[:nr, :nr], torch.int16, device)
+    out = torch.zeros(((nd + 1) * (nd // 2), nr * nr), dtype=torch.uint8, device=device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    grid = np.array(shape, dtype=np.int32)
+    bounds = np.ascontiguousarray(np.asarray(ImageSize, dtype=np.float64).reshape(-1)[:6])
+    st = torch.cuda.current_stream(device)
+    _lib.check(_lib.lib().sss_tail_mask(grid.ctypes.data_as(C.c_void_p),
+                                        bounds.ctypes.data_as(C.c_void_p), _ptr(vol),
+                                        int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(si),
+                                        int(AccelerationFactor or 1), _ptr(out), _ptr(status),
+                                        C.c_void_p(st.cuda_stream)))
+    st.synchronize()
+    _lib.check_status(int(status.item()))
+    return out
+
+
+def MaskGenerator(ActivityMap, AttenuationMap, ImageSize, Geometry, SinogramCoordinates,
+                  SinogramIndex, UseAttenuation, AccelerationFactor=1, device="cuda"):
+    t0 = time.time()
+    geom = np.asarray(Geometry)
+    nr, nd = geom.shape[:2]
+    vol = AttenuationMap if UseAttenuation else ActivityMap
+    m = tail_mask_device(vol, ImageSize, geom, SinogramCoordinates, SinogramIndex,
+                         AccelerationFactor, use_activity=not UseAttenuation, device=device)
+    print("Time for Generate Tail Mask:", time.time() - t0, "seconds")
+    return m.cpu().numpy().reshape(nd + 1, nd // 2, nr * nr)
+
+
+def GenerateTailsMask(SavePath, ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
+                      extendedGeometry, LORCoordinates, SinogramIndex, AccelerationFactor,
+                      UseAttenuation=True, Overwrite=False, device="cuda"):
+    path = os.path.join(SavePath, "AttenuationMask.npy")
+    if os.path.isfile(path) and not Overwrite:
+        return np.load(path)
+    if np.asarray(extendedGeometry).shape[0] != 0:
+        raise NotImplementedError("the span (axial mashing) tail mask is not part of this engine yet")
+    mask = MaskGenerator(ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
+                         LORCoordinates, SinogramIndex, UseAttenuation, AccelerationFactor, device)
+    np.save(path, mask)
+    return mask

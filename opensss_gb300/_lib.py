@@ -64,6 +64,10 @@ SIGNATURES = {
     "sss_tof_run": (C.c_int, [C.POINTER(TofProblem), _P, _I64, _P, _I64, _I64, _P, C.c_size_t,
                               _P, _P, _P]),
     "sss_tof_densify": (C.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _P, _P]),
+    "sss_upsample": (C.c_int, [_P, _I64, _I32, _P, _P, _I64, _I32, _P, _P]),
+    "sss_tail_mask": (C.c_int, [_P, _P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P]),
+    "sss_backproject_fit": (C.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _P,
+                                      _P, _I32, _P, _P, _P, _P, _P]),
     "sss_set_timing": (None, [C.c_int]),
     "sss_get_timing": (C.c_int, [_P]),
     "sss_probe_ex2_rate": (C.c_int, [C.POINTER(_D), _P]),

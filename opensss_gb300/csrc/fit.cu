@@ -1,0 +1,363 @@
+// Upsampling, tail mask and back-projection fit on sm_103a.
+//
+//  * upsample_kernel: the reference's nearest-neighbour upsampling
+//    (Python/openSSS/Interpolation.py:197-319) is a pure gather once the
+//    geometry-time source tables exist: output (cell, slice) copies the
+//    sampled value at cell_src[cell] + ring_src[slice] (clamped at 0 like
+//    fill_with_interp1d, :163), optionally summed over TOF bins in bin order
+//    (:317).  HBM-write bound.
+//  * mask_kernel: MaskDetectors (Python/openSSS/TailsMask.py:84-163): one
+//    thread per LOR on the AccelerationFactor lattice, FP64 walk and FP64
+//    line integral, mask = (1/exp(-sum) == 1).
+//  * bp_kernel + fit_reduce_kernel + fit_final_kernel: BackProjection and
+//    BackProjectionScatterRandFit (Python/openSSS/BackProjection.py:31-215):
+//    one thread per LOR, FP32 atomic scatter-add of P/n, S/n, R/n and 1 into
+//    four images, then per voxel Sbp = S/sens, T = max(P/sens - R/sens, 0)
+//    and the slope sum(x T)/sum(x^2) in FP64 with x = float(Sbp * 1e10).
+#include "common.cuh"
+#include "trace.cuh"
+
+namespace {
+
+using namespace sss;
+
+// LOR number -> (ring1, ring2, crystal index 1, crystal index 2) with the
+// ring pair fastest, so a warp handles one crystal pair on neighbouring ring
+// pairs (same sinogram cell, nearby slices, similar voxel paths).
+struct LorIndex {
+    int r1, r2, i1, i2;
+};
+
+__device__ __forceinline__ LorIndex lor_of(long long id, int nr, int na)
+{
+    LorIndex L;
+    L.r2 = (int)(id % nr);
+    id /= nr;
+    L.r1 = (int)(id % nr);
+    id /= nr;
+    L.i2 = (int)(id % na);
+    L.i1 = (int)(id / na);
+    return L;
+}
+
+__device__ __forceinline__ void lor_line(const double* geom, int nd, int r1, int d1, int r2, int d2,
+                                         double* lc)
+{
+    const double* p1 = geom + 3 * ((long long)r1 * nd + d1);
+    const double* p2 = geom + 3 * ((long long)r2 * nd + d2);
+    lc[0] = p1[0];
+    lc[1] = p1[1];
+    lc[2] = geom[3 * ((long long)r1 * nd) + 2];  // the ring's z (TailsMask.py:118, :125)
+    lc[3] = p2[0];
+    lc[4] = p2[1];
+    lc[5] = geom[3 * ((long long)r2 * nd) + 2];
+}
+
+// ---------------------------------------------------------------- upsampling
+
+__global__ void upsample_kernel(const float* __restrict__ in, long long bin_stride, int nbins,
+                                const long long* __restrict__ cell_src,
+                                const long long* __restrict__ ring_src, long long ncell, int nslices,
+                                float* __restrict__ out)
+{
+    const long long total = ncell * nslices;
+    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < total;
+         o += (long long)gridDim.x * blockDim.x) {
+        const long long cell = o / nslices;
+        const int s = (int)(o % nslices);
+        const long long src = cell_src[cell] + ring_src[s];
+        float acc = 0.f;
+        for (int b = 0; b < nbins; ++b) acc += fmaxf(__ldg(in + b * bin_stride + src), 0.f);
+        out[o] = acc;
+    }
+}
+
+// ---------------------------------------------------------------- tail mask
+
+struct MaskParams {
+    Grid g;
+    const float* mu;            // attenuation, or activity when use_activity
+    int use_activity;
+    long long nvox;
+    const double* geom;
+    const int16_t* lor;
+    const int16_t* sino;
+    int nr, nd, na, af, cap;
+    uint8_t* out;
+    int32_t* status;
+};
+
+__global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
+{
+    const long long n = (long long)P.nr * P.nr * P.na * P.na;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const LorIndex L = lor_of(id, P.nr, P.na);
+    const int d1 = L.i1 * P.af, d2 = L.i2 * P.af;
+    if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // TailsMask.py:129
+    double lc[6];
+    lor_line(P.geom, P.nd, L.r1, d1, L.r2, d2, lc);
+    double acf = 1.0;  // a miss gives Attenuation = 1 (:146-148)
+    Ray r;
+    if (ray_setup(P.g, lc, 1e-20, r)) {
+        double sum = 0.0;
+        bool bad = false;
+        int c = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
+            const long long v = lin - 1;
+            if (v < 0 || v >= P.nvox) {
+                bad = true;
+                return;
+            }
+            sum = add64(sum, mul64((double)__ldg(P.mu + v), ref_length(r, t0, t1)));
+        });
+        if (c < 0) raise_error(P.status, kErrOverrun);
+        if (bad) raise_error(P.status, kErrVoxel);
+        acf = P.use_activity ? (sum > 0.0 ? 0.0 : 1.0) : div64(1.0, exp(-sum));  // :144-156
+    }
+    if (acf == 1.0) {  // :150-161, one LOR per (cell, slice)
+        const int ang = P.lor[2 * ((long long)d1 * P.nd + d2)];
+        const int rad = P.lor[2 * ((long long)d1 * P.nd + d2) + 1];
+        if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2) {  // unset coordinates
+            raise_error(P.status, kErrCapacity);
+            return;
+        }
+        const long long nsino = (long long)P.nr * P.nr;
+        const long long cell = (long long)rad * (P.nd / 2) + ang;
+        P.out[cell * nsino + P.sino[L.r1 * P.nr + L.r2]] = 1;
+    }
+}
+
+// ---------------------------------------------------------------- back-projection fit
+
+struct FitParams {
+    Grid g;
+    long long nvox;
+    const double* geom;
+    const int16_t* lor;
+    const int16_t* order;       // [nr][nr]: slice read by the LOR (Ring1, Ring2) (:157-176)
+    int nr, nd, na, af, cap;
+    const float* prompts;       // [cell][slice]
+    const float* randoms;
+    const float* mask_f32;      // either a float mask (multiplied, :157-167) ...
+    const uint8_t* mask_u8;     // ... or a uint8 tail mask (mask >= 1, Scaling.py:76)
+    const float* scat;          // scatter values, addressed through the tables below
+    const long long* scat_cell; // [cell] offset of the scatter value's cell
+    const long long* scat_ring; // [slice] offset of the scatter value's slice
+    int scat_clamp;             // clamp the scatter value at 0 (upsampling's fill, :163)
+    float* img;                 // 4 x nvox: P, S, R, sensitivity
+    int32_t* status;
+};
+
+__global__ void __launch_bounds__(128) bp_kernel(FitParams P)
+{
+    const long long n = (long long)P.nr * P.nr * P.na * P.na;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const LorIndex L = lor_of(id, P.nr, P.na);
+    const int d1 = L.i1 * P.af, d2 = L.i2 * P.af;
+    if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // BackProjection.py:88
+    const int ang = P.lor[2 * ((long long)d1 * P.nd + d2)];
+    const int rad = P.lor[2 * ((long long)d1 * P.nd + d2) + 1];
+    const int slice = P.order[L.r1 * P.nr + L.r2];
+    if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2 || slice < 0 || slice >= P.nr * P.nr) {
+        raise_error(P.status, kErrCapacity);  // unset coordinates or a bad slice order
+        return;
+    }
+    const long long cell = (long long)rad * (P.nd / 2) + ang;
+    const long long c = cell * ((long long)P.nr * P.nr) + slice;
+    const float m = P.mask_u8 ? (P.mask_u8[c] >= 1 ? 1.f : 0.f) : P.mask_f32[c];
+    float sv = P.scat[P.scat_cell[cell] + P.scat_ring[slice]];
+    if (P.scat_clamp) sv = fmaxf(sv, 0.f);
+    const float s = m * sv;
+    if (s == 0.f) return;  // :99-100
+    const float pv = m * P.prompts[c], rv = m * P.randoms[c];
+    double lc[6];
+    lor_line(P.geom, P.nd, L.r1, d1, L.r2, d2, lc);
+    Ray r;
+    if (!ray_setup(P.g, lc, 1e-20, r)) return;
+    // first pass: voxel count (the reference divides by len(Lengths), :108-110)
+    Ray r2 = r;
+    int n_vox = ray_walk(P.g, r2, P.cap, [](int, int64_t, double, double) {});
+    if (n_vox < 0) {
+        raise_error(P.status, kErrOverrun);
+        return;
+    }
+    if (n_vox == 0) return;
+    const float fn = (float)n_vox;
+    const float ap = pv / fn, as = s / fn, ar = rv / fn;
+    bool bad = false;
+    ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double, double) {
+        const long long v = lin - 1;
+        if (v < 0 || v >= P.nvox) {
+            bad = true;
+            return;
+        }
+        atomicAdd(P.img + v, ap);
+        atomicAdd(P.img + P.nvox + v, as);
+        atomicAdd(P.img + 2 * P.nvox + v, ar);
+        atomicAdd(P.img + 3 * P.nvox + v, 1.0f);
+    });
+    if (bad) raise_error(P.status, kErrVoxel);
+}
+
+// per voxel: Sbp, T (BackProjection.py:191-204); sums of x*T and x*x in FP64
+__global__ void fit_reduce_kernel(const float* __restrict__ img, long long nvox, double* sums)
+{
+    double sxt = 0.0, sxx = 0.0;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nvox;
+         v += (long long)gridDim.x * blockDim.x) {
+        const float sens = img[3 * nvox + v];
+        float sb = img[nvox + v] / sens;
+        float ab = img[v] / sens;
+        float rb = img[2 * nvox + v] / sens;
+        if (isnan(sb) || isinf(sb)) sb = 0.f;
+        if (isnan(ab) || isinf(ab)) ab = 0.f;
+        if (isnan(rb) || isinf(rb)) rb = 0.f;
+        float t = ab - rb;
+        if (t < 0.f) t = 0.f;
+        const float x = (float)((double)sb * 1e10);  // float32 array * 1e10 (:207)
+        sxt += (double)x * (double)t;
+        sxx += (double)x * (double)x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sxt += __shfl_xor_sync(0xffffffffu, sxt, o);
+        sxx += __shfl_xor_sync(0xffffffffu, sxx, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(sums, sxt);
+        atomicAdd(sums + 1, sxx);
+    }
+}
+
+// lstsq of one column through the origin (:207-210): minimum-norm solution
+// sum(xT)/sum(x^2) (0 when x is all zero), cast to float32, times 1e10.
+__global__ void fit_final_kernel(const double* sums, float* scale)
+{
+    const double a = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+    *scale = (float)((double)(float)a * 1e10);
+}
+
+int check_grid(const int32_t* grid, const double* bounds, const char* who)
+{
+    if (!grid || !bounds) return sss_set_error(SSS_ERR_INVALID, "%s: null grid", who);
+    if (grid[0] < 1 || grid[1] < 1 || grid[2] < 1)
+        return sss_set_error(SSS_ERR_INVALID, "%s: grid must be positive", who);
+    if (!(bounds[3] > bounds[0] && bounds[4] > bounds[1] && bounds[5] > bounds[2]))
+        return sss_set_error(SSS_ERR_INVALID, "%s: bounds must satisfy max > min", who);
+    return SSS_OK;
+}
+
+Grid make_grid(const int32_t* grid, const double* bounds)
+{
+    Grid g;
+    g.nx = grid[0];
+    g.ny = grid[1];
+    g.nz = grid[2];
+    for (int k = 0; k < 6; ++k) g.b[k] = bounds[k];
+    return g;
+}
+
+unsigned blocks_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+extern "C" int sss_upsample(const float* sampled, int64_t bin_stride, int32_t nbins,
+                            const int64_t* cell_src, const int64_t* ring_src, int64_t ncell,
+                            int32_t nslices, float* out, void* stream)
+{
+    if (!sampled || !cell_src || !ring_src || !out || nbins < 1 || ncell < 1 || nslices < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sss_upsample: bad argument");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long total = (long long)ncell * nslices;
+    const long long want = (total + 255) / 256;
+    const unsigned blocks = (unsigned)(want < (long long)sms * 32 ? want : (long long)sms * 32);
+    upsample_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(
+        sampled, bin_stride, nbins, (const long long*)cell_src, (const long long*)ring_src, ncell,
+        nslices, out);
+    return sss_check_launch("upsample_kernel");
+}
+
+extern "C" int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float* map,
+                             int32_t use_activity, int32_t nr, int32_t nd, const double* geometry,
+                             const int16_t* lor, const int16_t* sino_index, int32_t af, uint8_t* out,
+                             int32_t* status, void* stream)
+{
+    int rc = check_grid(grid, bounds, "sss_tail_mask");
+    if (rc) return rc;
+    if (!map || !geometry || !lor || !sino_index || !out || nr < 1 || nd < 2 || af < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask: bad argument");
+    MaskParams P;
+    P.g = make_grid(grid, bounds);
+    P.mu = map;
+    P.use_activity = use_activity;
+    P.nvox = (long long)grid[0] * grid[1] * grid[2];
+    P.geom = geometry;
+    P.lor = lor;
+    P.sino = sino_index;
+    P.nr = nr;
+    P.nd = nd;
+    P.af = af;
+    P.na = (nd + af - 1) / af;
+    P.cap = grid[0] + grid[1] + grid[2];
+    P.out = out;
+    P.status = status;
+    const long long n = (long long)nr * nr * P.na * P.na;
+    mask_kernel<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(P);
+    return sss_check_launch("mask_kernel");
+}
+
+extern "C" int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr,
+                                   int32_t nd, const double* geometry, const int16_t* lor,
+                                   const int16_t* sino_order, int32_t af, const float* prompts,
+                                   const float* randoms, const float* mask_f32,
+                                   const uint8_t* mask_u8, const float* scatters,
+                                   const int64_t* scat_cell, const int64_t* scat_ring,
+                                   int32_t scat_clamp, float* images, double* sums, float* scale,
+                                   int32_t* status, void* stream)
+{
+    int rc = check_grid(grid, bounds, "sss_backproject_fit");
+    if (rc) return rc;
+    if (!geometry || !lor || !sino_order || !prompts || !randoms || (!mask_f32 && !mask_u8) ||
+        !scatters || !scat_cell || !scat_ring || !images || !sums || !scale || nr < 1 || nd < 2 ||
+        af < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    FitParams P;
+    P.g = make_grid(grid, bounds);
+    P.nvox = (long long)grid[0] * grid[1] * grid[2];
+    P.geom = geometry;
+    P.lor = lor;
+    P.order = sino_order;
+    P.nr = nr;
+    P.nd = nd;
+    P.af = af;
+    P.na = (nd + af - 1) / af;
+    P.cap = grid[0] + grid[1] + grid[2];
+    P.prompts = prompts;
+    P.randoms = randoms;
+    P.mask_f32 = mask_u8 ? nullptr : mask_f32;
+    P.mask_u8 = mask_u8;
+    P.scat = scatters;
+    P.scat_cell = (const long long*)scat_cell;
+    P.scat_ring = (const long long*)scat_ring;
+    P.scat_clamp = scat_clamp;
+    P.img = images;
+    P.status = status;
+    if (cudaMemsetAsync(images, 0, sizeof(float) * 4 * P.nvox, st) != cudaSuccess ||
+        cudaMemsetAsync(sums, 0, 2 * sizeof(double), st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_backproject_fit: memset failed");
+    const long long n = (long long)nr * nr * P.na * P.na;
+    bp_kernel<<<blocks_for(n, 128), 128, 0, st>>>(P);
+    if ((rc = sss_check_launch("bp_kernel"))) return rc;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = (P.nvox + 255) / 256;
+    fit_reduce_kernel<<<(unsigned)(want < sms * 4 ? want : sms * 4), 256, 0, st>>>(images, P.nvox, sums);
+    if ((rc = sss_check_launch("fit_reduce_kernel"))) return rc;
+    fit_final_kernel<<<1, 1, 0, st>>>(sums, scale);
+    return sss_check_launch("fit_final_kernel");
+}

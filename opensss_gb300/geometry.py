@@ -119,3 +119,53 @@ def ring_nearest(nr_rings: int, rings: np.ndarray) -> np.ndarray:
         frac = (r - rings[i]) / (rings[i + 1] - rings[i])
         out[r] = i if frac <= 0.5 else i + 1
     return out
+
+
+def slice_rings(sino_index: np.ndarray) -> np.ndarray:
+    """Inverse of SinogramIndex: int64 [NR*NR, 2] ring pair (Ring1, Ring2) of each slice."""
+    si = np.asarray(sino_index, dtype=np.int64)
+    nr = si.shape[0]
+    inv = np.full((nr * nr, 2), -1, dtype=np.int64)
+    r1, r2 = np.meshgrid(np.arange(nr), np.arange(nr), indexing="ij")
+    inv[si.reshape(-1), 0] = r1.reshape(-1)
+    inv[si.reshape(-1), 1] = r2.reshape(-1)
+    if (inv < 0).any():
+        raise ValueError("SinogramIndex is not a permutation of the slices")
+    return inv
+
+
+def upsample_tables(lor, sino_index, nru: int, ndu: int, layout: str = "dense"):
+    """Gather tables of the upsampling (Interpolation.py:197-319):
+    full-sinogram value (cell, slice) = sampled[cell_src[cell] + ring_src[slice]]
+    (per TOF bin, plus bin * bin_stride).
+
+    layout 'dense'  : the reference's sampled array [bins][ND+1][ND/2][NRU^2]
+    layout 'legpair': the engine's [bins][NL][NL], leg = crystal_index*NRU + ring_index
+    Returns (cell_src int64 [(ND+1)*(ND/2)], ring_src int64 [NR*NR], bin_stride)."""
+    lor = np.asarray(lor)
+    nd = lor.shape[0]
+    nr = np.asarray(sino_index).shape[0]
+    det = sampled_detectors(nd, ndu)
+    rings = sampled_rings(nr, nru)
+    src = upsample_source(lor, det).astype(np.int64)
+    a, b = np.divmod(src, ndu)
+    rmap = ring_nearest(nr, rings).astype(np.int64)
+    inv = slice_rings(sino_index)
+    # slice (r1, r2) copies the sampled pair (nearest(r1), nearest(r2)) (:251-310)
+    ri1, ri2 = rmap[inv[:, 0]], rmap[inv[:, 1]]
+    if layout == "dense":
+        rad = lor[det[a], det[b], 1].astype(np.int64)
+        ang = lor[det[a], det[b], 0].astype(np.int64)
+        cell_src = (rad * (nd // 2) + ang) * (nru * nru)
+        ring_src = ri1 * nru + ri2
+        stride = (nd + 1) * (nd // 2) * nru * nru
+    elif layout == "legpair":
+        nl = nru * ndu
+        lo, hi = np.minimum(a, b), np.maximum(a, b)
+        cell_src = lo * nru * nl + hi * nru
+        ring_src = ri1 * nl + ri2
+        stride = nl * nl
+    else:
+        raise ValueError(layout)
+    return (np.ascontiguousarray(cell_src.reshape(-1), dtype=np.int64),
+            np.ascontiguousarray(ring_src, dtype=np.int64), int(stride))

@@ -1,0 +1,129 @@
+"""GPU upsampling, tail mask and back-projection fit against the reference's outputs."""
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _sino(nd, nr):
+    from opensss_gb300.geometry import SinogramCoordinates
+
+    return SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_interpolate_scatters_matches_reference(cuda_ok, tmp_path, case):
+    from opensss_gb300.Interpolation import InterpolateScatters
+
+    g = golden("upsample")
+    nd, nr, nru, ndu, nb = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = _sino(nd, nr)
+    dense = O.densify(g[f"case{case}_compact"].astype(np.float64), lor, nd, nru, ndu)
+    out = InterpolateScatters(dense, nr, nru, nd, ndu, lor, si, str(tmp_path), False)
+    assert out.dtype == np.float32
+    assert np.array_equal(out, g[f"case{case}_sum"])  # bit-exact, bins summed in order
+    for b in range(nb):
+        saved = np.load(tmp_path / f"SSS_mashed_bin{b}.npz")["arr_0"]
+        assert np.array_equal(saved, g[f"case{case}_bins"][b])
+
+
+def test_upsample_from_engine_layout(cuda_ok):
+    """The engine's leg-pair output upsamples to the same sinogram."""
+    import torch
+
+    from opensss_gb300 import geometry as G
+    from opensss_gb300.Interpolation import upsample_device
+
+    g = golden("upsample")
+    nd, nr, nru, ndu, nb = (int(v) for v in g["case0_dims"])
+    lor, si, _ = _sino(nd, nr)
+    cmp = g["case0_compact"]
+    lp = cmp.reshape(nb, nru, nru, ndu, ndu).transpose(0, 3, 1, 4, 2).reshape(nb, nru * ndu, nru * ndu)
+    t = G.upsample_tables(lor, si, nru, ndu, "legpair")
+    out = upsample_device(torch.from_numpy(np.ascontiguousarray(lp)).cuda(), t, nb,
+                          (nd + 1) * (nd // 2), nr * nr)
+    assert np.array_equal(out.cpu().numpy().reshape(nd + 1, nd // 2, nr * nr), g["case0_sum"])
+
+
+@pytest.mark.parametrize("case", range(3))
+def test_tail_mask_matches_reference_bit_exact(cuda_ok, case):
+    from opensss_gb300.TailsMask import MaskGenerator
+
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = _sino(nd, nr)
+    mu = g[f"case{case}_mu"]
+    m = MaskGenerator(np.ones_like(mu), mu, g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor,
+                      si, True, af)
+    assert m.dtype == np.uint8
+    assert np.array_equal(m, g[f"case{case}_mask"])
+
+
+def test_activity_mask_matches_oracle_rule(cuda_ok):
+    """UseAttenuation=False marks LORs that see no activity (TailsMask.py:153-161)."""
+    from opensss_gb300.TailsMask import MaskGenerator
+
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g["case0_dims"])
+    lor, si, _ = _sino(nd, nr)
+    mu = g["case0_mu"]
+    act = (mu > 0.05).astype(np.float32)  # activity only inside the water
+    m_act = MaskGenerator(act, mu, g["case0_bounds"], g["case0_geometry"], lor, si, False, af)
+    m_mu = MaskGenerator(act, mu, g["case0_bounds"], g["case0_geometry"], lor, si, True, af)
+    # every LOR that misses the attenuation also misses the activity inside it
+    assert np.all(m_act >= m_mu)
+    assert m_act.sum() > m_mu.sum()
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_backprojection_fit_matches_reference(cuda_ok, case):
+    from opensss_gb300.BackProjection import BackProjectionScatterRandFit
+
+    g = golden("fit")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = _sino(nd, nr)
+    s = BackProjectionScatterRandFit(g[f"case{case}_prompts"], g[f"case{case}_scatter"],
+                                     g[f"case{case}_randoms"], g[f"case{case}_mask"],
+                                     g[f"case{case}_grid"], g[f"case{case}_bounds"],
+                                     g[f"case{case}_geometry"], lor, si[:nr, :nr].T, af)
+    ref = g[f"case{case}_scale"]
+    assert s.dtype == np.float32 and s.shape == (1,)
+    assert abs(float(s[0]) - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
+
+
+def test_fit_reads_upsampled_scatter_without_materialising(cuda_ok):
+    """Fused path: the fit reads the sampled (leg-pair) sinogram through the
+    upsampling tables; same scale as fitting the materialised upsampled
+    sinogram with the FP64 oracle."""
+    import torch
+
+    from opensss_gb300 import geometry as G, workloads as W
+    from opensss_gb300.BackProjection import fit_device
+
+    g = golden("upsample")
+    nd, nr, nru, ndu, nb = (int(v) for v in g["case1_dims"])
+    lor, si, _ = _sino(nd, nr)
+    cmp = g["case1_compact"]
+    lp = cmp.reshape(nb, nru, nru, ndu, ndu).transpose(0, 3, 1, 4, 2).reshape(nb, nru * ndu, nru * ndu)
+    up = g["case1_bins"][0]
+    sc = W.ring_scanner(nd, nr, radius_cm=20.3, ring_pitch_cm=1.1)
+    rng = np.random.default_rng(3)
+    shp = up.shape
+    prm = rng.poisson(3.0, size=shp).astype(np.float32)
+    rnd = np.full(shp, 0.1, np.float32)
+    mask = (rng.uniform(size=shp) < 0.5).astype(np.float32)
+    grid = np.array([10, 10, 8])
+    bounds = np.array([-8.0, -8.0, -6.0, 8.0, 8.0, 6.0])
+    order = si[:nr, :nr].T
+    ref = O.fit(prm, up, rnd, mask, grid, bounds, sc.geometry, lor, order, 1)
+    cell, ring, _ = G.upsample_tables(lor, si, nru, ndu, "legpair")
+    dev = "cuda"
+    flat = lambda a: torch.from_numpy(np.ascontiguousarray(a.reshape(-1, nr * nr))).to(dev)  # noqa: E731
+    s = fit_device(flat(prm), flat(rnd), flat(mask),
+                   torch.from_numpy(np.ascontiguousarray(lp[0])).to(dev), cell, ring, grid, bounds,
+                   sc.geometry, lor, order, 1, scat_clamp=True)
+    assert abs(s - float(ref[0])) <= 1e-5 * abs(float(ref[0]))

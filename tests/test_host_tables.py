@@ -84,3 +84,36 @@ def test_sampled_detectors_reference_rule():
     assert G.sampled_detectors(760, 32)[:4].tolist() == [0, 23, 46, 69]
     assert G.sampled_detectors(760, 96)[-1] == 665
     assert G.sampled_rings(80, 16)[[0, -1]].tolist() == [0, 79]
+
+
+def _legpair_from_compact(cmp, nru, ndu):
+    """[B, NRU^2, NDU, NDU] (sino = ri1*NRU + ri2) -> leg-pair [B, NL, NL]."""
+    b = cmp.shape[0]
+    x = cmp.reshape(b, nru, nru, ndu, ndu).transpose(0, 3, 1, 4, 2)
+    return x.reshape(b, ndu * nru, ndu * nru)
+
+
+@pytest.mark.parametrize("case", range(2))
+@pytest.mark.parametrize("layout", ["dense", "legpair"])
+def test_upsample_gather_tables_reproduce_reference(case, layout):
+    """The gather tables the upsampling kernel reads, applied with numpy,
+    reproduce the reference's InterpolateAllBins output exactly."""
+    from oracle import oracle as O
+
+    g = golden("upsample")
+    nd, nr, nru, ndu, nb = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    cmp = g[f"case{case}_compact"]
+    if layout == "dense":
+        src = O.densify(cmp.astype(np.float64), lor, nd, nru, ndu).astype(np.float32)
+    else:
+        src = _legpair_from_compact(cmp, nru, ndu)
+    cell, ring, stride = G.upsample_tables(lor, si, nru, ndu, layout)
+    flat = src.reshape(-1)
+    idx = cell[:, None] + ring[None, :]
+    total = np.zeros(idx.shape, np.float32)
+    for b in range(nb):
+        vb = np.maximum(flat[b * stride + idx], 0)
+        assert np.array_equal(vb.reshape(nd + 1, nd // 2, nr * nr), g[f"case{case}_bins"][b])
+        total += vb
+    assert np.array_equal(total.reshape(nd + 1, nd // 2, nr * nr), g[f"case{case}_sum"])
