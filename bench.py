@@ -286,6 +286,8 @@ def run_ours(args, rank, world, local_rank):
         got = leg_pair_to_compact(sub, pr.nr_rings_used, pr.nr_detectors_used)
         err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
 
+    pipeline = None if args.no_pipeline else run_pipeline(eng, pr, out, dev, args)
+
     ms = 1e3 * total_s / args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -298,8 +300,71 @@ def run_ours(args, rank, world, local_rank):
                     "path": "TofSSS.run on pinned host volumes, compact result copied back"},
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
-            "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu}
+            "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline}
     print(json.dumps(line), flush=True)
+
+
+def run_pipeline(eng, pr, sampled, dev, args):
+    """Downstream rows on the same scanner: upsampling of all bins, tail mask,
+    and the per-bin scale fit, each timed with CUDA events.  Prompts are
+    seeded Poisson draws of 1.4 x the upsampled scatter plus flat randoms
+    (trues are zero on the tail LORs the fit uses), so every fitted scale
+    should come out near 1.4."""
+    import torch
+
+    from opensss_gb300 import geometry as G
+    from opensss_gb300.BackProjection import fit_device
+    from opensss_gb300.Interpolation import upsample_device
+    from opensss_gb300.TailsMask import tail_mask_device
+
+    nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    tables = G.upsample_tables(lor, si, pr.nr_rings_used, pr.nr_detectors_used, "legpair")
+    ncell, nsl = (nd + 1) * (nd // 2), nr * nr
+    cs = torch.from_numpy(tables[0]).to(dev)
+    rs = torch.from_numpy(tables[1]).to(dev)
+    t_tables = (cs, rs, tables[2])
+    st = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        r = fn()
+        e1.record(st)
+        e1.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    up = torch.empty((ncell, nsl), dtype=torch.float32, device=dev)
+    upsample_device(sampled, t_tables, pr.nr_bins, ncell, nsl, out=up)
+    _, up_ms = timed(lambda: upsample_device(sampled, t_tables, pr.nr_bins, ncell, nsl, out=up))
+    af = args.af
+    mask, mask_ms = timed(lambda: tail_mask_device(pr.attenuation, pr.image_size, pr.scanner.geometry,
+                                                   lor, si, af, device=dev))
+    fit_grid = np.array([40, 40, 26])
+    zr = float(pr.scanner.geometry[-1, 0, 2]) + 0.16
+    fit_bounds = np.array([pr.image_size[0], pr.image_size[1], -zr, pr.image_size[3], pr.image_size[4], zr])
+    order = si[:nr, :nr].T
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    randoms = None
+    scales, fit_ms = [], []
+    for b in range(pr.nr_bins):
+        upsample_device(sampled, t_tables, pr.nr_bins, ncell, nsl, bin_index=b, out=up)
+        if randoms is None:
+            randoms = torch.full_like(up, 0.1 * float(up.mean()))
+        prompts = torch.poisson(1.4 * up + randoms, generator=gen)
+        bin_view = sampled[b]
+        s, ms = timed(lambda: fit_device(prompts, randoms, mask, bin_view, cs, rs, fit_grid, fit_bounds,
+                                         pr.scanner.geometry, lor, order, af, scat_clamp=True,
+                                         device=dev))
+        scales.append(s)
+        fit_ms.append(ms)
+        del prompts
+    n_mask_lors = int(mask.sum())
+    return {"upsample_all_bins_ms": up_ms, "upsample_gbs": ncell * nsl * 4 / (up_ms * 1e-3) / 1e9,
+            "tail_mask_ms": mask_ms, "mask_af": af, "masked_bins": n_mask_lors,
+            "fit_ms_per_bin": statistics.mean(fit_ms), "fitted_scales": scales,
+            "expected_scale": 1.4, "full_sinogram": [nd + 1, nd // 2, nsl]}
 
 
 def _sfu_peak(clocks):
@@ -337,6 +402,8 @@ def main():
     ap.add_argument("--ref-points", type=int, default=1024,
                     help="scatter points in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-pipeline", action="store_true", help="skip upsampling / mask / fit timings")
+    ap.add_argument("--af", type=int, default=6, help="AccelerationFactor of the mask and fit")
     ap.add_argument("--max-points", type=int, default=None,
                     help="limit each step to the first scatter points (profiling runs only)")
     args = ap.parse_args()

@@ -235,7 +235,7 @@ def densify(compact, lor, nd, nru, ndu):
 # ---------------------------------------------------------------- mask / fit
 
 
-def mask(mu, image_size, geometry, lor, sino_index, af, nthreads=0):
+def mask(mu, image_size, geometry, lor, sino_index, af, nthreads=0, use_activity=False):
     grid = np.ascontiguousarray(mu.shape, dtype=np.int64)
     muf = np.ascontiguousarray(mu.flatten(order="F"), dtype=np.float32)
     gb = np.ascontiguousarray(image_size, dtype=np.float64)
@@ -245,7 +245,8 @@ def mask(mu, image_size, geometry, lor, sino_index, af, nthreads=0):
     nr, nd = geom.shape[:2]
     out = np.zeros((nd + 1, nd // 2, nr * nr), np.uint8)
     st = lib().orc_mask(_p(grid), _p(muf), _p(gb), C.c_int64(nr), C.c_int64(nd), _p(geom), _p(lor),
-                        _p(si), C.c_int64(af), _p(out), C.c_int(nthreads))
+                        _p(si), C.c_int64(af), C.c_int(int(use_activity)), _p(out),
+                        C.c_int(nthreads))
     if st:
         raise RuntimeError(f"oracle mask failed {st}")
     return out

@@ -465,11 +465,12 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
 }
 
 /* ------------------------------------------------------------------------ */
-/* MaskDetectors / MaskGenerator (TailsMask.py:84-228), attenuation rule.
+/* MaskDetectors / MaskGenerator (TailsMask.py:84-228); `mu` is the activity
+ * map when use_activity (the UseAttenuation=False rule).
  * out: uint8 [(nd+1)][nd/2][nr*nr], slice SinogramIndex[Ring1, Ring2]. */
 int orc_mask(const int64_t *grid, const float *mu, const double *gb, int64_t nr, int64_t nd,
              const double *geom, const int16_t *lor, const int16_t *sino_index, int64_t af,
-             uint8_t *out, int nthreads)
+             int use_activity, uint8_t *out, int nthreads)
 {
     const int64_t nang = nd / 2, nsino = nr * nr;
     const int cap = (int)(grid[0] + grid[1] + grid[2]);
@@ -500,7 +501,8 @@ int orc_mask(const int64_t *grid, const float *mu, const double *gb, int64_t nr,
                     if (n != 0) {
                         double s = 0;
                         for (int k = 0; k < n; ++k) s += (double)mu[ix[k] - 1] * len[k];
-                        att = 1 / exp(-s);
+                        /* attenuation rule :145, activity rule :144 and :153-156 */
+                        att = use_activity ? (s > 0 ? 0.0 : 1.0) : 1 / exp(-s);
                     } else {
                         att = 1;
                     }

@@ -63,20 +63,21 @@ def test_tail_mask_matches_reference_bit_exact(cuda_ok, case):
     assert np.array_equal(m, g[f"case{case}_mask"])
 
 
-def test_activity_mask_matches_oracle_rule(cuda_ok):
+def test_activity_mask_matches_oracle(cuda_ok):
     """UseAttenuation=False marks LORs that see no activity (TailsMask.py:153-161)."""
+    from opensss_gb300 import workloads as W
     from opensss_gb300.TailsMask import MaskGenerator
 
     g = golden("mask")
     nd, nr, af = (int(v) for v in g["case0_dims"])
     lor, si, _ = _sino(nd, nr)
     mu = g["case0_mu"]
-    act = (mu > 0.05).astype(np.float32)  # activity only inside the water
+    act, _, _ = W.cylinder_phantom(mu.shape, 2.0, seed=0, radius_cm=3.0)  # activity in a 3 cm core
     m_act = MaskGenerator(act, mu, g["case0_bounds"], g["case0_geometry"], lor, si, False, af)
+    ref = O.mask(act, g["case0_bounds"], g["case0_geometry"], lor, si, af, use_activity=True)
+    assert np.array_equal(m_act, ref)
     m_mu = MaskGenerator(act, mu, g["case0_bounds"], g["case0_geometry"], lor, si, True, af)
-    # every LOR that misses the attenuation also misses the activity inside it
-    assert np.all(m_act >= m_mu)
-    assert m_act.sum() > m_mu.sum()
+    assert np.all(m_act >= m_mu) and m_act.sum() > m_mu.sum()
 
 
 @pytest.mark.parametrize("case", range(2))
@@ -119,7 +120,7 @@ def test_fit_reads_upsampled_scatter_without_materialising(cuda_ok):
     grid = np.array([10, 10, 8])
     bounds = np.array([-8.0, -8.0, -6.0, 8.0, 8.0, 6.0])
     order = si[:nr, :nr].T
-    ref = O.fit(prm, up, rnd, mask, grid, bounds, sc.geometry, lor, order, 1)
+    ref = O.fit(prm, up, rnd, mask, grid, bounds, sc.geometry, lor, si, 1)  # the oracle transposes
     cell, ring, _ = G.upsample_tables(lor, si, nru, ndu, "legpair")
     dev = "cuda"
     flat = lambda a: torch.from_numpy(np.ascontiguousarray(a.reshape(-1, nr * nr))).to(dev)  # noqa: E731
