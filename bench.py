@@ -348,16 +348,18 @@ def run_pipeline(eng, pr, sampled, dev, args):
     gen.manual_seed(7)
     randoms = None
     scales, fit_ms = [], []
+    counts_per_unit = None  # SSS values are probabilities: scale them to counts
     for b in range(pr.nr_bins):
         upsample_device(sampled, t_tables, pr.nr_bins, ncell, nsl, bin_index=b, out=up)
         if randoms is None:
-            randoms = torch.full_like(up, 0.1 * float(up.mean()))
-        prompts = torch.poisson(1.4 * up + randoms, generator=gen)
+            counts_per_unit = 20.0 / max(float(up.mean()), 1e-30)
+            randoms = torch.full_like(up, 0.1 * 1.4 * 20.0)
+        prompts = torch.poisson(1.4 * counts_per_unit * up + randoms, generator=gen)
         bin_view = sampled[b]
         s, ms = timed(lambda: fit_device(prompts, randoms, mask, bin_view, cs, rs, fit_grid, fit_bounds,
                                          pr.scanner.geometry, lor, order, af, scat_clamp=True,
                                          device=dev))
-        scales.append(s)
+        scales.append(s / counts_per_unit)
         fit_ms.append(ms)
         del prompts
     n_mask_lors = int(mask.sum())
