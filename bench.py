@@ -348,11 +348,11 @@ def run_pipeline(eng, pr, sampled, dev, args):
     gen.manual_seed(7)
     randoms = None
     scales, fit_ms = [], []
-    counts_per_unit = None  # SSS values are probabilities: scale them to counts
     for b in range(pr.nr_bins):
         upsample_device(sampled, t_tables, pr.nr_bins, ncell, nsl, bin_index=b, out=up)
+        # SSS values are probabilities: scale each bin to ~20 counts per bin on average
+        counts_per_unit = 20.0 / max(float(up.mean()), 1e-30)
         if randoms is None:
-            counts_per_unit = 20.0 / max(float(up.mean()), 1e-30)
             randoms = torch.full_like(up, 0.1 * 1.4 * 20.0)
         prompts = torch.poisson(1.4 * counts_per_unit * up + randoms, generator=gen)
         bin_view = sampled[b]

@@ -30,10 +30,9 @@ using namespace sss;
 constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
 constexpr int kMaxWaveSlices = 256;
 constexpr int kPairWarps = 8;  // warps per pair-kernel block
-// pair-kernel shared memory: log2 weight table (floats), bin table (bytes),
-// then 32 float2 voxels per warp starting on a 16-byte boundary
-constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
-constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
+// pair-kernel shared memory: (log2 largest weight, its bin) per TOF offset
+// as float2, then 32 float2 voxels per warp starting on a 16-byte boundary
+constexpr int kSmemVbufFloats = (2 * kTofEntries + 3) & ~3;
 static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
 struct LatticeDims {
@@ -259,10 +258,10 @@ __device__ __noinline__ int energy_row_fp64(const PairParams& P, int s, int ri1,
 // largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
 // between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Bins go two
 // at a time through packed FP32x2 instructions; NP = number of bin pairs.
-template <int NP, bool SINGLE>
+template <int NP, bool SINGLE, bool ODD>
 __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
-                                                 const float* sY, const unsigned char* sN,
-                                                 const PairParams& P, bool& tof_bad)
+                                                 const float2* sYN, const PairParams& P,
+                                                 bool& tof_bad)
 {
     // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
     const float y = __fadd_rd(x, 12582912.0f);
@@ -277,8 +276,8 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
             return;
         }
     }
-    const float Y = sY[t];
-    const float n = (float)sN[t];
+    const float2 yn = sYN[t];
+    const float Y = yn.x, n = yn.y;
     // beta = 2 kappa w (off - s_n), s_n = s0 + n w
     const float beta = P.kappa2w * (off - fmaf(n, P.w, P.s0));
     if constexpr (SINGLE) {
@@ -292,7 +291,9 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
         for (int k = 0; k < NP; ++k) {
             const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
             const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
-            acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), ex2(e2.y)), acc[k]);
+            // with an odd bin count the last pair's second bin does not exist
+            const float wy = (ODD && k + 1 == NP) ? 0.f : ex2(e2.y);
+            acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), wy), acc[k]);
             if (k + 1 < NP) nd = __fadd2_rn(nd, two);
         }
     }
@@ -307,17 +308,14 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
 // same per-slice count.  All lanes walk the same voxel list: 32 voxels at a
 // time are staged in a per-warp shared buffer and read back as broadcasts,
 // so the trip count is uniform across the warp.
-template <int NP, bool SINGLE, int MINB>
+template <int NP, bool SINGLE, bool ODD, int MINB>
 __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
 {
     extern __shared__ float smem[];
-    float* sY = smem;
-    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
+    float2* sYN = reinterpret_cast<float2*>(smem);
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
-    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
-        sY[i] = P.tof_log2w[2 * i];
-        sN[i] = (unsigned char)P.tof_log2w[2 * i + 1];
-    }
+    const float2* gYN = reinterpret_cast<const float2*>(P.tof_log2w);
+    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) sYN[i] = gYN[i];
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -423,8 +421,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
                             const float2 v = vbuf[j];
-                            accumulate_voxel<NP, SINGLE>(acc, c * v.x, fmaf(sigma, v.y, u), sY, sN,
-                                                         P, tof_bad);
+                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u),
+                                                              sYN, P, tof_bad);
                         }
                     }
                 }
@@ -459,11 +457,11 @@ size_t pair_smem_bytes()
     return sizeof(float) * kSmemVbufFloats + sizeof(float2) * 32 * kPairWarps;
 }
 
-template <int NP, bool SINGLE>
+template <int NP, bool SINGLE, bool ODD>
 int launch_pairs(const PairParams& P, cudaStream_t st)
 {
     constexpr int MINB = NP <= 8 ? 3 : 2;
-    auto kern = pair_kernel<NP, SINGLE, MINB>;
+    auto kern = pair_kernel<NP, SINGLE, ODD, MINB>;
     const size_t smem = pair_smem_bytes();
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int dev = 0, sms = 0, per_sm = 0;
@@ -481,10 +479,11 @@ int launch_pairs(const PairParams& P, cudaStream_t st)
 
 int dispatch_pairs(const PairParams& P, cudaStream_t st)
 {
-    if (P.nbins == 1) return launch_pairs<1, true>(P, st);
+    if (P.nbins == 1) return launch_pairs<1, true, false>(P, st);
+    const bool odd = P.nbins & 1;
     switch ((P.nbins + 1) / 2) {
 #define SSS_NP(k) \
-    case k: return launch_pairs<k, false>(P, st);
+    case k: return odd ? launch_pairs<k, false, true>(P, st) : launch_pairs<k, false, false>(P, st);
         SSS_NP(1) SSS_NP(2) SSS_NP(3) SSS_NP(4) SSS_NP(5) SSS_NP(6) SSS_NP(7) SSS_NP(8)
         SSS_NP(9) SSS_NP(10) SSS_NP(11) SSS_NP(12) SSS_NP(13) SSS_NP(14) SSS_NP(15) SSS_NP(16)
         SSS_NP(17) SSS_NP(18) SSS_NP(19) SSS_NP(20) SSS_NP(21) SSS_NP(22) SSS_NP(23) SSS_NP(24)
