@@ -30,9 +30,10 @@ using namespace sss;
 constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
 constexpr int kMaxWaveSlices = 256;
 constexpr int kPairWarps = 8;  // warps per pair-kernel block
-// pair-kernel shared memory: (log2 largest weight, its bin) per TOF offset
-// as float2, then 32 float2 voxels per warp starting on a 16-byte boundary
-constexpr int kSmemVbufFloats = (2 * kTofEntries + 3) & ~3;
+// pair-kernel shared memory: log2 largest weight per TOF offset (floats),
+// its bin (bytes), then 32 float2 voxels per warp on a 16-byte boundary
+constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
+constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
 static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
 struct LatticeDims {
@@ -260,8 +261,8 @@ __device__ __noinline__ int energy_row_fp64(const PairParams& P, int s, int ri1,
 // at a time through packed FP32x2 instructions; NP = number of bin pairs.
 template <int NP, bool SINGLE, bool ODD>
 __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
-                                                 const float2* sYN, const PairParams& P,
-                                                 bool& tof_bad)
+                                                 const float* sY, const unsigned char* sN,
+                                                 const PairParams& P, bool& tof_bad)
 {
     // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
     const float y = __fadd_rd(x, 12582912.0f);
@@ -276,8 +277,8 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
             return;
         }
     }
-    const float2 yn = sYN[t];
-    const float Y = yn.x, n = yn.y;
+    const float Y = sY[t];
+    const float n = (float)sN[t];
     // beta = 2 kappa w (off - s_n), s_n = s0 + n w
     const float beta = P.kappa2w * (off - fmaf(n, P.w, P.s0));
     if constexpr (SINGLE) {
@@ -312,10 +313,13 @@ template <int NP, bool SINGLE, bool ODD, int MINB>
 __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
 {
     extern __shared__ float smem[];
-    float2* sYN = reinterpret_cast<float2*>(smem);
+    float* sY = smem;
+    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
-    const float2* gYN = reinterpret_cast<const float2*>(P.tof_log2w);
-    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) sYN[i] = gYN[i];
+    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
+        sY[i] = P.tof_log2w[2 * i];
+        sN[i] = (unsigned char)P.tof_log2w[2 * i + 1];
+    }
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
                         for (int j = 0; j < jn; ++j) {
                             const float2 v = vbuf[j];
                             accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u),
-                                                              sYN, P, tof_bad);
+                                                              sY, sN, P, tof_bad);
                         }
                     }
                 }
