@@ -138,6 +138,30 @@ int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t nd
                     const int16_t *lor, const int32_t *detectors, float *dense, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Batched simulation (no counterpart in the reference, which runs one
+ * SingleScatterSimulationTOF call per problem).  sss_batch_plan enumerates the
+ * scatter points of n problems (different volumes, scanners, samplings and
+ * bin counts allowed), cuts them into (problem, sampled z-slice) items and
+ * packs the items into waves that fit the workspace; each wave is one leg
+ * launch over all its items and one pair launch per TOF class (bin count and
+ * TOF kernel).  Everything lives in the caller's device workspace: the plan
+ * itself allocates no device memory.  It synchronises `stream` once.  outs[i]
+ * (device) receives problem i's output in the leg-pair layout of
+ * sss_tof_run.  sss_batch_run zeroes the outputs and enqueues the waves on
+ * `stream` without synchronising; it may run again after the activity maps
+ * change in place (the attenuation maps, which decide the scatter points,
+ * must not) and may be captured in a CUDA graph.  The problems' device
+ * arrays, the outputs and the workspace must outlive the plan's last run.
+ * sss_batch_info: info[0] waves, info[1] kernel launches per run, info[2]
+ * detector-pair x bin evaluations per run, info[3] scatter points. */
+typedef struct sss_batch sss_batch;
+int sss_batch_plan(const sss_tof_problem *problems, int32_t n, float *const *outs, void *workspace,
+                   size_t workspace_bytes, int32_t *status, sss_batch **plan, void *stream);
+int sss_batch_run(const sss_batch *plan, void *stream);
+int sss_batch_info(const sss_batch *plan, int64_t info[4]);
+void sss_batch_free(sss_batch *plan);
+
+/* ---------------------------------------------------------------------------
  * Upsampling.  Replaces InterpolateAllBins (Python/openSSS/Interpolation.py:197-319)
  * once its nearest-neighbour choices are known (geometry time, see
  * opensss_gb300/geometry.py): out[cell*nslices + s] = sum over the nbins bins

@@ -1,0 +1,103 @@
+"""Many TOF-SSS problems in one schedule (sss_batch_* of libsss300.so).
+
+The reference simulates one problem per SingleScatterSimulationTOF call
+(Python/openSSS/SingleScatterSimulationTOF.py:46-178).  ``BatchSSS`` plans a
+list of problems once -- scatter points, (problem, z-slice) items, waves that
+fit a workspace -- and then runs the whole list as a fixed sequence of
+launches.  Activity maps can be replaced in place between runs; the
+attenuation maps fix the scatter points and therefore the plan.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import WS_BUDGET_BYTES, TofSSS, _ptr, fortran_flat
+
+
+class BatchSSS:
+    """A planned batch of TOF-SSS problems.
+
+    jobs: sequence of ``(engine, ActivityMap, AttenuationMap, ImageSize)`` with
+    ``engine`` a :class:`TofSSS` (scanner, sampling, tables; engines may be
+    shared between jobs).  Maps may be numpy arrays (x, y, z) or CUDA tensors
+    already flattened in Fortran order with ``shape`` given as the fifth
+    element of the job tuple.
+    """
+
+    def __init__(self, jobs, workspace_bytes: int | None = None, stream=None):
+        if not jobs:
+            raise ValueError("empty batch")
+        L = _lib.lib()
+        self.engines: list[TofSSS] = []
+        self.shapes = []
+        self._keep = []
+        probs = (_lib.TofProblem * len(jobs))()
+        dev = jobs[0][0].device
+        self.device = dev
+        for i, job in enumerate(jobs):
+            eng, act, mu, size = job[:4]
+            if eng.device != dev:
+                raise ValueError("all engines of a batch must be on one device")
+            if len(job) > 4:
+                shape = tuple(int(s) for s in job[4])
+                act_f = act if isinstance(act, torch.Tensor) else fortran_flat(act, dev)
+                mu_f = mu if isinstance(mu, torch.Tensor) else fortran_flat(mu, dev)
+            else:
+                shape = tuple(int(s) for s in np.shape(act))
+                act_f, mu_f = fortran_flat(act, dev), fortran_flat(mu, dev)
+            probs[i] = eng.problem(act_f, mu_f, shape, size)
+            self.engines.append(eng)
+            self.shapes.append(shape)
+            self._keep.append((act_f, mu_f))
+        self.outs = [torch.empty((e.nbins, e.nl, e.nl), dtype=torch.float32, device=dev)
+                     for e in self.engines]
+        out_ptrs = (C.c_void_p * len(jobs))(*[o.data_ptr() for o in self.outs])
+        if workspace_bytes is None:
+            workspace_bytes = min(WS_BUDGET_BYTES, int(torch.cuda.mem_get_info(dev)[0] * 0.5))
+        self.workspace = torch.empty(int(workspace_bytes), dtype=torch.uint8, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._probs = probs
+        st = stream if stream is not None else torch.cuda.current_stream(dev)
+        plan = C.c_void_p(0)
+        _lib.check(L.sss_batch_plan(probs, len(jobs), C.cast(out_ptrs, C.c_void_p), _ptr(self.workspace),
+                                    self.workspace.numel(), _ptr(self.status), C.byref(plan),
+                                    C.c_void_p(st.cuda_stream)))
+        self._plan = plan
+        info = np.zeros(4, dtype=np.int64)
+        _lib.check(L.sss_batch_info(plan, info.ctypes.data_as(C.c_void_p)))
+        self.waves, self.launches, self.units, self.points = (int(v) for v in info)
+
+    def activity(self, i: int) -> torch.Tensor:
+        """Problem i's resident activity map (flat, Fortran order); write into
+        it in place to re-run the plan on new activity."""
+        return self._keep[i][0]
+
+    def run(self, stream=None, check: bool = True) -> list[torch.Tensor]:
+        """Enqueue the whole batch; outputs are the leg-pair sinograms
+        [B, NL, NL] of each problem (reused across runs)."""
+        if self._plan is None:
+            raise RuntimeError("batch plan was freed")
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if check:
+            self.status.zero_()
+        _lib.check(_lib.lib().sss_batch_run(self._plan, C.c_void_p(st.cuda_stream)))
+        if check:
+            st.synchronize()
+            _lib.check_status(int(self.status.item()))
+        return self.outs
+
+    def close(self):
+        if getattr(self, "_plan", None):
+            _lib.lib().sss_batch_free(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,421 @@
+// Batched TOF-SSS: many problems of different sizes run as one schedule.
+//
+// A plan enumerates every problem's scatter points (one small kernel per
+// problem, one synchronisation), cuts the work into (problem, z-slice) items
+// and packs consecutive items into waves that fit the workspace.  A wave is
+// one leg launch over all its items and one persistent pair launch per TOF
+// class (bin count and TOF kernel; a launch shares one TOF table in shared
+// memory).  Every item carries its own problem's geometry, sampling, tables
+// and output, so problems of different sizes share a launch.  All device
+// memory a plan uses is carved from the caller's workspace, and sss_batch_run
+// is a fixed sequence of asynchronous launches: the same plan can be run
+// again on new activity maps (the attenuation, and with it the scatter
+// points, stays fixed) and captured in a CUDA graph.
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "legs.cuh"
+#include "pair.cuh"
+#include "trace.cuh"
+
+namespace {
+
+using namespace sss;
+
+struct LegItem {
+    LegParams p;              // points / legA / legB / vox already point at this item's data
+    long long thread_begin;   // prefix over the wave's items of npts * nl
+};
+
+struct PairItem {
+    PairCtx ctx;              // s_first = 0, s_count = the item's points
+    int nchunks;
+    long long task_begin;     // prefix over the launch's items of nl * nchunks
+};
+
+__global__ void __launch_bounds__(128) batch_leg_kernel(const LegItem* __restrict__ items, int nitems,
+                                                        long long total)
+{
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= total) return;
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].thread_begin <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    const LegItem& it = items[lo];
+    const long long local = gid - it.thread_begin;
+    leg_one(it.p, (int)(local / it.p.nl), (int)(local % it.p.nl));
+}
+
+template <int NP, bool SINGLE, bool ODD, int MINB>
+__global__ void __launch_bounds__(kPairWarps * 32, MINB)
+    batch_pair_kernel(const PairItem* __restrict__ items, int nitems, long long ntasks, TofConst T,
+                      const float* tof_log2w, unsigned int* counter, int32_t* status)
+{
+    extern __shared__ float smem[];
+    float* sY = smem;
+    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
+    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
+    load_tof_table(tof_log2w, sY, sN);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    bool tof_bad = false, energy_bad = false;
+    unsigned long long walked = 0, npairs = 0;
+    for (;;) {
+        long long task = 0;
+        if (lane == 0) task = atomicAdd(counter, 1u);
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= ntasks) break;
+        int lo = 0, hi = nitems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].task_begin <= task) lo = mid;
+            else hi = mid - 1;
+        }
+        const PairItem& it = items[lo];
+        const int rem = (int)(task - it.task_begin);
+        walk_task<NP, SINGLE, ODD>(it.ctx, T, rem / it.nchunks, rem % it.nchunks, lane, sY, sN, vbuf,
+                                   tof_bad, energy_bad, walked, npairs);
+    }
+    finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
+}
+
+template <int NP, bool SINGLE, bool ODD>
+int launch_batch_pairs(const PairItem* items, int nitems, long long ntasks, const TofConst& T,
+                       const float* tof, unsigned int* counter, int32_t* status, cudaStream_t st)
+{
+    constexpr int MINB = NP <= 8 ? 3 : 2;
+    auto kern = batch_pair_kernel<NP, SINGLE, ODD, MINB>;
+    const size_t smem = pair_smem_bytes();
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPairWarps * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    long long blocks = std::min<long long>((long long)sms * per_sm, (ntasks + kPairWarps - 1) / kPairWarps);
+    if (blocks < 1) blocks = 1;
+    kern<<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(items, nitems, ntasks, T, tof, counter, status);
+    return sss_check_launch("batch_pair_kernel");
+}
+
+int dispatch_batch_pairs(int nbins, const PairItem* items, int nitems, long long ntasks,
+                         const TofConst& T, const float* tof, unsigned int* counter, int32_t* status,
+                         cudaStream_t st)
+{
+    if (nbins == 1) return launch_batch_pairs<1, true, false>(items, nitems, ntasks, T, tof, counter, status, st);
+    const bool odd = nbins & 1;
+    switch ((nbins + 1) / 2) {
+#define SSS_BNP(k)                                                                                   \
+    case k:                                                                                          \
+        return odd ? launch_batch_pairs<k, false, true>(items, nitems, ntasks, T, tof, counter, status, st) \
+                   : launch_batch_pairs<k, false, false>(items, nitems, ntasks, T, tof, counter, status, st);
+        SSS_BNP(1) SSS_BNP(2) SSS_BNP(3) SSS_BNP(4) SSS_BNP(5) SSS_BNP(6) SSS_BNP(7) SSS_BNP(8)
+        SSS_BNP(9) SSS_BNP(10) SSS_BNP(11) SSS_BNP(12) SSS_BNP(13) SSS_BNP(14) SSS_BNP(15) SSS_BNP(16)
+        SSS_BNP(17) SSS_BNP(18) SSS_BNP(19) SSS_BNP(20) SSS_BNP(21) SSS_BNP(22) SSS_BNP(23) SSS_BNP(24)
+        SSS_BNP(25) SSS_BNP(26) SSS_BNP(27) SSS_BNP(28) SSS_BNP(29) SSS_BNP(30) SSS_BNP(31) SSS_BNP(32)
+#undef SSS_BNP
+    }
+    return sss_set_error(SSS_ERR_INVALID, "nbins out of range");
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct LatticeSize {
+    long long lz, capacity;
+};
+
+LatticeSize lattice_size(const sss_tof_problem& p)
+{
+    const long long lx = (p.nx + p.sample_step[0] - 1) / p.sample_step[0];
+    const long long ly = (p.ny + p.sample_step[1] - 1) / p.sample_step[1];
+    const long long lz = (p.nz + p.sample_step[2] - 1) / p.sample_step[2];
+    return {lz, lx * ly * lz};
+}
+
+// leg-record bytes of `npts` scatter points of problem p
+size_t item_bytes(const sss_tof_problem& p, long long npts)
+{
+    const long long nl = (long long)p.nru * p.ndu;
+    const long long cap = (long long)p.nx + p.ny + p.nz;
+    return 2 * align256(sizeof(float4) * npts * nl) + align256(sizeof(float2) * npts * nl * cap);
+}
+
+}  // namespace
+
+struct sss_batch {
+    struct Launch {
+        int nbins;
+        TofConst T;
+        const float* tof;
+        const PairItem* items;  // device
+        int nitems;
+        long long ntasks;
+        unsigned int* counter;  // device
+    };
+    struct Wave {
+        const LegItem* legs;    // device
+        int nlegs;
+        long long threads;
+        std::vector<Launch> launches;
+    };
+    std::vector<sss_tof_problem> problems;
+    std::vector<float*> outs;
+    std::vector<long long> npoints;
+    std::vector<Wave> waves;
+    unsigned int* counters = nullptr;
+    int ncounters = 0;
+    int32_t* status = nullptr;
+    long long units = 0;
+};
+
+extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float* const* outs,
+                              void* workspace, size_t workspace_bytes, int32_t* status,
+                              sss_batch** plan, void* stream)
+{
+    if (!problems || n < 1 || !outs || !workspace || !plan)
+        return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan: bad argument");
+    *plan = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int i = 0; i < n; ++i) {
+        int rc = sss_internal_validate(&problems[i]);
+        if (rc) return rc;
+        if (!outs[i]) return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan: null output %d", i);
+    }
+    char* ws = (char*)workspace;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    // 1. scatter points of every problem
+    std::vector<size_t> pts_off(n), cnt_off(n);
+    std::vector<LatticeSize> lat(n);
+    for (int i = 0; i < n; ++i) {
+        lat[i] = lattice_size(problems[i]);
+        pts_off[i] = take(sizeof(double) * 4 * (size_t)std::max<long long>(lat[i].capacity, 1));
+        cnt_off[i] = take(sizeof(unsigned long long) * (size_t)(1 + lat[i].lz));
+    }
+    if (off > workspace_bytes)
+        return sss_set_error(SSS_ERR_WORKSPACE, "sss_batch_plan: workspace too small for the point lists");
+    for (int i = 0; i < n; ++i) {
+        unsigned long long* cnt = (unsigned long long*)(ws + cnt_off[i]);
+        if (cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (size_t)(1 + lat[i].lz), st) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: memset failed");
+        int rc = sss_internal_scatter_points(&problems[i], (double*)(ws + pts_off[i]), lat[i].capacity,
+                                             cnt, st);
+        if (rc) return rc;
+    }
+    std::vector<std::vector<unsigned long long>> counts(n);
+    for (int i = 0; i < n; ++i) {
+        counts[i].resize((size_t)(1 + lat[i].lz));
+        if (cudaMemcpyAsync(counts[i].data(), ws + cnt_off[i], counts[i].size() * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: count copy failed");
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: %s", cudaGetErrorString(cudaGetLastError()));
+
+    // 2. items = (problem, z-slice) with points
+    struct Item {
+        int prob;
+        long long first, count;
+    };
+    std::vector<Item> items;
+    std::unique_ptr<sss_batch> B(new sss_batch());
+    B->problems.assign(problems, problems + n);
+    B->outs.assign(outs, outs + n);
+    B->status = status;
+    for (int i = 0; i < n; ++i) {
+        long long first = 0;
+        for (long long z = 0; z < lat[i].lz; ++z) {
+            const long long c = (long long)counts[i][1 + z];
+            if (c > 0) items.push_back({i, first, c});
+            first += c;
+        }
+        B->npoints.push_back(first);
+        const long long nru = problems[i].nru, ndu = problems[i].ndu;
+        const long long pairs = nru * nru * ndu * (ndu - 1) / 2 + ndu * nru * (nru - 1);
+        B->units += first * pairs * problems[i].nbins;
+    }
+    // descriptors: one LegItem and one PairItem per item, counters per launch
+    const size_t desc_off = take(sizeof(LegItem) * std::max<size_t>(items.size(), 1));
+    const size_t pdesc_off = take(sizeof(PairItem) * std::max<size_t>(items.size(), 1));
+    const int max_launches = (int)items.size() + 1;
+    const size_t ctr_off = take(sizeof(unsigned int) * (size_t)max_launches);
+    const size_t data_off = off;
+    if (data_off >= workspace_bytes)
+        return sss_set_error(SSS_ERR_WORKSPACE, "sss_batch_plan: no workspace left for leg records");
+    const size_t data_bytes = workspace_bytes - data_off;
+
+    // 3. waves of consecutive items that fit
+    std::vector<LegItem> hleg(items.size());
+    std::vector<PairItem> hpair(items.size());
+    LegItem* dleg = (LegItem*)(ws + desc_off);
+    PairItem* dpair = (PairItem*)(ws + pdesc_off);
+    unsigned int* dctr = (unsigned int*)(ws + ctr_off);
+    int nctr = 0;
+    size_t k = 0;
+    while (k < items.size()) {
+        size_t used = 0, k_end = k;
+        while (k_end < items.size()) {
+            const size_t b = item_bytes(problems[items[k_end].prob], items[k_end].count);
+            if (used + b > data_bytes) break;
+            used += b;
+            ++k_end;
+        }
+        if (k_end == k)
+            return sss_set_error(SSS_ERR_WORKSPACE,
+                                 "sss_batch_plan: a z-slice of problem %d needs %zu bytes of leg records, "
+                                 "only %zu available", items[k].prob,
+                                 item_bytes(problems[items[k].prob], items[k].count), data_bytes);
+        sss_batch::Wave W;
+        W.legs = dleg + k;
+        W.nlegs = (int)(k_end - k);
+        W.threads = 0;
+        size_t doff = data_off;
+        // group the wave's items by TOF class for the pair launches
+        std::map<std::tuple<int, double, double>, std::vector<size_t>> classes;
+        for (size_t j = k; j < k_end; ++j) {
+            const Item& it = items[j];
+            const sss_tof_problem& p = problems[it.prob];
+            const long long nl = (long long)p.nru * p.ndu, cap = (long long)p.nx + p.ny + p.nz;
+            LegItem& L = hleg[j];
+            L.p.g.nx = p.nx;
+            L.p.g.ny = p.ny;
+            L.p.g.nz = p.nz;
+            for (int q = 0; q < 6; ++q) L.p.g.b[q] = p.image_size[q];
+            L.p.act = p.activity;
+            L.p.mu = p.attenuation;
+            L.p.geom = p.geometry;
+            L.p.normals = p.normals;
+            L.p.rings = p.rings;
+            L.p.dets = p.detectors;
+            L.p.nd = p.nd;
+            L.p.nru = p.nru;
+            L.p.ndu = p.ndu;
+            L.p.nl = (int)nl;
+            L.p.cap = (int)cap;
+            L.p.nvox = (long long)p.nx * p.ny * p.nz;
+            L.p.points = (const double*)(ws + pts_off[it.prob]) + 4 * it.first;
+            L.p.npts = (int)it.count;
+            L.p.legA = (float4*)(ws + doff);
+            doff += align256(sizeof(float4) * it.count * nl);
+            L.p.legB = (float4*)(ws + doff);
+            doff += align256(sizeof(float4) * it.count * nl);
+            L.p.vox = (float2*)(ws + doff);
+            doff += align256(sizeof(float2) * it.count * nl * cap);
+            L.p.status = status;
+            L.thread_begin = W.threads;
+            W.threads += it.count * nl;
+            classes[std::make_tuple(p.nbins, p.tof_bin_width, p.tof_resolution)].push_back(j);
+        }
+        // pair items, contiguous per class
+        size_t pk = k;
+        for (auto& kv : classes) {
+            sss_batch::Launch Lc;
+            const sss_tof_problem& p0 = problems[items[kv.second[0]].prob];
+            Lc.nbins = p0.nbins;
+            Lc.T = tof_const(p0);
+            Lc.tof = p0.tof_log2w;
+            Lc.items = dpair + pk;
+            Lc.nitems = (int)kv.second.size();
+            Lc.ntasks = 0;
+            Lc.counter = dctr + nctr++;
+            for (size_t j : kv.second) {
+                const Item& it = items[j];
+                const sss_tof_problem& p = problems[it.prob];
+                PairItem& P = hpair[pk++];
+                PairCtx& C = P.ctx;
+                C.nru = p.nru;
+                C.ndu = p.ndu;
+                C.nl = p.nru * p.ndu;
+                C.nd = p.nd;
+                C.cap = p.nx + p.ny + p.nz;
+                C.nbins = p.nbins;
+                C.geo_c = geo_const(p);
+                C.gamma_kn = gamma_kn_const();
+                C.eff = p.efficiency;
+                C.ratio = p.atten_ratio;
+                C.geom = p.geometry;
+                C.rings = p.rings;
+                C.dets = p.detectors;
+                C.points = hleg[j].p.points;
+                C.legA = hleg[j].p.legA;
+                C.legB = hleg[j].p.legB;
+                C.vox = hleg[j].p.vox;
+                C.s_first = 0;
+                C.s_count = (int)it.count;
+                C.out = outs[it.prob];
+                P.nchunks = pair_chunks(p.nru, p.ndu);
+                P.task_begin = Lc.ntasks;
+                Lc.ntasks += (long long)C.nl * P.nchunks;
+            }
+            W.launches.push_back(Lc);
+        }
+        B->waves.push_back(W);
+        k = k_end;
+    }
+    if (!items.empty()) {
+        if (cudaMemcpyAsync(dleg, hleg.data(), sizeof(LegItem) * hleg.size(), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(dpair, hpair.data(), sizeof(PairItem) * hpair.size(), cudaMemcpyHostToDevice,
+                            st) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: descriptor upload failed");
+        if (cudaStreamSynchronize(st) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    B->counters = dctr;
+    B->ncounters = nctr;
+    *plan = B.release();
+    return SSS_OK;
+}
+
+extern "C" int sss_batch_run(const sss_batch* B, void* stream)
+{
+    if (!B) return sss_set_error(SSS_ERR_INVALID, "sss_batch_run: null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (size_t i = 0; i < B->problems.size(); ++i) {
+        const sss_tof_problem& p = B->problems[i];
+        const size_t nl = (size_t)p.nru * p.ndu;
+        if (cudaMemsetAsync(B->outs[i], 0, sizeof(float) * p.nbins * nl * nl, st) != cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
+    }
+    if (B->ncounters > 0 &&
+        cudaMemsetAsync(B->counters, 0, sizeof(unsigned int) * B->ncounters, st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
+    for (const auto& W : B->waves) {
+        batch_leg_kernel<<<(unsigned)((W.threads + 127) / 128), 128, 0, st>>>(W.legs, W.nlegs, W.threads);
+        int rc = sss_check_launch("batch_leg_kernel");
+        if (rc) return rc;
+        for (const auto& L : W.launches) {
+            rc = dispatch_batch_pairs(L.nbins, L.items, L.nitems, L.ntasks, L.T, L.tof, L.counter, B->status,
+                                      st);
+            if (rc) return rc;
+        }
+    }
+    return SSS_OK;
+}
+
+extern "C" int sss_batch_info(const sss_batch* B, int64_t* info)
+{
+    if (!B || !info) return sss_set_error(SSS_ERR_INVALID, "sss_batch_info: bad argument");
+    int64_t launches = 0;
+    for (const auto& W : B->waves) launches += 1 + (int64_t)W.launches.size();
+    info[0] = (int64_t)B->waves.size();
+    info[1] = launches;
+    info[2] = B->units;
+    int64_t pts = 0;
+    for (long long v : B->npoints) pts += v;
+    info[3] = pts;
+    return SSS_OK;
+}
+
+extern "C" void sss_batch_free(sss_batch* B) { delete B; }

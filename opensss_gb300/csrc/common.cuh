@@ -36,6 +36,11 @@ __device__ __forceinline__ float ex2(float x)
 
 }  // namespace sss
 
-// Host helpers shared by the entry points (defined in api.cu).
+// Host helpers shared by the entry points (defined in api.cu and sss.cu).
 int sss_set_error(int code, const char* fmt, ...);
 int sss_check_launch(const char* what);
+int sss_internal_validate(const sss_tof_problem* p);
+// Enumerates p's scatter points into points (capacity entries of 4 doubles);
+// counts[0] = total, counts[1 + i] = points of sampled slice i (zeroed by the caller).
+int sss_internal_scatter_points(const sss_tof_problem* p, double* points, long long capacity,
+                                unsigned long long* counts, cudaStream_t st);

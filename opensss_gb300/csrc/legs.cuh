@@ -1,0 +1,88 @@
+// The TOF-SSS leg stage: one scatter point to one sampled crystal.  Shared
+// by the single-problem kernel (sss.cu) and the batched kernels (batch.cu).
+// Reference: bodySSS legs, Python/openSSS/SingleScatterSimulationTOF.py:400-430.
+#pragma once
+
+#include "common.cuh"
+#include "pair.cuh"
+#include "trace.cuh"
+
+namespace sss {
+
+struct LegParams {
+    Grid g;
+    const float* act;
+    const float* mu;
+    const double* geom;
+    const double* normals;
+    const int32_t* rings;
+    const int32_t* dets;
+    int nd, nru, ndu, nl, cap;
+    long long nvox;
+    const double* points;  // wave's first point, [n][4]
+    int npts;
+    float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
+    float4* legB;   // [npts][nl]: unit vector to the crystal, voxel-list length (int bits)
+    float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major
+    int32_t* status;
+};
+
+// One leg: scatter point s to sampled crystal leg l.
+__device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
+{
+    const int di = l / P.nru, ri = l % P.nru;  // legs are crystal-major
+    const int ring = P.rings[ri], det = P.dets[di];
+    const double* dp = P.geom + 3 * ((long long)ring * P.nd + det);
+    const double zD = P.geom[3 * ((long long)ring * P.nd) + 2];  // :402 (crystal 0's z)
+    const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
+    double lc[6] = {xS, yS, zS, dp[0], dp[1], zD};
+
+    // incidence angle term |cos a| (:424-430, :533-535) and distance (:442-444)
+    const double vx = dp[0] - xS, vy = dp[1] - yS, vz = zD - zS;
+    const double* nv = P.normals + 3 * ((long long)ring * P.nd + det);
+    const double vn = sqrt(vx * vx + vy * vy + vz * vz);
+    const double nn = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+    const double cosa = fabs((vx * nv[0] + vy * nv[1] + vz * nv[2]) / (nn * vn));
+    const float sv = (float)vn;
+
+    float asum = 0.f, musum = 0.f;
+    int nlist = 0;
+    Ray r;
+    if (ray_setup(P.g, lc, 1e-20, r)) {
+        const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
+        const float inv_c = (float)(1.0 / kLightCmPerPs);
+        const double t0 = r.tmin;
+        float2* out = P.vox + ((long long)s * P.nl + l) * P.cap;
+        int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
+            long long v = lin - 1;
+            if (v < 0 || v >= P.nvox) {
+                raise_error(P.status, kErrVoxel);
+                return;
+            }
+            // |vec| * |dt|; for near-zero steps the reference's own FP64 length
+            // expression decides whether a corner-grazing segment is zero or
+            // not (that decides whether a leg carries activity, :483-488)
+            const double dt = tb - ta;
+            float len = fabs(dt) < 1e-9 ? (float)ref_length(r, ta, tb) : vlen * (float)fabs(dt);
+            float a = __ldg(P.act + v) * len;
+            musum = fmaf(__ldg(P.mu + v), len, musum);
+            asum += a;
+            if (a != 0.f) {
+                // sample = half the distance walked to the voxel's exit (:155-156)
+                float rho = vlen * (float)(tb - t0) * inv_c;
+                out[nlist] = make_float2(a, rho);
+                ++nlist;
+            }
+        });
+        if (c < 0) raise_error(P.status, kErrOverrun);
+    }
+    const long long o = (long long)s * P.nl + l;
+    // exp(-I) underflows to 0 in FP64 above ~745.13 (the skip at :451 / :483)
+    const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
+    P.legA[o] = make_float4(sv, asum, ilog2, (float)(cosa / (vn * vn)));
+    const float inv = (float)(1.0 / vn);
+    P.legB[o] = make_float4((float)vx * inv, (float)vy * inv, (float)vz * inv,
+                            __int_as_float(nlist));
+}
+
+}  // namespace sss

@@ -1,0 +1,296 @@
+// The TOF-SSS pair stage: one warp task = (z-slice of one problem, walking
+// leg lw, 32 partner legs).  Shared by the single-problem kernel (sss.cu)
+// and the batched kernels (batch.cu).  Reference: bodySSS,
+// Python/openSSS/SingleScatterSimulationTOF.py:433-557.
+#pragma once
+
+#include "common.cuh"
+#include "trace.cuh"
+
+namespace sss {
+
+constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
+constexpr int kPairWarps = 8;                           // warps per pair-kernel block
+// pair-kernel shared memory: log2 largest weight per TOF offset (floats),
+// its bin (bytes), then 32 float2 voxels per warp on a 16-byte boundary
+constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
+constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
+static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
+
+inline size_t pair_smem_bytes()
+{
+    return sizeof(float) * kSmemVbufFloats + sizeof(float2) * 32 * kPairWarps;
+}
+
+// TOF constants of one launch (every task of a launch shares one TOF table)
+struct TofConst {
+    float s0, w;           // first bin centre offset and bin width (ps)
+    float kappa2w, gamma;  // 2 kappa w and kappa w^2, kappa = 4/FWHM^2 (log2 units)
+};
+
+// Everything one task needs about its problem and z-slice.
+struct PairCtx {
+    int nru, ndu, nl, nd, cap, nbins;
+    float geo_c;             // (ds0*ds1*1e-2)^2 / (4 pi)
+    float gamma_kn;          // E/(m_e c^2) of the reference's KleinNishina
+    const float* eff;        // [2000]
+    const float* ratio;      // [2000]
+    const double* geom;      // [nr][nd][3]
+    const int32_t* rings;
+    const int32_t* dets;
+    const double* points;    // scatter points the leg arrays are indexed by
+    const float4* legA;      // [point][nl]
+    const float4* legB;
+    const float2* vox;       // [point][nl][cap]
+    int s_first, s_count;    // the slice's points
+    float* out;              // [nbins][nl][nl]
+};
+
+// Launch constants of a problem's TOF table (:98, :282) and Watson factors.
+inline TofConst tof_const(const sss_tof_problem& p)
+{
+    const double w = p.tof_bin_width;
+    const double kappa = 4.0 / (p.tof_resolution * p.tof_resolution);
+    TofConst T;
+    T.s0 = (float)((1.0 - (p.nbins + 1) / 2.0) * w);
+    T.w = (float)w;
+    T.kappa2w = (float)(2.0 * kappa * w);
+    T.gamma = (float)(kappa * w * w);
+    return T;
+}
+inline float geo_const(const sss_tof_problem& p)
+{
+    const double ds = p.detector_size[0] * p.detector_size[1] * 1e-2;
+    return (float)(ds * ds / (4.0 * 3.141592653589793));
+}
+inline float gamma_kn_const()
+{
+    return (float)(511.0E3 * 1.6E-19 / (9.10938356E-31 * (299792458.0 * 299792458.0)));
+}
+
+// 32-partner chunks per walking leg: nl legs plus nru same-crystal entries
+__host__ __device__ inline int pair_chunks(int nru, int ndu) { return (nru * ndu + nru + 31) / 32; }
+
+// Block-wide load of the (log2 largest weight, bin) table into shared memory.
+__device__ __forceinline__ void load_tof_table(const float* g, float* sY, unsigned char* sN)
+{
+    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
+        sY[i] = g[2 * i];
+        sN[i] = (unsigned char)g[2 * i + 1];
+    }
+}
+
+// Energy row of a pair exactly as the reference computes it in FP64
+// (:442-444, :474-475, :495-501), used when the FP32 estimate lies within
+// 1e-3 keV of a rounding boundary.
+static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int ri1, int di1, int ri2,
+                                            int di2)
+{
+    const double xS = C.points[4 * s], yS = C.points[4 * s + 1], zS = C.points[4 * s + 2];
+    const int r1 = C.rings[ri1], r2 = C.rings[ri2], d1 = C.dets[di1], d2 = C.dets[di2];
+    const double* p1 = C.geom + 3 * ((long long)r1 * C.nd + d1);
+    const double* p2 = C.geom + 3 * ((long long)r2 * C.nd + d2);
+    const double z1 = C.geom[3 * ((long long)r1 * C.nd) + 2];
+    const double z2 = C.geom[3 * ((long long)r2 * C.nd) + 2];
+    double sv1 = __dsqrt_rn(add64(add64(mul64(sub64(p1[0], xS), sub64(p1[0], xS)),
+                                        mul64(sub64(p1[1], yS), sub64(p1[1], yS))),
+                                  mul64(sub64(z1, zS), sub64(z1, zS))));
+    double sv2 = __dsqrt_rn(add64(add64(mul64(sub64(p2[0], xS), sub64(p2[0], xS)),
+                                        mul64(sub64(p2[1], yS), sub64(p2[1], yS))),
+                                  mul64(sub64(z2, zS), sub64(z2, zS))));
+    double lor = add64(add64(mul64(sub64(p1[0], p2[0]), sub64(p1[0], p2[0])),
+                             mul64(sub64(p1[1], p2[1]), sub64(p1[1], p2[1]))),
+                       mul64(sub64(z1, z2), sub64(z1, z2)));
+    double a = mul64(sv1, sv1), b = mul64(sv2, sv2);
+    double q = div64(sub64(add64(a, b), lor), mul64(2.0, __dsqrt_rn(mul64(a, b))));
+    double th = sub64(180.0, mul64(acos(q), 180.0 / 3.141592653589793));
+    double cth = cos(mul64(th, 3.141592653589793 / 180.0));
+    double es = floor(add64(div64(511.0, add64(1.0, mul64(1.0, sub64(1.0, cth)))), 0.5));
+    return (int)mul64(es, 2.0) - 1;
+}
+
+// Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
+// reference's 8001-entry TOF table, :520-528).  w_b is rebuilt from the
+// largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
+// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Bins go two
+// at a time through packed FP32x2 instructions; NP = number of bin pairs.
+template <int NP, bool SINGLE, bool ODD>
+__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
+                                                 const float* sY, const unsigned char* sN,
+                                                 const TofConst& T, bool& tof_bad)
+{
+    // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
+    const float y = __fadd_rd(x, 12582912.0f);
+    int t = __float_as_int(y) - 0x4B400000;
+    float off = y - 12586912.0f;  // t - 4000, exact
+    if ((unsigned)t >= (unsigned)kTofEntries) {
+        if (t < 0 && t + kTofEntries >= 0) {  // numpy negative index wraps (:521, :527)
+            t += kTofEntries;
+            off = (float)(t - kTimeRange);
+        } else {
+            tof_bad = true;
+            return;
+        }
+    }
+    const float Y = sY[t];
+    const float n = (float)sN[t];
+    // beta = 2 kappa w (off - s_n), s_n = s0 + n w
+    const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));
+    if constexpr (SINGLE) {
+        acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(T.gamma, n, beta), Y)), acc[0].x);
+    } else {
+        const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
+        const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-T.gamma, -T.gamma);
+        const float2 two = make_float2(2.f, 2.f);
+        float2 nd = make_float2(-n, 1.f - n);  // b - n for the pair (b, b+1)
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
+            const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
+            // with an odd bin count the last pair's second bin does not exist
+            const float wy = (ODD && k + 1 == NP) ? 0.f : ex2(e2.y);
+            acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), wy), acc[k]);
+            if (k + 1 < NP) nd = __fadd2_rn(nd, two);
+        }
+    }
+}
+
+// One task.  Every lane pairs lw with its own partner leg lp; the pair
+// (l1, l2) is ordered as the reference orders it (crystal of l1 < crystal of
+// l2, :469).  The task adds the part of the pair's TOF sum that runs over
+// lw's voxels (AB1 if lw is l1, AB2 if lw is l2, :519-530); the other part
+// comes from the task that walks lp.  Both tasks see the same scatter points,
+// so both divide by the same per-slice count (:555-557).  All lanes walk the
+// same voxel list: 32 voxels at a time are staged in the warp's shared
+// buffer and read back as broadcasts, so the trip count is uniform.
+template <int NP, bool SINGLE, bool ODD>
+__device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int lw, int chunk,
+                                          int lane, const float* sY, const unsigned char* sN,
+                                          float2* vbuf, bool& tof_bad, bool& energy_bad,
+                                          unsigned long long& walked, unsigned long long& npairs)
+{
+    const float inv_c = (float)(1.0 / kLightCmPerPs);
+    const int dw = lw / C.nru, rw = lw % C.nru;  // legs are crystal-major
+
+    // partner of this lane: legs 0..nl-1 (lw leads the pair unless its
+    // crystal is the larger), then one more entry per other ring for the
+    // same crystal in the opposite role (both orders are distinct pairs)
+    const int q = chunk * 32 + lane;
+    int lp = lw, rp = rw, dp = dw;
+    bool w_first = true, lane_ok = false;
+    if (q < C.nl) {
+        lp = q;
+        dp = q / C.nru;
+        rp = q % C.nru;
+        lane_ok = lp != lw;
+        w_first = dp >= dw;
+    } else if (q < C.nl + C.nru) {
+        rp = q - C.nl;
+        dp = dw;
+        lp = dw * C.nru + rp;
+        lane_ok = rp != rw;
+        w_first = false;
+    }
+    const int ri1 = w_first ? rw : rp, di1 = w_first ? dw : dp;
+    const int ri2 = w_first ? rp : rw, di2 = w_first ? dp : dw;
+    const int l1 = w_first ? lw : lp, l2 = w_first ? lp : lw;
+    const float sigma = w_first ? -1.f : 1.f;
+
+    float2 acc[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);
+    float cnt = 0.f;
+
+    for (int s = C.s_first; s < C.s_first + C.s_count; ++s) {
+        const long long lo = (long long)s * C.nl;
+        const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw];
+        const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp];
+        const float4 A1 = w_first ? Aw : Ap, A2 = w_first ? Ap : Aw;
+        const float4 B1 = w_first ? Bw : Bp, B2 = w_first ? Bp : Bw;
+        bool ok = lane_ok && A1.z != INFINITY && A2.z != INFINITY && !(A1.y == 0.f && A2.y == 0.f);
+        float c = 0.f;
+        if (ok) {
+            // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
+            float qc = fmaf(B1.x, B2.x, fmaf(B1.y, B2.y, B1.z * B2.z));
+            qc = fminf(1.f, fmaxf(-1.f, qc));
+            const float e = 511.0f / (2.0f + qc);
+            const float eh = e + 0.5f;
+            const float fr = eh - floorf(eh);
+            int row;
+            if (fr < 1e-3f || fr > 1.0f - 1e-3f)
+                row = energy_row_fp64(C, s, ri1, di1, ri2, di2);
+            else
+                row = 2 * (int)floorf(eh) - 1;
+            if (row < 0 || row >= 2000) {
+                energy_bad = true;
+            } else {
+                const float effp = __ldg(C.eff + row);
+                if (effp != 0.f) {  // :508-509 skips before the count is added
+                    const float rr = __ldg(C.ratio + row);
+                    // Klein-Nishina with cos(theta) = -qc (:239-258)
+                    const float ratio = 1.0f / (1.0f + C.gamma_kn * (1.0f + qc));
+                    const float sin2 = 1.0f - qc * qc;
+                    const float kn = ratio * ratio * (ratio + 1.0f / ratio - sin2);
+                    // geometry (:533-536): (ds)^2 |cos a1||cos a2| / (4 pi sv1^2 sv2^2)
+                    const float f = C.geo_c * A1.w * A2.w * effp * kn;
+                    // this task's part: M1 * M2^r * AB1 or M2 * M1^r * AB2 (:540)
+                    const float mw = ex2(-Aw.z), mpr = ex2(-rr * Ap.z);
+                    if (Aw.y != 0.f) c = f * mw * mpr;
+                    cnt += (A1.y != 0.f && A2.y != 0.f) ? 2.f : 1.f;  // :485-488
+                    npairs += 1;
+                }
+            }
+        }
+        // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
+        const float u = fmaf(A1.x - A2.x, inv_c, 4000.5f);
+        if (__any_sync(0xffffffffu, c != 0.f)) {
+            const int nw = __float_as_int(Bw.w);
+            if (c != 0.f) walked += nw;
+            const float2* vw = C.vox + (lo + lw) * C.cap;
+            for (int k0 = 0; k0 < nw; k0 += 32) {
+                __syncwarp();
+                if (k0 + lane < nw) vbuf[lane] = vw[k0 + lane];
+                __syncwarp();
+                const int jn = min(32, nw - k0);
+                if (c != 0.f) {
+#pragma unroll 2
+                    for (int j = 0; j < jn; ++j) {
+                        const float2 v = vbuf[j];
+                        accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sY, sN,
+                                                          T, tof_bad);
+                    }
+                }
+            }
+        }
+    }
+    if (lane_ok && cnt > 0.f) {
+        float* o = C.out + (long long)l1 * C.nl + l2;
+        const long long plane = (long long)C.nl * C.nl;
+        const float inv = 1.0f / cnt;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            if (2 * k < C.nbins) atomicAdd(o + (2 * k) * plane, acc[k].x * inv);
+            if (2 * k + 1 < C.nbins) atomicAdd(o + (2 * k + 1) * plane, acc[k].y * inv);
+        }
+    }
+}
+
+// Block-end bookkeeping: error bits and the walked / evaluated counters.
+__device__ __forceinline__ void finish_pairs(int lane, bool tof_bad, bool energy_bad,
+                                             unsigned long long walked, unsigned long long npairs,
+                                             int32_t* status, unsigned long long* work)
+{
+    if (tof_bad) raise_error(status, kErrTofRange);
+    if (energy_bad) raise_error(status, kErrEnergy);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        walked += __shfl_xor_sync(0xffffffffu, walked, o);
+        npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
+    }
+    if (lane == 0 && work) {
+        atomicAdd(work, walked);
+        atomicAdd(work + 1, npairs);
+    }
+}
+
+}  // namespace sss

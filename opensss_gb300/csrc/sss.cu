@@ -21,20 +21,15 @@
 #include <vector>
 
 #include "common.cuh"
+#include "legs.cuh"
+#include "pair.cuh"
 #include "trace.cuh"
 
 namespace {
 
 using namespace sss;
 
-constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
 constexpr int kMaxWaveSlices = 256;
-constexpr int kPairWarps = 8;  // warps per pair-kernel block
-// pair-kernel shared memory: log2 largest weight per TOF offset (floats),
-// its bin (bytes), then 32 float2 voxels per warp on a 16-byte boundary
-constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
-constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
-static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
 struct LatticeDims {
     int lx, ly, lz;     // lattice points per axis
@@ -118,82 +113,11 @@ __global__ void __launch_bounds__(1024) scatter_points_kernel(
 
 // ---------------------------------------------------------------- 2. legs
 
-struct LegParams {
-    Grid g;
-    const float* act;
-    const float* mu;
-    const double* geom;
-    const double* normals;
-    const int32_t* rings;
-    const int32_t* dets;
-    int nd, nru, ndu, nl, cap;
-    long long nvox;
-    const double* points;  // wave's first point, [n][4]
-    int npts;
-    float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
-    float4* legB;   // [npts][nl]: unit vector to the crystal, voxel-list length (int bits)
-    float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major
-    int32_t* status;
-};
-
 __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
 {
     long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)P.npts * P.nl) return;
-    const int s = (int)(gid / P.nl), l = (int)(gid % P.nl);
-    const int di = l / P.nru, ri = l % P.nru;  // legs are crystal-major
-    const int ring = P.rings[ri], det = P.dets[di];
-    const double* dp = P.geom + 3 * ((long long)ring * P.nd + det);
-    const double zD = P.geom[3 * ((long long)ring * P.nd) + 2];  // :402 (crystal 0's z)
-    const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
-    double lc[6] = {xS, yS, zS, dp[0], dp[1], zD};
-
-    // incidence angle term |cos a| (:424-430, :533-535) and distance (:442-444)
-    const double vx = dp[0] - xS, vy = dp[1] - yS, vz = zD - zS;
-    const double* nv = P.normals + 3 * ((long long)ring * P.nd + det);
-    const double vn = sqrt(vx * vx + vy * vy + vz * vz);
-    const double nn = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-    const double cosa = fabs((vx * nv[0] + vy * nv[1] + vz * nv[2]) / (nn * vn));
-    const float sv = (float)vn;
-
-    float asum = 0.f, musum = 0.f;
-    int nlist = 0;
-    Ray r;
-    if (ray_setup(P.g, lc, 1e-20, r)) {
-        const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
-        const float inv_c = (float)(1.0 / kLightCmPerPs);
-        const double t0 = r.tmin;
-        float2* out = P.vox + ((long long)s * P.nl + l) * P.cap;
-        int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
-            long long v = lin - 1;
-            if (v < 0 || v >= P.nvox) {
-                raise_error(P.status, kErrVoxel);
-                return;
-            }
-            // |vec| * |dt|; for near-zero steps the reference's own FP64 length
-            // expression decides whether a corner-grazing segment is zero or
-            // not (that decides whether a leg carries activity, :483-488)
-            const double dt = tb - ta;
-            float len = fabs(dt) < 1e-9 ? (float)ref_length(r, ta, tb) : vlen * (float)fabs(dt);
-            float a = __ldg(P.act + v) * len;
-            musum = fmaf(__ldg(P.mu + v), len, musum);
-            asum += a;
-            if (a != 0.f) {
-                // sample = half the distance walked to the voxel's exit (:155-156)
-                float rho = vlen * (float)(tb - t0) * inv_c;
-                out[nlist] = make_float2(a, rho);
-                ++nlist;
-            }
-        });
-        if (c < 0) raise_error(P.status, kErrOverrun);
-    }
-    const long long o = (long long)s * P.nl + l;
-    // exp(-I) underflows to 0 in FP64 above ~745.13 (the skip at :451 / :483)
-    const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
-    P.legA[o] = make_float4(sv, asum, ilog2, (float)(cosa / (vn * vn)));
-    const float inv = (float)(1.0 / vn);
-    P.legB[o] = make_float4((float)vx * inv, (float)vy * inv, (float)vz * inv,
-                            __int_as_float(nlist));
+    leg_one(P, (int)(gid / P.nl), (int)(gid % P.nl));
 }
 
 // ---------------------------------------------------------------- 3. pairs
@@ -225,90 +149,6 @@ struct PairParams {
     int32_t* status;
 };
 
-// Energy row of a pair exactly as the reference computes it in FP64
-// (:442-444, :474-475, :495-501), used when the FP32 estimate lies within
-// 1e-3 keV of a rounding boundary.
-__device__ __noinline__ int energy_row_fp64(const PairParams& P, int s, int ri1, int di1, int ri2,
-                                            int di2)
-{
-    const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
-    const int r1 = P.rings[ri1], r2 = P.rings[ri2], d1 = P.dets[di1], d2 = P.dets[di2];
-    const double* p1 = P.geom + 3 * ((long long)r1 * P.nd + d1);
-    const double* p2 = P.geom + 3 * ((long long)r2 * P.nd + d2);
-    const double z1 = P.geom[3 * ((long long)r1 * P.nd) + 2];
-    const double z2 = P.geom[3 * ((long long)r2 * P.nd) + 2];
-    double sv1 = __dsqrt_rn(add64(add64(mul64(sub64(p1[0], xS), sub64(p1[0], xS)),
-                                      mul64(sub64(p1[1], yS), sub64(p1[1], yS))),
-                                 mul64(sub64(z1, zS), sub64(z1, zS))));
-    double sv2 = __dsqrt_rn(add64(add64(mul64(sub64(p2[0], xS), sub64(p2[0], xS)),
-                                      mul64(sub64(p2[1], yS), sub64(p2[1], yS))),
-                                 mul64(sub64(z2, zS), sub64(z2, zS))));
-    double lor = add64(add64(mul64(sub64(p1[0], p2[0]), sub64(p1[0], p2[0])),
-                           mul64(sub64(p1[1], p2[1]), sub64(p1[1], p2[1]))),
-                      mul64(sub64(z1, z2), sub64(z1, z2)));
-    double a = mul64(sv1, sv1), b = mul64(sv2, sv2);
-    double q = div64(sub64(add64(a, b), lor), mul64(2.0, __dsqrt_rn(mul64(a, b))));
-    double th = sub64(180.0, mul64(acos(q), 180.0 / 3.141592653589793));
-    double cth = cos(mul64(th, 3.141592653589793 / 180.0));
-    double es = floor(add64(div64(511.0, add64(1.0, mul64(1.0, sub64(1.0, cth)))), 0.5));
-    return (int)mul64(es, 2.0) - 1;
-}
-
-// Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
-// reference's 8001-entry TOF table, :520-528).  w_b is rebuilt from the
-// largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
-// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Bins go two
-// at a time through packed FP32x2 instructions; NP = number of bin pairs.
-template <int NP, bool SINGLE, bool ODD>
-__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
-                                                 const float* sY, const unsigned char* sN,
-                                                 const PairParams& P, bool& tof_bad)
-{
-    // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
-    const float y = __fadd_rd(x, 12582912.0f);
-    int t = __float_as_int(y) - 0x4B400000;
-    float off = y - 12586912.0f;  // t - 4000, exact
-    if ((unsigned)t >= (unsigned)kTofEntries) {
-        if (t < 0 && t + kTofEntries >= 0) {  // numpy negative index wraps (:521, :527)
-            t += kTofEntries;
-            off = (float)(t - kTimeRange);
-        } else {
-            tof_bad = true;
-            return;
-        }
-    }
-    const float Y = sY[t];
-    const float n = (float)sN[t];
-    // beta = 2 kappa w (off - s_n), s_n = s0 + n w
-    const float beta = P.kappa2w * (off - fmaf(n, P.w, P.s0));
-    if constexpr (SINGLE) {
-        acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(P.gamma, n, beta), Y)), acc[0].x);
-    } else {
-        const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
-        const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-P.gamma, -P.gamma);
-        const float2 two = make_float2(2.f, 2.f);
-        float2 nd = make_float2(-n, 1.f - n);  // b - n for the pair (b, b+1)
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-            const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
-            const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
-            // with an odd bin count the last pair's second bin does not exist
-            const float wy = (ODD && k + 1 == NP) ? 0.f : ex2(e2.y);
-            acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), wy), acc[k]);
-            if (k + 1 < NP) nd = __fadd2_rn(nd, two);
-        }
-    }
-}
-
-// One task = (slice, walking leg lw, chunk of 32 partner legs).  Every lane
-// pairs lw with its own partner leg lp; the pair (l1, l2) is ordered as the
-// reference orders it (crystal of l1 < crystal of l2, :469).  The task adds
-// the part of the pair's TOF sum that runs over lw's voxels (AB1 if lw is
-// l1, AB2 if lw is l2, :519-530); the other part comes from the task that
-// walks lp.  Both tasks see the same scatter points, so both divide by the
-// same per-slice count.  All lanes walk the same voxel list: 32 voxels at a
-// time are staged in a per-warp shared buffer and read back as broadcasts,
-// so the trip count is uniform across the warp.
 template <int NP, bool SINGLE, bool ODD, int MINB>
 __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
 {
@@ -316,19 +156,34 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
     float* sY = smem;
     unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
-    for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
-        sY[i] = P.tof_log2w[2 * i];
-        sN[i] = (unsigned char)P.tof_log2w[2 * i + 1];
-    }
+    load_tof_table(P.tof_log2w, sY, sN);
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
     const long long per_slice = (long long)P.nl * P.nchunks;
     const long long ntasks = (long long)P.nslices * per_slice;
-    const float inv_c = (float)(1.0 / kLightCmPerPs);
+    const TofConst T{P.s0, P.w, P.kappa2w, P.gamma};
+    PairCtx C;
+    C.nru = P.nru;
+    C.ndu = P.ndu;
+    C.nl = P.nl;
+    C.nd = P.nd;
+    C.cap = P.cap;
+    C.nbins = P.nbins;
+    C.geo_c = P.geo_c;
+    C.gamma_kn = P.gamma_kn;
+    C.eff = P.eff;
+    C.ratio = P.ratio;
+    C.geom = P.geom;
+    C.rings = P.rings;
+    C.dets = P.dets;
+    C.points = P.points;
+    C.legA = P.legA;
+    C.legB = P.legB;
+    C.vox = P.vox;
+    C.out = P.out;
     bool tof_bad = false, energy_bad = false;
     unsigned long long walked = 0, npairs = 0;
-
     for (;;) {
         long long task = 0;
         if (lane == 0) task = atomicAdd(P.counter, 1u);
@@ -336,129 +191,12 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
         if (task >= ntasks) break;
         const int slice = (int)(task / per_slice);
         const int rem = (int)(task % per_slice);
-        const int lw = rem / P.nchunks;
-        const int dw = lw / P.nru, rw = lw % P.nru;
-
-        // partner of this lane: legs 0..nl-1 (lw leads the pair unless its
-        // crystal is the larger), then one more entry per other ring for the
-        // same crystal in the opposite role (both orders are distinct pairs)
-        const int q = (rem % P.nchunks) * 32 + lane;
-        int lp = lw, rp = rw, dp = dw;
-        bool w_first = true, lane_ok = false;
-        if (q < P.nl) {
-            lp = q;
-            dp = q / P.nru;
-            rp = q % P.nru;
-            lane_ok = lp != lw;
-            w_first = dp >= dw;
-        } else if (q < P.nl + P.nru) {
-            rp = q - P.nl;
-            dp = dw;
-            lp = dw * P.nru + rp;
-            lane_ok = rp != rw;
-            w_first = false;
-        }
-        const int ri1 = w_first ? rw : rp, di1 = w_first ? dw : dp;
-        const int ri2 = w_first ? rp : rw, di2 = w_first ? dp : dw;
-        const int l1 = w_first ? lw : lp, l2 = w_first ? lp : lw;
-        const float sigma = w_first ? -1.f : 1.f;
-
-        float2 acc[NP];
-#pragma unroll
-        for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);
-        float cnt = 0.f;
-
-        const int sfirst = P.slice_first[slice], scount = P.slice_count[slice];
-        for (int s = sfirst; s < sfirst + scount; ++s) {
-            const long long lo = (long long)s * P.nl;
-            const float4 Aw = P.legA[lo + lw], Bw = P.legB[lo + lw];
-            const float4 Ap = P.legA[lo + lp], Bp = P.legB[lo + lp];
-            const float4 A1 = w_first ? Aw : Ap, A2 = w_first ? Ap : Aw;
-            const float4 B1 = w_first ? Bw : Bp, B2 = w_first ? Bp : Bw;
-            bool ok = lane_ok && A1.z != INFINITY && A2.z != INFINITY &&
-                      !(A1.y == 0.f && A2.y == 0.f);
-            float c = 0.f;
-            if (ok) {
-                // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
-                float qc = fmaf(B1.x, B2.x, fmaf(B1.y, B2.y, B1.z * B2.z));
-                qc = fminf(1.f, fmaxf(-1.f, qc));
-                const float e = 511.0f / (2.0f + qc);
-                const float eh = e + 0.5f;
-                const float fr = eh - floorf(eh);
-                int row;
-                if (fr < 1e-3f || fr > 1.0f - 1e-3f)
-                    row = energy_row_fp64(P, s, ri1, di1, ri2, di2);
-                else
-                    row = 2 * (int)floorf(eh) - 1;
-                if (row < 0 || row >= 2000) {
-                    energy_bad = true;
-                } else {
-                    const float effp = __ldg(P.eff + row);
-                    if (effp != 0.f) {  // :508-509 skips before the count is added
-                        const float rr = __ldg(P.ratio + row);
-                        // Klein-Nishina with cos(theta) = -qc (:239-258)
-                        const float ratio = 1.0f / (1.0f + P.gamma_kn * (1.0f + qc));
-                        const float sin2 = 1.0f - qc * qc;
-                        const float kn = ratio * ratio * (ratio + 1.0f / ratio - sin2);
-                        // geometry (:533-536): (ds)^2 |cos a1||cos a2| / (4 pi sv1^2 sv2^2)
-                        const float f = P.geo_c * A1.w * A2.w * effp * kn;
-                        // this task's part: M1 * M2^r * AB1 or M2 * M1^r * AB2 (:540)
-                        const float mw = ex2(-Aw.z), mpr = ex2(-rr * Ap.z);
-                        if (Aw.y != 0.f) c = f * mw * mpr;
-                        cnt += (A1.y != 0.f && A2.y != 0.f) ? 2.f : 1.f;  // :485-488
-                        npairs += 1;
-                    }
-                }
-            }
-            // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
-            const float u = fmaf(A1.x - A2.x, inv_c, 4000.5f);
-            if (__any_sync(0xffffffffu, c != 0.f)) {
-                const int nw = __float_as_int(Bw.w);
-                if (c != 0.f) walked += nw;
-                const float2* vw = P.vox + (lo + lw) * P.cap;
-                for (int k0 = 0; k0 < nw; k0 += 32) {
-                    __syncwarp();
-                    if (k0 + lane < nw) vbuf[lane] = vw[k0 + lane];
-                    __syncwarp();
-                    const int jn = min(32, nw - k0);
-                    if (c != 0.f) {
-#pragma unroll 2
-                        for (int j = 0; j < jn; ++j) {
-                            const float2 v = vbuf[j];
-                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u),
-                                                              sY, sN, P, tof_bad);
-                        }
-                    }
-                }
-            }
-        }
-        if (lane_ok && cnt > 0.f) {
-            float* o = P.out + (long long)l1 * P.nl + l2;
-            const long long plane = (long long)P.nl * P.nl;
-            const float inv = 1.0f / cnt;
-#pragma unroll
-            for (int k = 0; k < NP; ++k) {
-                if (2 * k < P.nbins) atomicAdd(o + (2 * k) * plane, acc[k].x * inv);
-                if (2 * k + 1 < P.nbins) atomicAdd(o + (2 * k + 1) * plane, acc[k].y * inv);
-            }
-        }
+        C.s_first = P.slice_first[slice];
+        C.s_count = P.slice_count[slice];
+        walk_task<NP, SINGLE, ODD>(C, T, rem / P.nchunks, rem % P.nchunks, lane, sY, sN, vbuf, tof_bad,
+                                   energy_bad, walked, npairs);
     }
-    if (tof_bad) raise_error(P.status, kErrTofRange);
-    if (energy_bad) raise_error(P.status, kErrEnergy);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        walked += __shfl_xor_sync(0xffffffffu, walked, o);
-        npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
-    }
-    if (lane == 0 && P.work) {
-        atomicAdd(P.work, walked);
-        atomicAdd(P.work + 1, npairs);
-    }
-}
-
-size_t pair_smem_bytes()
-{
-    return sizeof(float) * kSmemVbufFloats + sizeof(float2) * 32 * kPairWarps;
+    finish_pairs(lane, tof_bad, energy_bad, walked, npairs, P.status, P.work);
 }
 
 template <int NP, bool SINGLE, bool ODD>
@@ -565,11 +303,6 @@ WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
     return w;
 }
 
-// partner chunks per walking leg: nl legs plus nru same-crystal entries
-int chunk_count(const sss_tof_problem& p)
-{
-    return ((p.nru * p.ndu + p.nru) + 31) / 32;
-}
 
 int validate(const sss_tof_problem* p)
 {
@@ -592,6 +325,21 @@ int validate(const sss_tof_problem* p)
 }
 
 }  // namespace
+
+int sss_internal_validate(const sss_tof_problem* p) { return validate(p); }
+
+int sss_internal_scatter_points(const sss_tof_problem* p, double* points, long long capacity,
+                                unsigned long long* counts, cudaStream_t st)
+{
+    LatticeDims L = lattice(*p);
+    const double* IS = p->image_size;
+    const double zvox = (IS[5] - IS[2]) / p->nz;  // :87
+    const double zstart = zvox / 2 - (-IS[2]);    // :176, :179
+    const double radius = -IS[0];                 // :177
+    scatter_points_kernel<<<1, 1024, 0, st>>>(p->attenuation, p->nx, p->ny, p->nz, L, radius, zstart,
+                                               zvox, points, capacity, counts, counts + 1);
+    return sss_check_launch("scatter_points_kernel");
+}
 
 extern "C" int sss_scatter_points(const sss_tof_problem* p, double* points, int64_t capacity,
                                   int64_t* count, int64_t* slice_counts, void* stream)
@@ -715,7 +463,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     PP.legA = LP.legA;
     PP.legB = LP.legB;
     PP.vox = LP.vox;
-    PP.nchunks = chunk_count(*p);
+    PP.nchunks = pair_chunks(p->nru, p->ndu);
     PP.counter = (unsigned int*)(ws + w.counter);
     PP.work = (unsigned long long*)(ws + w.counter + 8);
     PP.out = out;

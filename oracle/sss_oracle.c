@@ -157,6 +157,16 @@ int orc_trace(const int64_t *grid, const double *gb, const double *lc, double ep
 }
 
 /* Batched wrapper: rays [n][6] -> fixed-stride outputs [n][cap]. */
+/* Linear indices past the volume (the reference's sub2ind uses Ny as the x
+ * stride, so Nx != Ny volumes can produce them) make the reference's numpy
+ * indexing raise IndexError; here they are status -6. */
+static int orc_indices_ok(const int32_t *ix, int n, int64_t nvox)
+{
+    for (int k = 0; k < n; ++k)
+        if (ix[k] < 1 || (int64_t)ix[k] > nvox) return 0;
+    return 1;
+}
+
 int orc_trace_batch(const int64_t *grid, const double *gb, const double *lines, int64_t nrays,
                     double eps, int cap, int32_t *counts, double *len, int32_t *idx,
                     double *samp, int nthreads)
@@ -337,6 +347,12 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
 #endif
                     status = -3;
                     n = 0;
+                } else if (!orc_indices_ok(ix, n, p->nx * p->ny * p->nz)) {
+#ifdef _OPENMP
+#pragma omp atomic write
+#endif
+                    status = -6;
+                    n = 0;
                 }
                 double asum = 0, musum = 0;
                 for (int k = 0; k < n; ++k) {
@@ -498,6 +514,7 @@ int orc_mask(const int64_t *grid, const float *mu, const double *gb, int64_t nr,
                     int n = orc_trace(grid, gb, lc, 1e-20, len, ix, sm, cap);
                     double att;
                     if (n < 0) { status = -3; continue; }
+                    if (!orc_indices_ok(ix, n, grid[0] * grid[1] * grid[2])) { status = -6; continue; }
                     if (n != 0) {
                         double s = 0;
                         for (int k = 0; k < n; ++k) s += (double)mu[ix[k] - 1] * len[k];
@@ -566,6 +583,7 @@ int orc_fit(const int64_t *grid, const double *gb, int64_t nr, int64_t nd, const
                     double lc[6] = {p1[0], p1[1], z1, p2[0], p2[1], z2};
                     int n = orc_trace(grid, gb, lc, 1e-20, len, ix, sm, cap);
                     if (n < 0) { status = -3; continue; }
+                    if (!orc_indices_ok(ix, n, nvox)) { status = -6; continue; }
                     if (n > 0) {
                         float fn = (float)n;
                         float ap = pv / fn, as = sv / fn, ar = rv / fn;

@@ -60,6 +60,11 @@ def test_invalid_arguments_fail_before_any_device_work(lib):
     rc = lib.sss_raytrace(grid.ctypes.data_as(C.c_void_p), ok.ctypes.data_as(C.c_void_p), None, 0,
                           2, 12, C.c_void_p(8), None, None, C.c_void_p(8), None, None, None)
     assert rc == 1
+    plan = C.c_void_p(0)
+    rc = lib.sss_batch_plan(None, 0, None, None, 0, None, C.byref(plan), None)
+    assert rc == 1 and not plan.value
+    assert lib.sss_batch_run(None, None) == 1
+    lib.sss_batch_free(None)
 
 
 def test_status_codes(lib):
