@@ -287,6 +287,7 @@ def run_ours(args, rank, world, local_rank):
         err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
 
     pipeline = None if args.no_pipeline else run_pipeline(eng, pr, out, dev, args)
+    batch = None if args.no_batch or world > 1 else run_batch(dev, args, att)
 
     ms = 1e3 * total_s / args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -300,7 +301,8 @@ def run_ours(args, rank, world, local_rank):
                     "path": "TofSSS.run on pinned host volumes, compact result copied back"},
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
-            "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline}
+            "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
+            "batch": batch}
     print(json.dumps(line), flush=True)
 
 
@@ -369,6 +371,75 @@ def run_pipeline(eng, pr, sampled, dev, args):
             "expected_scale": 1.4, "full_sinogram": [nd + 1, nd // 2, nsl]}
 
 
+def run_batch(dev, args, att):
+    """The uneven batch: 64 seeded instances (33..95 voxels across a 40 cm
+    FOV, 24..64 crystals x 8..24 rings, 1/13/33 TOF bins) planned once and
+    replayed as one CUDA graph per step, inputs resident on the device.
+    Compared with the same instances run one after another through
+    TofSSS.run (the plain per-problem path)."""
+    import torch
+
+    from opensss_gb300 import TofSSS, workloads as W
+    from opensss_gb300.batch import BatchSSS
+    from opensss_gb300.engine import fortran_flat
+
+    inst = W.config3_instances(args.batch_size, seed=0)
+    engines, jobs = [], []
+    for pr in inst:
+        e = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
+                   pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used,
+                   pr.sample_step, pr.tof_resolution, pr.tof_range, pr.nr_bins, device=dev)
+        engines.append(e)
+        jobs.append((e, fortran_flat(pr.activity, dev), fortran_flat(pr.attenuation, dev), pr.image_size,
+                     pr.grid))
+    t0 = time.perf_counter()
+    b = BatchSSS(jobs)
+    torch.cuda.synchronize(dev)
+    plan_s = time.perf_counter() - t0
+    b.run()  # checked run (status word) before capturing
+    b.capture()
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        b.replay(check=False)
+    steps = max(1, min(args.steps, args.batch_steps))
+    ms = []
+    with ClockSampler(dev.index or 0) as clk:
+        torch.cuda.synchronize(dev)
+        for _ in range(steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            b.replay(check=False)
+            e1.record(st)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    b.replay(check=True)
+    # plain path: the same problems one after another (one warm-up pass of the smallest)
+    engines[0].run(inst[0].activity, inst[0].attenuation, inst[0].image_size)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for (e, a, m, size, shape) in jobs:
+        e.run_flat(a, m, shape, size, check=False)
+        e._ws = None  # stream-ordered reuse: the next instance takes the same memory
+    e1.record(st)
+    e1.synchronize()
+    solo_ms = e0.elapsed_time(e1)
+    mean_ms = statistics.mean(ms)
+    res = {"workload": f"{len(inst)} uneven instances (seed 0)", "units_per_step": b.units,
+           "scatter_points": b.points, "waves": b.waves, "launches_per_step": b.launches,
+           "graph": True, "steps": steps, "ms_per_step": mean_ms, "value": b.units / (mean_ms / 1e3),
+           "unit": UNIT, "plan_s": plan_s, "plain_sequential_ms": solo_ms,
+           "plain_sequential_value": b.units / (solo_ms / 1e3),
+           "speedup_vs_plain": solo_ms / mean_ms, "clocks": clk.summary(),
+           "plain_note": "scatter points, host sync and leg/pair waves per instance, kernels only"}
+    b.close()
+    del b
+    torch.cuda.empty_cache()
+    return res
+
+
 def _sfu_peak(clocks):
     """SFU 2^x peak measured in this process (sss_probe_ex2_rate: every SM
     issuing independent ex2 chains), else 152 SMs x 16 results/clk x max clock."""
@@ -406,6 +477,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-pipeline", action="store_true", help="skip upsampling / mask / fit timings")
     ap.add_argument("--af", type=int, default=6, help="AccelerationFactor of the mask and fit")
+    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch measurement")
+    ap.add_argument("--batch-size", type=int, default=64, help="instances in the uneven batch")
+    ap.add_argument("--batch-steps", type=int, default=3, help="timed replays of the batch (at most --steps)")
     ap.add_argument("--max-points", type=int, default=None,
                     help="limit each step to the first scatter points (profiling runs only)")
     args = ap.parse_args()

@@ -91,7 +91,32 @@ class BatchSSS:
             _lib.check_status(int(self.status.item()))
         return self.outs
 
+    def capture(self):
+        """Record one run in a CUDA graph; ``replay()`` then enqueues the whole
+        batch (output zeroing, every wave's leg and pair launches) as one
+        graph launch on the current stream."""
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            self.run(stream=s, check=False)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self._graph = g
+        return g
+
+    def replay(self, check: bool = True) -> list[torch.Tensor]:
+        if getattr(self, "_graph", None) is None:
+            raise RuntimeError("capture() first")
+        if check:
+            self.status.zero_()
+        self._graph.replay()
+        if check:
+            torch.cuda.current_stream(self.device).synchronize()
+            _lib.check_status(int(self.status.item()))
+        return self.outs
+
     def close(self):
+        self._graph = None
         if getattr(self, "_plan", None):
             _lib.lib().sss_batch_free(self._plan)
             self._plan = None

@@ -86,43 +86,48 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB)
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
 }
 
+using BatchPairFn = void (*)(const PairItem*, int, long long, TofConst, const float*, unsigned int*,
+                            int32_t*);
+
 template <int NP, bool SINGLE, bool ODD>
-int launch_batch_pairs(const PairItem* items, int nitems, long long ntasks, const TofConst& T,
-                       const float* tof, unsigned int* counter, int32_t* status, cudaStream_t st)
+BatchPairFn batch_pair_fn()
 {
-    constexpr int MINB = NP <= 8 ? 3 : 2;
-    auto kern = batch_pair_kernel<NP, SINGLE, ODD, MINB>;
-    const size_t smem = pair_smem_bytes();
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPairWarps * 32, smem);
-    if (per_sm < 1) per_sm = 1;
-    long long blocks = std::min<long long>((long long)sms * per_sm, (ntasks + kPairWarps - 1) / kPairWarps);
-    if (blocks < 1) blocks = 1;
-    kern<<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(items, nitems, ntasks, T, tof, counter, status);
-    return sss_check_launch("batch_pair_kernel");
+    return batch_pair_kernel<NP, SINGLE, ODD, (NP <= 8 ? 3 : 2)>;
 }
 
-int dispatch_batch_pairs(int nbins, const PairItem* items, int nitems, long long ntasks,
-                         const TofConst& T, const float* tof, unsigned int* counter, int32_t* status,
-                         cudaStream_t st)
+// The pair kernel of a bin count (same register / occupancy choices as sss_tof_run).
+BatchPairFn pick_batch_pairs(int nbins)
 {
-    if (nbins == 1) return launch_batch_pairs<1, true, false>(items, nitems, ntasks, T, tof, counter, status, st);
+    if (nbins == 1) return batch_pair_fn<1, true, false>();
     const bool odd = nbins & 1;
     switch ((nbins + 1) / 2) {
-#define SSS_BNP(k)                                                                                   \
-    case k:                                                                                          \
-        return odd ? launch_batch_pairs<k, false, true>(items, nitems, ntasks, T, tof, counter, status, st) \
-                   : launch_batch_pairs<k, false, false>(items, nitems, ntasks, T, tof, counter, status, st);
+#define SSS_BNP(k) \
+    case k: return odd ? batch_pair_fn<k, false, true>() : batch_pair_fn<k, false, false>();
         SSS_BNP(1) SSS_BNP(2) SSS_BNP(3) SSS_BNP(4) SSS_BNP(5) SSS_BNP(6) SSS_BNP(7) SSS_BNP(8)
         SSS_BNP(9) SSS_BNP(10) SSS_BNP(11) SSS_BNP(12) SSS_BNP(13) SSS_BNP(14) SSS_BNP(15) SSS_BNP(16)
         SSS_BNP(17) SSS_BNP(18) SSS_BNP(19) SSS_BNP(20) SSS_BNP(21) SSS_BNP(22) SSS_BNP(23) SSS_BNP(24)
         SSS_BNP(25) SSS_BNP(26) SSS_BNP(27) SSS_BNP(28) SSS_BNP(29) SSS_BNP(30) SSS_BNP(31) SSS_BNP(32)
 #undef SSS_BNP
     }
-    return sss_set_error(SSS_ERR_INVALID, "nbins out of range");
+    return nullptr;
+}
+
+// Shared-memory opt-in and persistent grid size of a pair launch, decided at
+// plan time so that a run only enqueues launches (and can be captured).
+int prepare_batch_pairs(BatchPairFn fn, long long ntasks, long long* blocks)
+{
+    const size_t smem = pair_smem_bytes();
+    if (cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: %s", cudaGetErrorString(cudaGetLastError()));
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kPairWarps * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    *blocks = std::max<long long>(
+        1, std::min<long long>((long long)sms * per_sm, (ntasks + kPairWarps - 1) / kPairWarps));
+    return SSS_OK;
 }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -158,6 +163,8 @@ struct sss_batch {
         int nitems;
         long long ntasks;
         unsigned int* counter;  // device
+        BatchPairFn fn;
+        long long blocks;
     };
     struct Wave {
         const LegItem* legs;    // device
@@ -329,6 +336,8 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
             Lc.nitems = (int)kv.second.size();
             Lc.ntasks = 0;
             Lc.counter = dctr + nctr++;
+            Lc.fn = pick_batch_pairs(p0.nbins);
+            if (!Lc.fn) return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan: nbins out of range");
             for (size_t j : kv.second) {
                 const Item& it = items[j];
                 const sss_tof_problem& p = problems[it.prob];
@@ -358,6 +367,8 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
                 P.task_begin = Lc.ntasks;
                 Lc.ntasks += (long long)C.nl * P.nchunks;
             }
+            int rc = prepare_batch_pairs(Lc.fn, Lc.ntasks, &Lc.blocks);
+            if (rc) return rc;
             W.launches.push_back(Lc);
         }
         B->waves.push_back(W);
@@ -396,8 +407,9 @@ extern "C" int sss_batch_run(const sss_batch* B, void* stream)
         int rc = sss_check_launch("batch_leg_kernel");
         if (rc) return rc;
         for (const auto& L : W.launches) {
-            rc = dispatch_batch_pairs(L.nbins, L.items, L.nitems, L.ntasks, L.T, L.tof, L.counter, B->status,
-                                      st);
+            L.fn<<<(unsigned)L.blocks, kPairWarps * 32, pair_smem_bytes(), st>>>(
+                L.items, L.nitems, L.ntasks, L.T, L.tof, L.counter, B->status);
+            rc = sss_check_launch("batch_pair_kernel");
             if (rc) return rc;
         }
     }

@@ -128,10 +128,17 @@ class TofSSS:
         lattice order (a partial last slice is normalised over its points,
         like the oracle's bounded samples)."""
         dev = self.device
-        shape = tuple(int(s) for s in (ActivityMap.shape if not isinstance(ActivityMap, torch.Tensor)
-                                       else ActivityMap.shape))
+        shape = tuple(int(s) for s in ActivityMap.shape)
         act = fortran_flat(ActivityMap, dev)
         mu = fortran_flat(AttenuationMap, dev)
+        return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, stream, check)
+
+    def run_flat(self, act, mu, shape, ImageSize, max_points: int | None = None,
+                 wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
+                 check: bool = True) -> torch.Tensor:
+        """``run`` on device-resident maps already flattened in Fortran order
+        (float32, Nx*Ny*Nz)."""
+        dev = self.device
         p = self.problem(act, mu, shape, ImageSize)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         pts, counts = self.scatter_points(p, st)

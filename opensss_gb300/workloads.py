@@ -43,10 +43,12 @@ class Scanner:
 
 
 def ring_scanner(nr_detectors: int = 760, nr_rings: int = 80, radius_cm: float = 41.0,
-                 ring_pitch_cm: float = 0.32, crystal_mm: float = 3.2) -> Scanner:
-    """Ideal cylindrical scanner: crystal k of ring r sits at angle 2*pi*k/ND,
-    axial position (r - (NR-1)/2) * pitch, with an inward unit face normal."""
-    phi = 2.0 * np.pi * np.arange(nr_detectors) / nr_detectors
+                 ring_pitch_cm: float = 0.32, crystal_mm: float = 3.2,
+                 phase: float = 0.0) -> Scanner:
+    """Ideal cylindrical scanner: crystal k of ring r sits at angle
+    2*pi*(k + phase)/ND, axial position (r - (NR-1)/2) * pitch, with an inward
+    unit face normal."""
+    phi = 2.0 * np.pi * (np.arange(nr_detectors) + phase) / nr_detectors
     z = (np.arange(nr_rings) - (nr_rings - 1) / 2.0) * ring_pitch_cm
     geom = np.zeros((nr_rings, nr_detectors, 3))
     geom[:, :, 0] = radius_cm * np.cos(phi)[None, :]
@@ -184,8 +186,17 @@ def config4(seed: int = 0) -> SSSProblem:
 def config3_instances(count: int = 64, seed: int = 0):
     """Uneven batch: volumes from 32x32x24 to 96x96x64 on a 40 cm FOV,
     24-64 detectors x 8-24 rings, TOF bins in {1, 13, 33}, body radius
-    8-18 cm, all drawn from ``seed``."""
+    8-18 cm, all drawn from ``seed``.
+
+    The scanner is rotated by half a crystal.  Scatter points sit on voxel
+    faces ((x+1)*FOV/n - FOV/2, SingleScatterSimulationTOF.py:388, :394); a
+    leg from such a point to a crystal on an axis (x or y exactly 0 or
+    +-41 cm) can pass exactly through voxel corners, where the reference's
+    traversal runs past Nx+Ny+Nz voxels and raises IndexError (seen on several
+    of these volumes with the unrotated ring).  No crystal sits on an axis
+    after the half-crystal rotation."""
     rng = np.random.default_rng(seed)
+    scanner = ring_scanner(phase=0.5)
     out = []
     for i in range(count):
         n = int(rng.integers(32, 97))
@@ -203,7 +214,7 @@ def config3_instances(count: int = 64, seed: int = 0):
         else:
             width, res = 1.5, 214.0
         out.append(make_problem(f"c3-{i}", (n, n, nz), vox, nru, ndu, bins, width, res,
-                                seed=seed * 1000 + i, radius_cm=min(radius, 19.0)))
+                                seed=seed * 1000 + i, radius_cm=min(radius, 19.0), scanner=scanner))
     return out
 
 
