@@ -325,7 +325,7 @@ def run_pipeline(eng, pr, sampled, dev, args):
     ncell, nsl = (nd + 1) * (nd // 2), nr * nr
     cs = torch.from_numpy(tables[0]).to(dev)
     rs = torch.from_numpy(tables[1]).to(dev)
-    t_tables = (cs, rs, tables[2])
+    t_tables = tables
     st = torch.cuda.current_stream(dev)
 
     def timed(fn):

@@ -165,13 +165,16 @@ void sss_batch_free(sss_batch *plan);
  * Upsampling.  Replaces InterpolateAllBins (Python/openSSS/Interpolation.py:197-319)
  * once its nearest-neighbour choices are known (geometry time, see
  * opensss_gb300/geometry.py): out[cell*nslices + s] = sum over the nbins bins
- * of max(sampled[b*bin_stride + cell_src[cell] + ring_src[s]], 0), in bin
- * order (one bin: nbins = 1).  cell = rad*(ND/2) + ang over the full
- * (ND+1) x ND/2 sinogram, s = full-sinogram slice.  The two offset tables
- * (device int64) address either the reference's dense sampled layout or the
- * leg-pair layout of sss_tof_run.  out (device) is [ncell][nslices]. */
+ * of max(sampled[b*bin_stride + cell_src[cell] + ring_off[ring_idx[s]]], 0),
+ * in bin order (one bin: nbins = 1).  cell = rad*(ND/2) + ang over the full
+ * (ND+1) x ND/2 sinogram, s = full-sinogram slice, ring_off = the nring
+ * distinct sampled ring-pair offsets (nring <= 16384), ring_idx[s] in
+ * [0, nring).  The offset tables (device) address either the reference's
+ * dense sampled layout or the leg-pair layout of sss_tof_run.  out (device)
+ * is [ncell][nslices]. */
 int sss_upsample(const float *sampled, int64_t bin_stride, int32_t nbins, const int64_t *cell_src,
-                 const int64_t *ring_src, int64_t ncell, int32_t nslices, float *out, void *stream);
+                 int64_t ncell, const int64_t *ring_off, int32_t nring, const int32_t *ring_idx,
+                 int32_t nslices, float *out, void *stream);
 
 /* Tail mask.  Replaces MaskGenerator / MaskDetectors (Python/openSSS/TailsMask.py:84-228):
  * every LOR (Ring1, d1, Ring2, d2) with d1, d2 multiples of af and d1 <= d2

@@ -26,18 +26,21 @@ def _ptr(t):
 
 def upsample_device(sampled: torch.Tensor, tables, nbins: int, ncell: int, nslices: int,
                     bin_index: int | None = None, out: torch.Tensor | None = None) -> torch.Tensor:
-    """Gather on the device.  bin_index None sums all bins (in bin order)."""
-    cell_src, ring_src, stride = tables
+    """Gather on the device.  ``tables``: geometry.upsample_tables(...).
+    bin_index None sums all bins (in bin order)."""
+    if not isinstance(tables, geometry.UpsampleTables):
+        tables = geometry.UpsampleTables(*(t.cpu().numpy() if isinstance(t, torch.Tensor) else t
+                                           for t in tables[:2]), int(tables[2]))
+    stride = tables[2]
     dev = sampled.device
-    cs = cell_src if isinstance(cell_src, torch.Tensor) else torch.from_numpy(cell_src).to(dev)
-    rs = ring_src if isinstance(ring_src, torch.Tensor) else torch.from_numpy(ring_src).to(dev)
+    cs, ro, ri = tables.on(dev)
     if out is None:
         out = torch.empty((ncell, nslices), dtype=torch.float32, device=dev)
     base = sampled if bin_index is None else sampled.reshape(-1)[bin_index * stride:]
     st = torch.cuda.current_stream(dev)
     _lib.check(_lib.lib().sss_upsample(_ptr(base), stride, nbins if bin_index is None else 1,
-                                       _ptr(cs), _ptr(rs), ncell, nslices, _ptr(out),
-                                       C.c_void_p(st.cuda_stream)))
+                                       _ptr(cs), ncell, _ptr(ro), int(ro.numel()), _ptr(ri), nslices,
+                                       _ptr(out), C.c_void_p(st.cuda_stream)))
     return out
 
 

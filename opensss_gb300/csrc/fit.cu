@@ -3,9 +3,9 @@
 //  * upsample_kernel: the reference's nearest-neighbour upsampling
 //    (Python/openSSS/Interpolation.py:197-319) is a pure gather once the
 //    geometry-time source tables exist: output (cell, slice) copies the
-//    sampled value at cell_src[cell] + ring_src[slice] (clamped at 0 like
-//    fill_with_interp1d, :163), optionally summed over TOF bins in bin order
-//    (:317).  HBM-write bound.
+//    sampled value at cell_src[cell] + ring_off[ring_idx[slice]] (clamped at
+//    0 like fill_with_interp1d, :163), optionally summed over TOF bins in bin
+//    order (:317).  HBM-write bound.
 //  * mask_kernel: MaskDetectors (Python/openSSS/TailsMask.py:84-163): one
 //    thread per LOR on the AccelerationFactor lattice, FP64 walk and FP64
 //    line integral, mask = (1/exp(-sum) == 1).
@@ -55,20 +55,31 @@ __device__ __forceinline__ void lor_line(const double* geom, int nd, int r1, int
 
 // ---------------------------------------------------------------- upsampling
 
-__global__ void upsample_kernel(const float* __restrict__ in, long long bin_stride, int nbins,
-                                const long long* __restrict__ cell_src,
-                                const long long* __restrict__ ring_src, long long ncell, int nslices,
-                                float* __restrict__ out)
+// One sinogram cell per block iteration: the cell's distinct sampled ring
+// pairs (nring values, bins summed in bin order) go to shared memory, then
+// the cell's nslices outputs are written from there with coalesced
+// streaming stores.  Every sampled value a cell needs is read once per cell
+// instead of once per output.
+__global__ void __launch_bounds__(256) upsample_kernel(const float* __restrict__ in, long long bin_stride,
+                                                       int nbins, const long long* __restrict__ cell_src,
+                                                       long long ncell,
+                                                       const long long* __restrict__ ring_off, int nring,
+                                                       const int32_t* __restrict__ ring_idx, int nslices,
+                                                       float* __restrict__ out)
 {
-    const long long total = ncell * nslices;
-    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < total;
-         o += (long long)gridDim.x * blockDim.x) {
-        const long long cell = o / nslices;
-        const int s = (int)(o % nslices);
-        const long long src = cell_src[cell] + ring_src[s];
-        float acc = 0.f;
-        for (int b = 0; b < nbins; ++b) acc += fmaxf(__ldg(in + b * bin_stride + src), 0.f);
-        out[o] = acc;
+    extern __shared__ float vals[];
+    for (long long cell = blockIdx.x; cell < ncell; cell += gridDim.x) {
+        const long long base = cell_src[cell];
+        __syncthreads();  // the previous cell's stores have read vals
+        for (int j = threadIdx.x; j < nring; j += blockDim.x) {
+            const float* src = in + base + ring_off[j];
+            float acc = 0.f;
+            for (int b = 0; b < nbins; ++b) acc += fmaxf(__ldg(src + (long long)b * bin_stride), 0.f);
+            vals[j] = acc;
+        }
+        __syncthreads();
+        float* o = out + cell * nslices;
+        for (int sl = threadIdx.x; sl < nslices; sl += blockDim.x) __stcs(o + sl, vals[__ldg(ring_idx + sl)]);
     }
 }
 
@@ -262,21 +273,21 @@ unsigned blocks_for(long long n, int threads) { return (unsigned)((n + threads -
 
 }  // namespace
 
-extern "C" int sss_upsample(const float* sampled, int64_t bin_stride, int32_t nbins,
-                            const int64_t* cell_src, const int64_t* ring_src, int64_t ncell,
+extern "C" int sss_upsample(const float* sampled, int64_t bin_stride, int32_t nbins, const int64_t* cell_src,
+                            int64_t ncell, const int64_t* ring_off, int32_t nring, const int32_t* ring_idx,
                             int32_t nslices, float* out, void* stream)
 {
-    if (!sampled || !cell_src || !ring_src || !out || nbins < 1 || ncell < 1 || nslices < 1)
+    if (!sampled || !cell_src || !ring_off || !ring_idx || !out || nbins < 1 || ncell < 1 || nslices < 1 ||
+        nring < 1 || nring > 16384)
         return sss_set_error(SSS_ERR_INVALID, "sss_upsample: bad argument");
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long total = (long long)ncell * nslices;
-    const long long want = (total + 255) / 256;
-    const unsigned blocks = (unsigned)(want < (long long)sms * 32 ? want : (long long)sms * 32);
-    upsample_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(
-        sampled, bin_stride, nbins, (const long long*)cell_src, (const long long*)ring_src, ncell,
-        nslices, out);
+    const long long cap = (long long)sms * 8;
+    const unsigned blocks = (unsigned)(ncell < cap ? ncell : cap);
+    upsample_kernel<<<blocks, 256, sizeof(float) * nring, (cudaStream_t)stream>>>(
+        sampled, bin_stride, nbins, (const long long*)cell_src, ncell, (const long long*)ring_off, nring,
+        ring_idx, nslices, out);
     return sss_check_launch("upsample_kernel");
 }
 

@@ -134,6 +134,31 @@ def slice_rings(sino_index: np.ndarray) -> np.ndarray:
     return inv
 
 
+class UpsampleTables(tuple):
+    """``(cell_src, ring_src, bin_stride)`` plus ``ring_off`` (the distinct
+    values of ring_src, int64) and ``ring_idx`` (int32, ring_src =
+    ring_off[ring_idx]): the upsampling kernel stages one cell's distinct
+    ring pairs in shared memory."""
+
+    def __new__(cls, cell_src, ring_src, stride):
+        self = super().__new__(cls, (cell_src, ring_src, stride))
+        off, inv = np.unique(np.asarray(ring_src), return_inverse=True)
+        self.ring_off = np.ascontiguousarray(off, dtype=np.int64)
+        self.ring_idx = np.ascontiguousarray(inv.reshape(-1), dtype=np.int32)
+        self.device_copies = {}
+        return self
+
+    def on(self, device):
+        """(cell_src, ring_off, ring_idx) as device tensors, cached per device."""
+        import torch
+
+        key = str(device)
+        if key not in self.device_copies:
+            self.device_copies[key] = tuple(torch.from_numpy(a).to(device)
+                                            for a in (self[0], self.ring_off, self.ring_idx))
+        return self.device_copies[key]
+
+
 def upsample_tables(lor, sino_index, nru: int, ndu: int, layout: str = "dense"):
     """Gather tables of the upsampling (Interpolation.py:197-319):
     full-sinogram value (cell, slice) = sampled[cell_src[cell] + ring_src[slice]]
@@ -141,7 +166,8 @@ def upsample_tables(lor, sino_index, nru: int, ndu: int, layout: str = "dense"):
 
     layout 'dense'  : the reference's sampled array [bins][ND+1][ND/2][NRU^2]
     layout 'legpair': the engine's [bins][NL][NL], leg = crystal_index*NRU + ring_index
-    Returns (cell_src int64 [(ND+1)*(ND/2)], ring_src int64 [NR*NR], bin_stride)."""
+    Returns UpsampleTables (cell_src int64 [(ND+1)*(ND/2)], ring_src int64
+    [NR*NR], bin_stride)."""
     lor = np.asarray(lor)
     nd = lor.shape[0]
     nr = np.asarray(sino_index).shape[0]
@@ -167,5 +193,5 @@ def upsample_tables(lor, sino_index, nru: int, ndu: int, layout: str = "dense"):
         stride = nl * nl
     else:
         raise ValueError(layout)
-    return (np.ascontiguousarray(cell_src.reshape(-1), dtype=np.int64),
-            np.ascontiguousarray(ring_src, dtype=np.int64), int(stride))
+    return UpsampleTables(np.ascontiguousarray(cell_src.reshape(-1), dtype=np.int64),
+                          np.ascontiguousarray(ring_src, dtype=np.int64), int(stride))

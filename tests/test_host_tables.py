@@ -108,7 +108,10 @@ def test_upsample_gather_tables_reproduce_reference(case, layout):
         src = O.densify(cmp.astype(np.float64), lor, nd, nru, ndu).astype(np.float32)
     else:
         src = _legpair_from_compact(cmp, nru, ndu)
-    cell, ring, stride = G.upsample_tables(lor, si, nru, ndu, layout)
+    t = G.upsample_tables(lor, si, nru, ndu, layout)
+    cell, ring, stride = t
+    assert np.array_equal(t.ring_off[t.ring_idx], ring)  # the kernel's staged form
+    assert len(t.ring_off) <= nru * nru
     flat = src.reshape(-1)
     idx = cell[:, None] + ring[None, :]
     total = np.zeros(idx.shape, np.float32)
