@@ -32,7 +32,8 @@ struct LegItem {
 };
 
 struct PairItem {
-    PairCtx ctx;              // s_first = 0, s_count = the item's points
+    PairCtx ctx;              // legs indexed from the item's first point
+    int npts;                 // the item's points (one z-slice)
     int nchunks;
     long long task_begin;     // prefix over the launch's items of nl * nchunks
 };
@@ -80,8 +81,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB)
         }
         const PairItem& it = items[lo];
         const int rem = (int)(task - it.task_begin);
-        walk_task<NP, SINGLE, ODD>(it.ctx, T, rem / it.nchunks, rem % it.nchunks, lane, sY, sN, vbuf,
-                                   tof_bad, energy_bad, walked, npairs);
+        walk_task<NP, SINGLE, ODD>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sY, sN,
+                                   vbuf, tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
 }
@@ -360,9 +361,8 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
                 C.legA = hleg[j].p.legA;
                 C.legB = hleg[j].p.legB;
                 C.vox = hleg[j].p.vox;
-                C.s_first = 0;
-                C.s_count = (int)it.count;
                 C.out = outs[it.prob];
+                P.npts = (int)it.count;
                 P.nchunks = pair_chunks(p.nru, p.ndu);
                 P.task_begin = Lc.ntasks;
                 Lc.ntasks += (long long)C.nl * P.nchunks;

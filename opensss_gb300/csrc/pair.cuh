@@ -42,7 +42,6 @@ struct PairCtx {
     const float4* legA;      // [point][nl]
     const float4* legB;
     const float2* vox;       // [point][nl][cap]
-    int s_first, s_count;    // the slice's points
     float* out;              // [nbins][nl][nl]
 };
 
@@ -164,8 +163,8 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
 // same voxel list: 32 voxels at a time are staged in the warp's shared
 // buffer and read back as broadcasts, so the trip count is uniform.
 template <int NP, bool SINGLE, bool ODD>
-__device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int lw, int chunk,
-                                          int lane, const float* sY, const unsigned char* sN,
+__device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int s_first, int s_count,
+                                          int lw, int chunk, int lane, const float* sY, const unsigned char* sN,
                                           float2* vbuf, bool& tof_bad, bool& energy_bad,
                                           unsigned long long& walked, unsigned long long& npairs)
 {
@@ -201,7 +200,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
     for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);
     float cnt = 0.f;
 
-    for (int s = C.s_first; s < C.s_first + C.s_count; ++s) {
+    for (int s = s_first; s < s_first + s_count; ++s) {
         const long long lo = (long long)s * C.nl;
         const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw];
         const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp];

@@ -123,29 +123,15 @@ __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
 // ---------------------------------------------------------------- 3. pairs
 
 struct PairParams {
-    int nru, ndu, nl, nd, cap;
-    int nbins;
-    float s0, w;            // first bin centre offset (ps) and bin width (ps)
-    float kappa2w, gamma;   // 2*kappa*w and kappa*w^2, kappa = 4/R^2 (log2 units)
-    float geo_c;            // (ds0*ds1*1e-2)^2 / (4 pi)
-    float gamma_kn;         // E/(m_e c^2) of the reference's KleinNishina
+    PairCtx ctx;            // the problem (legs of the wave's first point at index 0)
+    TofConst T;             // TOF bin centres and Gaussian constants
     const float* tof_log2w; // [8001][2]
-    const float* eff;       // [2000]
-    const float* ratio;     // [2000]
-    const double* geom;
-    const int32_t* rings;
-    const int32_t* dets;
-    const double* points;   // wave's first point
-    const float4* legA;
-    const float4* legB;
-    const float2* vox;
     int nchunks;            // 32-partner chunks per walking leg
     int nslices;
     int slice_first[kMaxWaveSlices];   // first point of slice j within the wave
     int slice_count[kMaxWaveSlices];
     unsigned int* counter;
     unsigned long long* work;  // [0] voxel lists walked per pair, [1] pairs evaluated
-    float* out;             // [nbins][nl][nl]
     int32_t* status;
 };
 
@@ -160,28 +146,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    const long long per_slice = (long long)P.nl * P.nchunks;
+    const long long per_slice = (long long)P.ctx.nl * P.nchunks;
     const long long ntasks = (long long)P.nslices * per_slice;
-    const TofConst T{P.s0, P.w, P.kappa2w, P.gamma};
-    PairCtx C;
-    C.nru = P.nru;
-    C.ndu = P.ndu;
-    C.nl = P.nl;
-    C.nd = P.nd;
-    C.cap = P.cap;
-    C.nbins = P.nbins;
-    C.geo_c = P.geo_c;
-    C.gamma_kn = P.gamma_kn;
-    C.eff = P.eff;
-    C.ratio = P.ratio;
-    C.geom = P.geom;
-    C.rings = P.rings;
-    C.dets = P.dets;
-    C.points = P.points;
-    C.legA = P.legA;
-    C.legB = P.legB;
-    C.vox = P.vox;
-    C.out = P.out;
     bool tof_bad = false, energy_bad = false;
     unsigned long long walked = 0, npairs = 0;
     for (;;) {
@@ -191,10 +157,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
         if (task >= ntasks) break;
         const int slice = (int)(task / per_slice);
         const int rem = (int)(task % per_slice);
-        C.s_first = P.slice_first[slice];
-        C.s_count = P.slice_count[slice];
-        walk_task<NP, SINGLE, ODD>(C, T, rem / P.nchunks, rem % P.nchunks, lane, sY, sN, vbuf, tof_bad,
-                                   energy_bad, walked, npairs);
+        walk_task<NP, SINGLE, ODD>(P.ctx, P.T, P.slice_first[slice], P.slice_count[slice], rem / P.nchunks,
+                                   rem % P.nchunks, lane, sY, sN, vbuf, tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, P.status, P.work);
 }
@@ -211,7 +175,7 @@ int launch_pairs(const PairParams& P, cudaStream_t st)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPairWarps * 32, smem);
     if (per_sm < 1) per_sm = 1;
-    long long ntasks = (long long)P.nslices * P.nl * P.nchunks;
+    long long ntasks = (long long)P.nslices * P.ctx.nl * P.nchunks;
     long long blocks = std::min<long long>((long long)sms * per_sm,
                                            (ntasks + kPairWarps - 1) / kPairWarps);
     if (blocks < 1) blocks = 1;
@@ -221,9 +185,9 @@ int launch_pairs(const PairParams& P, cudaStream_t st)
 
 int dispatch_pairs(const PairParams& P, cudaStream_t st)
 {
-    if (P.nbins == 1) return launch_pairs<1, true, false>(P, st);
-    const bool odd = P.nbins & 1;
-    switch ((P.nbins + 1) / 2) {
+    if (P.ctx.nbins == 1) return launch_pairs<1, true, false>(P, st);
+    const bool odd = P.ctx.nbins & 1;
+    switch ((P.ctx.nbins + 1) / 2) {
 #define SSS_NP(k) \
     case k: return odd ? launch_pairs<k, false, true>(P, st) : launch_pairs<k, false, false>(P, st);
         SSS_NP(1) SSS_NP(2) SSS_NP(3) SSS_NP(4) SSS_NP(5) SSS_NP(6) SSS_NP(7) SSS_NP(8)
@@ -439,34 +403,29 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     LP.status = status;
 
     PairParams PP;
-    PP.nru = p->nru;
-    PP.ndu = p->ndu;
-    PP.nl = (int)nl;
-    PP.nd = p->nd;
-    PP.cap = (int)cap;
-    PP.nbins = p->nbins;
-    const double wbin = p->tof_bin_width;
-    const double kappa = 4.0 / (p->tof_resolution * p->tof_resolution);
-    PP.s0 = (float)((1.0 - (p->nbins + 1) / 2.0) * wbin);  // :282
-    PP.w = (float)wbin;
-    PP.kappa2w = (float)(2.0 * kappa * wbin);
-    PP.gamma = (float)(kappa * wbin * wbin);
-    const double ds = p->detector_size[0] * p->detector_size[1] * 1e-2;
-    PP.geo_c = (float)(ds * ds / (4.0 * 3.141592653589793));
-    PP.gamma_kn = (float)(511.0E3 * 1.6E-19 / (9.10938356E-31 * (299792458.0 * 299792458.0)));
+    PairCtx& C = PP.ctx;
+    C.nru = p->nru;
+    C.ndu = p->ndu;
+    C.nl = (int)nl;
+    C.nd = p->nd;
+    C.cap = (int)cap;
+    C.nbins = p->nbins;
+    C.geo_c = geo_const(*p);
+    C.gamma_kn = gamma_kn_const();
+    C.eff = p->efficiency;
+    C.ratio = p->atten_ratio;
+    C.geom = p->geometry;
+    C.rings = p->rings;
+    C.dets = p->detectors;
+    C.legA = LP.legA;
+    C.legB = LP.legB;
+    C.vox = LP.vox;
+    C.out = out;
+    PP.T = tof_const(*p);
     PP.tof_log2w = p->tof_log2w;
-    PP.eff = p->efficiency;
-    PP.ratio = p->atten_ratio;
-    PP.geom = p->geometry;
-    PP.rings = p->rings;
-    PP.dets = p->detectors;
-    PP.legA = LP.legA;
-    PP.legB = LP.legB;
-    PP.vox = LP.vox;
     PP.nchunks = pair_chunks(p->nru, p->ndu);
     PP.counter = (unsigned int*)(ws + w.counter);
     PP.work = (unsigned long long*)(ws + w.counter + 8);
-    PP.out = out;
     cudaMemsetAsync(ws + w.counter, 0, 256, st);
     PP.status = status;
 
@@ -498,7 +457,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
             leg_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(LP);
             if ((rc = sss_check_launch("leg_kernel"))) return rc;
             if (g_timer.on) cudaEventRecord(g_timer.get(), st);
-            PP.points = LP.points;
+            PP.ctx.points = LP.points;
             cudaMemsetAsync(PP.counter, 0, sizeof(unsigned int), st);
             if (g_timer.on) cudaEventRecord(g_timer.get(), st);
             if ((rc = dispatch_pairs(PP, st))) return rc;
