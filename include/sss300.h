@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SSS300_ABI_VERSION 1
+#define SSS300_ABI_VERSION 2
 
 enum {
     SSS_OK = 0,
@@ -89,7 +89,14 @@ typedef struct sss_tof_problem {
     const float *efficiency;       /* device, [2000]: eff(E)*eff(511 keV); exact 0 where the
                                       FP64 product is 0 (:505-509) */
     const float *atten_ratio;      /* device, [2000]: water mu(E)/mu(511) (:117-120) */
+    int32_t flags;                 /* SSS_FLAG_*; 0 = the plain FP32 reduction */
 } sss_tof_problem;
+
+/* sss_tof_problem.flags.  SSS_FLAG_KAHAN: sum each detector pair's per-point
+ * terms over a z-slice's scatter points with Kahan's compensated addition
+ * (the reference sums them in FP32 too, :551).  Honoured by sss_tof_run;
+ * sss_batch_* always uses the plain reduction. */
+#define SSS_FLAG_KAHAN 1
 
 /* Scatter points on the SampleStep lattice with mu > 0, z-slice major, in the
  * reference's order (:182, :381-394).  points (device) receives [count][4]

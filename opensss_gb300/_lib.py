@@ -14,6 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libsss300.so")
 
 SSS_OK = 0
+ABI_VERSION = 2  # SSS300_ABI_VERSION of include/sss300.h
 ERROR_NAMES = {
     1: "SSS_ERR_INVALID", 2: "SSS_ERR_CUDA", 3: "SSS_ERR_OVERRUN", 4: "SSS_ERR_TOF_RANGE",
     5: "SSS_ERR_ENERGY", 6: "SSS_ERR_VOXEL", 7: "SSS_ERR_WORKSPACE", 8: "SSS_ERR_CAPACITY",
@@ -49,7 +50,11 @@ class TofProblem(C.Structure):
         ("nbins", _I32),
         ("tof_bin_width", _D), ("tof_resolution", _D),
         ("tof_log2w", _P), ("efficiency", _P), ("atten_ratio", _P),
+        ("flags", _I32),
     ]
+
+
+SSS_FLAG_KAHAN = 1
 
 
 SIGNATURES = {
@@ -96,9 +101,15 @@ def lib():
             except OSError as e:  # wrong architecture, missing libcudart, ...
                 raise EngineUnavailable(f"cannot load {LIB_PATH}: {e}") from e
             for name, (res, args) in SIGNATURES.items():
-                f = getattr(h, name)
+                try:
+                    f = getattr(h, name)
+                except AttributeError as e:
+                    raise EngineUnavailable(f"{LIB_PATH} is stale (no {name}); rebuild it") from e
                 f.restype = res
                 f.argtypes = args
+            if h.sss_abi_version() != ABI_VERSION:
+                raise EngineUnavailable(f"{LIB_PATH} has ABI {h.sss_abi_version()}, expected {ABI_VERSION}; "
+                                        "rebuild it")
             _lib = h
     return _lib
 

@@ -81,8 +81,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB)
         }
         const PairItem& it = items[lo];
         const int rem = (int)(task - it.task_begin);
-        walk_task<NP, SINGLE, ODD>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sY, sN,
-                                   vbuf, tof_bad, energy_bad, walked, npairs);
+        walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sY,
+                                          sN, vbuf, nullptr, tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
 }

@@ -17,9 +17,14 @@ constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
 constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
 static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
-inline size_t pair_smem_bytes()
+// Kahan running sums and compensations: float2 [2 * NP][threads], after the voxel buffers
+constexpr int kSmemKahanFloats = kSmemVbufFloats + 2 * 32 * kPairWarps;
+
+// Dynamic shared memory of a pair launch; kahan_np = bin pairs of a
+// Kahan-compensated launch, 0 otherwise.
+inline size_t pair_smem_bytes(int kahan_np = 0)
 {
-    return sizeof(float) * kSmemVbufFloats + sizeof(float2) * 32 * kPairWarps;
+    return sizeof(float) * kSmemKahanFloats + sizeof(float2) * 2 * kahan_np * 32 * kPairWarps;
 }
 
 // TOF constants of one launch (every task of a launch shares one TOF table)
@@ -162,10 +167,10 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
 // so both divide by the same per-slice count (:555-557).  All lanes walk the
 // same voxel list: 32 voxels at a time are staged in the warp's shared
 // buffer and read back as broadcasts, so the trip count is uniform.
-template <int NP, bool SINGLE, bool ODD>
+template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int s_first, int s_count,
                                           int lw, int chunk, int lane, const float* sY, const unsigned char* sN,
-                                          float2* vbuf, bool& tof_bad, bool& energy_bad,
+                                          float2* vbuf, float2* kahan, bool& tof_bad, bool& energy_bad,
                                           unsigned long long& walked, unsigned long long& npairs)
 {
     const float inv_c = (float)(1.0 / kLightCmPerPs);
@@ -199,8 +204,17 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
 #pragma unroll
     for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);
     float cnt = 0.f;
+    constexpr int kStride = 32 * kPairWarps;  // this thread's Kahan column: [j * kStride]
+    if constexpr (KAHAN) {
+#pragma unroll
+        for (int j = 0; j < 2 * NP; ++j) kahan[j * kStride] = make_float2(0.f, 0.f);
+    }
 
     for (int s = s_first; s < s_first + s_count; ++s) {
+        if constexpr (KAHAN) {
+#pragma unroll
+            for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);  // this point's partial
+        }
         const long long lo = (long long)s * C.nl;
         const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw];
         const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp];
@@ -260,6 +274,25 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                     }
                 }
             }
+        }
+        if constexpr (KAHAN) {
+            // sum += partial with Kahan's compensated addition (all terms >= 0)
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                float2 sum = kahan[k * kStride], cmp = kahan[(NP + k) * kStride];
+                const float yx = __fsub_rn(acc[k].x, cmp.x), yy = __fsub_rn(acc[k].y, cmp.y);
+                const float tx = __fadd_rn(sum.x, yx), ty = __fadd_rn(sum.y, yy);
+                cmp = make_float2(__fsub_rn(__fsub_rn(tx, sum.x), yx), __fsub_rn(__fsub_rn(ty, sum.y), yy));
+                kahan[k * kStride] = make_float2(tx, ty);
+                kahan[(NP + k) * kStride] = cmp;
+            }
+        }
+    }
+    if constexpr (KAHAN) {
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            const float2 sum = kahan[k * kStride], cmp = kahan[(NP + k) * kStride];
+            acc[k] = make_float2(__fsub_rn(sum.x, cmp.x), __fsub_rn(sum.y, cmp.y));
         }
     }
     if (lane_ok && cnt > 0.f) {

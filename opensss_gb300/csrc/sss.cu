@@ -23,13 +23,12 @@
 #include "common.cuh"
 #include "legs.cuh"
 #include "pair.cuh"
+#include "pair_launch.cuh"
 #include "trace.cuh"
 
 namespace {
 
 using namespace sss;
-
-constexpr int kMaxWaveSlices = 256;
 
 struct LatticeDims {
     int lx, ly, lz;     // lattice points per axis
@@ -122,83 +121,6 @@ __global__ void __launch_bounds__(128) leg_kernel(LegParams P)
 
 // ---------------------------------------------------------------- 3. pairs
 
-struct PairParams {
-    PairCtx ctx;            // the problem (legs of the wave's first point at index 0)
-    TofConst T;             // TOF bin centres and Gaussian constants
-    const float* tof_log2w; // [8001][2]
-    int nchunks;            // 32-partner chunks per walking leg
-    int nslices;
-    int slice_first[kMaxWaveSlices];   // first point of slice j within the wave
-    int slice_count[kMaxWaveSlices];
-    unsigned int* counter;
-    unsigned long long* work;  // [0] voxel lists walked per pair, [1] pairs evaluated
-    int32_t* status;
-};
-
-template <int NP, bool SINGLE, bool ODD, int MINB>
-__global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
-{
-    extern __shared__ float smem[];
-    float* sY = smem;
-    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
-    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
-    load_tof_table(P.tof_log2w, sY, sN);
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31;
-    const long long per_slice = (long long)P.ctx.nl * P.nchunks;
-    const long long ntasks = (long long)P.nslices * per_slice;
-    bool tof_bad = false, energy_bad = false;
-    unsigned long long walked = 0, npairs = 0;
-    for (;;) {
-        long long task = 0;
-        if (lane == 0) task = atomicAdd(P.counter, 1u);
-        task = __shfl_sync(0xffffffffu, task, 0);
-        if (task >= ntasks) break;
-        const int slice = (int)(task / per_slice);
-        const int rem = (int)(task % per_slice);
-        walk_task<NP, SINGLE, ODD>(P.ctx, P.T, P.slice_first[slice], P.slice_count[slice], rem / P.nchunks,
-                                   rem % P.nchunks, lane, sY, sN, vbuf, tof_bad, energy_bad, walked, npairs);
-    }
-    finish_pairs(lane, tof_bad, energy_bad, walked, npairs, P.status, P.work);
-}
-
-template <int NP, bool SINGLE, bool ODD>
-int launch_pairs(const PairParams& P, cudaStream_t st)
-{
-    constexpr int MINB = NP <= 8 ? 3 : 2;
-    auto kern = pair_kernel<NP, SINGLE, ODD, MINB>;
-    const size_t smem = pair_smem_bytes();
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPairWarps * 32, smem);
-    if (per_sm < 1) per_sm = 1;
-    long long ntasks = (long long)P.nslices * P.ctx.nl * P.nchunks;
-    long long blocks = std::min<long long>((long long)sms * per_sm,
-                                           (ntasks + kPairWarps - 1) / kPairWarps);
-    if (blocks < 1) blocks = 1;
-    kern<<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(P);
-    return sss_check_launch("pair_kernel");
-}
-
-int dispatch_pairs(const PairParams& P, cudaStream_t st)
-{
-    if (P.ctx.nbins == 1) return launch_pairs<1, true, false>(P, st);
-    const bool odd = P.ctx.nbins & 1;
-    switch ((P.ctx.nbins + 1) / 2) {
-#define SSS_NP(k) \
-    case k: return odd ? launch_pairs<k, false, true>(P, st) : launch_pairs<k, false, false>(P, st);
-        SSS_NP(1) SSS_NP(2) SSS_NP(3) SSS_NP(4) SSS_NP(5) SSS_NP(6) SSS_NP(7) SSS_NP(8)
-        SSS_NP(9) SSS_NP(10) SSS_NP(11) SSS_NP(12) SSS_NP(13) SSS_NP(14) SSS_NP(15) SSS_NP(16)
-        SSS_NP(17) SSS_NP(18) SSS_NP(19) SSS_NP(20) SSS_NP(21) SSS_NP(22) SSS_NP(23) SSS_NP(24)
-        SSS_NP(25) SSS_NP(26) SSS_NP(27) SSS_NP(28) SSS_NP(29) SSS_NP(30) SSS_NP(31) SSS_NP(32)
-#undef SSS_NP
-    }
-    return sss_set_error(SSS_ERR_INVALID, "nbins out of range");
-}
-
 // ---------------------------------------------------------------- densify
 
 __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, int nd,
@@ -289,6 +211,9 @@ int validate(const sss_tof_problem* p)
 }
 
 }  // namespace
+
+// The pair kernels of the plain reduction (the compensated ones are in kahan.cu).
+int sss::dispatch_pairs_plain(const PairParams& P, cudaStream_t st) { return dispatch_pairs<false>(P, st); }
 
 int sss_internal_validate(const sss_tof_problem* p) { return validate(p); }
 
@@ -460,7 +385,8 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
             PP.ctx.points = LP.points;
             cudaMemsetAsync(PP.counter, 0, sizeof(unsigned int), st);
             if (g_timer.on) cudaEventRecord(g_timer.get(), st);
-            if ((rc = dispatch_pairs(PP, st))) return rc;
+            if ((rc = (p->flags & SSS_FLAG_KAHAN) ? dispatch_pairs_kahan(PP, st) : dispatch_pairs_plain(PP, st)))
+                return rc;
             if (g_timer.on) cudaEventRecord(g_timer.get(), st);
             g_timer.launches += 2;
             g_timer.waves += 1;

@@ -81,8 +81,9 @@ class TofSSS:
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
 
     # ------------------------------------------------------------------
-    def problem(self, act_flat, mu_flat, shape, image_size) -> _lib.TofProblem:
+    def problem(self, act_flat, mu_flat, shape, image_size, kahan: bool = False) -> _lib.TofProblem:
         p = _lib.TofProblem()
+        p.flags = _lib.SSS_FLAG_KAHAN if kahan else 0
         p.nx, p.ny, p.nz = (int(s) for s in shape)
         p.activity = act_flat.data_ptr()
         p.attenuation = mu_flat.data_ptr()
@@ -121,25 +122,27 @@ class TofSSS:
 
     def run(self, ActivityMap, AttenuationMap, ImageSize, max_points: int | None = None,
             wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
-            check: bool = True) -> torch.Tensor:
+            check: bool = True, kahan: bool = False) -> torch.Tensor:
         """Sampled scatter sinogram, leg-pair layout [B, NL, NL] float32 (CUDA).
 
         ``max_points`` restricts the run to the first scatter points in
         lattice order (a partial last slice is normalised over its points,
-        like the oracle's bounded samples)."""
+        like the oracle's bounded samples).  ``kahan`` sums each pair's
+        per-point terms with Kahan's compensated addition."""
         dev = self.device
         shape = tuple(int(s) for s in ActivityMap.shape)
         act = fortran_flat(ActivityMap, dev)
         mu = fortran_flat(AttenuationMap, dev)
-        return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, stream, check)
+        return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, stream, check,
+                             kahan)
 
     def run_flat(self, act, mu, shape, ImageSize, max_points: int | None = None,
                  wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
-                 check: bool = True) -> torch.Tensor:
+                 check: bool = True, kahan: bool = False) -> torch.Tensor:
         """``run`` on device-resident maps already flattened in Fortran order
         (float32, Nx*Ny*Nz)."""
         dev = self.device
-        p = self.problem(act, mu, shape, ImageSize)
+        p = self.problem(act, mu, shape, ImageSize, kahan)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         pts, counts = self.scatter_points(p, st)
         if max_points is not None:

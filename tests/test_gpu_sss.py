@@ -144,3 +144,27 @@ def test_tof_bins_sum_to_nontof(cuda_ok, att_table):
     non = _gpu_compact(pr1, att_table)
     # weights only sum to one away from the table edges; the tiny scanner stays inside
     assert rel_l2(tof.sum(axis=0), non[0]) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["sss_tiny_b5", "sss_c1"])
+def test_kahan_reduction_matches_reference(cuda_ok, att_table, name):
+    """SSS_FLAG_KAHAN (compensated sum over the scatter points) stays within
+    the same 1e-4 bar and agrees with the plain reduction to FP32 noise."""
+    g = golden(name)
+    pr = problem_from_golden(g)
+    plain = _gpu_compact(pr, att_table)
+    kahan = _gpu_compact(pr, att_table, kahan=True)
+    ref = g["compact"]
+    assert_same_support(kahan, ref)
+    assert rel_l2(kahan, ref) < TOL
+    assert rel_l2(kahan, plain) < 1e-5
+
+
+def test_kahan_on_config4_sample(cuda_ok, att_table):
+    from opensss_gb300 import workloads as W
+
+    pr = W.config4()
+    got = _gpu_compact(pr, att_table, max_points=6, kahan=True)
+    ref = _oracle_compact(pr, att_table, sp_end=6)
+    assert_same_support(got, ref)
+    assert rel_l2(got, ref) < TOL
