@@ -288,6 +288,7 @@ def run_ours(args, rank, world, local_rank):
 
     pipeline = None if args.no_pipeline else run_pipeline(eng, pr, out, dev, args)
     batch = None if args.no_batch or world > 1 else run_batch(dev, args, att)
+    precision = None if args.no_precision or world > 1 else run_precision(dev, args, att)
 
     ms = 1e3 * total_s / args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -302,7 +303,7 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
             "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
-            "batch": batch}
+            "batch": batch, "precision": precision}
     print(json.dumps(line), flush=True)
 
 
@@ -440,6 +441,100 @@ def run_batch(dev, args, att):
     return res
 
 
+def run_precision(dev, args, att):
+    """The precision-stress instance: 128x128x96 @ 4 mm, 32 rings x 96
+    crystals, 33 TOF bins of 15 mm.  Full-size throughput with the plain and
+    the Kahan-compensated scatter-point reduction, then both against the FP64
+    oracle on the first ``--precision-points`` scatter points: relative L2,
+    largest bin error (over the largest reference bin) and the fitted scale
+    of the centre TOF bin (prompts drawn from the FP64 scatter)."""
+    import torch
+
+    from opensss_gb300 import TofSSS, geometry as G, workloads as W
+    from opensss_gb300.BackProjection import fit_device
+    from opensss_gb300.engine import compact_to_leg_pair, fortran_flat, leg_pair_to_compact
+    from opensss_gb300.Interpolation import upsample_device
+    from opensss_gb300.TailsMask import tail_mask_device
+
+    pr = W.config4(seed=0)
+    eng = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
+                 pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used,
+                 pr.sample_step, pr.tof_resolution, pr.tof_range, pr.nr_bins, device=dev)
+    act, mu = fortran_flat(pr.activity, dev), fortran_flat(pr.attenuation, dev)
+    p = eng.problem(act, mu, pr.grid, pr.image_size)
+    _, counts = eng.scatter_points(p)
+    nsp = int(counts.sum())
+    units = nsp * _pairs(pr.nr_rings_used, pr.nr_detectors_used) * pr.nr_bins
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    full = {}
+    with ClockSampler(dev.index or 0) as clk:
+        for kahan in (False, True):
+            for _ in range(args.precision_warmup):
+                eng.run_flat(act, mu, pr.grid, pr.image_size, kahan=kahan)
+            ms = []
+            for _ in range(args.precision_steps):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                eng.run_flat(act, mu, pr.grid, pr.image_size, kahan=kahan, check=False)
+                e1.record(st)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            key = "kahan" if kahan else "plain"
+            full[key] = {"ms_per_step": statistics.mean(ms), "value": units / (statistics.mean(ms) / 1e3),
+                         "steps": args.precision_steps, "warmup": args.precision_warmup}
+    eng._ws = None
+    # errors on a bounded sample against the FP64 oracle
+    n = args.precision_points
+    ref, _ = oracle_sample(pr, att, n, cpu_threads())
+    nru, ndu = pr.nr_rings_used, pr.nr_detectors_used
+    outs = {k: eng.run_flat(act, mu, pr.grid, pr.image_size, max_points=n, kahan=(k == "kahan"))
+            for k in ("plain", "kahan")}
+    err = {}
+    for k, o in outs.items():
+        got = leg_pair_to_compact(o.cpu().numpy(), nru, ndu).astype(np.float64)
+        err[k] = {"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                  "max_bin": float(np.abs(got - ref).max() / np.abs(ref).max())}
+    # fitted scale of the centre bin
+    nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    tables = G.upsample_tables(lor, si, nru, ndu, "legpair")
+    cs, rs = torch.from_numpy(tables[0]).to(dev), torch.from_numpy(tables[1]).to(dev)
+    ncell, nsl = (nd + 1) * (nd // 2), nr * nr
+    b = pr.nr_bins // 2
+    ref_lp = torch.from_numpy(compact_to_leg_pair(ref.astype(np.float32), nru, ndu)[b]).to(dev)
+    up = upsample_device(ref_lp.reshape(1, -1), tables, 1, ncell, nsl)
+    k = 20.0 / max(float(up.mean()), 1e-30)
+    randoms = torch.full_like(up, 0.1 * 1.4 * 20.0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(11)
+    prompts = torch.poisson(1.4 * k * up + randoms, generator=gen)
+    del up
+    mask = tail_mask_device(pr.attenuation, pr.image_size, pr.scanner.geometry, lor, si, args.af, device=dev)
+    zr = float(pr.scanner.geometry[-1, 0, 2]) + 0.16
+    fit_bounds = np.array([pr.image_size[0], pr.image_size[1], -zr, pr.image_size[3], pr.image_size[4], zr])
+    order = si[:nr, :nr].T
+
+    def fit(scatter_lp):
+        return fit_device(prompts, randoms, mask, scatter_lp, cs, rs, np.array([40, 40, 26]), fit_bounds,
+                          pr.scanner.geometry, lor, order, args.af, scat_clamp=True, device=dev) / k
+
+    s_ref = fit(ref_lp)
+    for key, o in outs.items():
+        s = fit(o[b].contiguous())
+        err[key]["fitted_scale"] = s
+        err[key]["fitted_scale_rel_err"] = abs(s - s_ref) / abs(s_ref)
+    del prompts, randoms, mask
+    torch.cuda.empty_cache()
+    return {"workload": pr.name, "volume": list(pr.grid), "sampled_rings": nru, "sampled_crystals": ndu,
+            "tof_bins": pr.nr_bins, "scatter_points": nsp, "units_per_step": units, "full": full,
+            "clocks": clk.summary(),
+            "error_vs_fp64_oracle": err, "fp64_fitted_scale": s_ref, "fit_bin": b,
+            "sample": f"first {n} scatter points ({n * _pairs(nru, ndu) * pr.nr_bins:.3e} units)",
+            "fp64_oracle": "oracle/sss_oracle.c (FP64 C restatement), host cores"}
+
+
 def _sfu_peak(clocks):
     """SFU 2^x peak measured in this process (sss_probe_ex2_rate: every SM
     issuing independent ex2 chains), else 152 SMs x 16 results/clk x max clock."""
@@ -480,6 +575,11 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-batch measurement")
     ap.add_argument("--batch-size", type=int, default=64, help="instances in the uneven batch")
     ap.add_argument("--batch-steps", type=int, default=3, help="timed replays of the batch (at most --steps)")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 33-bin precision study")
+    ap.add_argument("--precision-points", type=int, default=32,
+                    help="scatter points of the FP64 oracle sample in the precision study")
+    ap.add_argument("--precision-steps", type=int, default=1)
+    ap.add_argument("--precision-warmup", type=int, default=1)
     ap.add_argument("--max-points", type=int, default=None,
                     help="limit each step to the first scatter points (profiling runs only)")
     args = ap.parse_args()

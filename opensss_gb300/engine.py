@@ -203,3 +203,10 @@ def leg_pair_to_compact(lp: np.ndarray, nru: int, ndu: int) -> np.ndarray:
     b = lp.shape[0]
     x = lp.reshape(b, ndu, nru, ndu, nru).transpose(0, 2, 4, 1, 3)
     return x.reshape(b, nru * nru, ndu, ndu)
+
+
+def compact_to_leg_pair(cmp: np.ndarray, nru: int, ndu: int) -> np.ndarray:
+    """Inverse of ``leg_pair_to_compact``: [B, NRU*NRU, NDU, NDU] -> [B, NL, NL]."""
+    b = cmp.shape[0]
+    x = cmp.reshape(b, nru, nru, ndu, ndu).transpose(0, 3, 1, 4, 2)
+    return np.ascontiguousarray(x.reshape(b, nru * ndu, nru * ndu))

@@ -179,8 +179,14 @@ def config2(seed: int = 0) -> SSSProblem:
 
 def config4(seed: int = 0) -> SSSProblem:
     """Precision stress: 128x128x96 @ 4 mm, 32 rings x 96 detectors,
-    33 TOF bins of 15 mm, 214 ps FWHM."""
-    return make_problem("c4-tof33-128x128x96", (128, 128, 96), 0.4, 32, 96, 33, 1.5, 214.0, seed)
+    33 TOF bins of 15 mm, 214 ps FWHM.
+
+    The scanner is rotated by half a crystal: with crystal 0 at (41, 0) cm,
+    736 of the 35 million legs of this volume (scatter points on voxel faces
+    to that crystal, through exact voxel corners) make the reference's
+    traversal run past Nx+Ny+Nz voxels and raise IndexError."""
+    return make_problem("c4-tof33-128x128x96", (128, 128, 96), 0.4, 32, 96, 33, 1.5, 214.0, seed,
+                        scanner=ring_scanner(phase=0.5))
 
 
 def config3_instances(count: int = 64, seed: int = 0):
