@@ -165,6 +165,21 @@ typedef struct sss_batch sss_batch;
 int sss_batch_plan(const sss_tof_problem *problems, int32_t n, float *const *outs, void *workspace,
                    size_t workspace_bytes, int32_t *status, sss_batch **plan, void *stream);
 int sss_batch_run(const sss_batch *plan, void *stream);
+/* sss_batch_plan for problems whose scatter points are already known (for
+ * instance from sss_scatter_points, which depend on the attenuation map
+ * only): points[i] (device, [count][4]) and slice_counts[i] (host,
+ * ceil(nz/step_z) entries) for each problem.  Does not synchronise `stream`
+ * except to upload the plan's descriptors; the point arrays must outlive the
+ * plan's last run. */
+int sss_batch_plan_points(const sss_tof_problem *problems, int32_t n, float *const *outs,
+                          const double *const *points, const int64_t *const *slice_counts,
+                          void *workspace, size_t workspace_bytes, int32_t *status, sss_batch **plan,
+                          void *stream);
+/* Run waves [first, first + count) of a plan (0 <= first, first + count <=
+ * info[0]).  Waves must run in order, each once per run, and the outputs are
+ * complete after the last; starting at wave 0 zeroes them.  A caller can
+ * interleave other work between waves (continuous batching). */
+int sss_batch_run_waves(const sss_batch *plan, int32_t first, int32_t count, void *stream);
 int sss_batch_info(const sss_batch *plan, int64_t info[4]);
 void sss_batch_free(sss_batch *plan);
 

@@ -72,6 +72,9 @@ SIGNATURES = {
     "sss_batch_plan": (C.c_int, [C.POINTER(TofProblem), _I32, _P, _P, C.c_size_t, _P,
                                  C.POINTER(_P), _P]),
     "sss_batch_run": (C.c_int, [_P, _P]),
+    "sss_batch_plan_points": (C.c_int, [C.POINTER(TofProblem), _I32, _P, _P, _P, _P, C.c_size_t, _P,
+                                        C.POINTER(_P), _P]),
+    "sss_batch_run_waves": (C.c_int, [_P, _I32, _I32, _P]),
     "sss_batch_info": (C.c_int, [_P, _P]),
     "sss_batch_free": (None, [_P]),
     "sss_upsample": (C.c_int, [_P, _I64, _I32, _P, _I64, _P, _I32, _P, _I32, _P, _P]),

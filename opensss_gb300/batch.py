@@ -29,7 +29,13 @@ class BatchSSS:
     element of the job tuple.
     """
 
-    def __init__(self, jobs, workspace_bytes: int | None = None, stream=None):
+    def __init__(self, jobs, workspace_bytes: int | None = None, stream=None, points=None,
+                 workspace: torch.Tensor | None = None, outs=None):
+        """``points``: optional per-job ``(points, slice_counts)`` from
+        ``TofSSS.scatter_points`` (they depend on the attenuation map only);
+        with them the plan skips the scatter-point pass.  ``workspace`` /
+        ``outs``: caller-owned device buffers to plan into (otherwise
+        allocated here)."""
         if not jobs:
             raise ValueError("empty batch")
         L = _lib.lib()
@@ -54,19 +60,32 @@ class BatchSSS:
             self.engines.append(eng)
             self.shapes.append(shape)
             self._keep.append((act_f, mu_f))
-        self.outs = [torch.empty((e.nbins, e.nl, e.nl), dtype=torch.float32, device=dev)
-                     for e in self.engines]
+        self.outs = list(outs) if outs is not None else [
+            torch.empty((e.nbins, e.nl, e.nl), dtype=torch.float32, device=dev) for e in self.engines]
         out_ptrs = (C.c_void_p * len(jobs))(*[o.data_ptr() for o in self.outs])
-        if workspace_bytes is None:
-            workspace_bytes = min(WS_BUDGET_BYTES, int(torch.cuda.mem_get_info(dev)[0] * 0.5))
-        self.workspace = torch.empty(int(workspace_bytes), dtype=torch.uint8, device=dev)
+        if workspace is None:
+            if workspace_bytes is None:
+                workspace_bytes = min(WS_BUDGET_BYTES, int(torch.cuda.mem_get_info(dev)[0] * 0.5))
+            workspace = torch.empty(int(workspace_bytes), dtype=torch.uint8, device=dev)
+        self.workspace = workspace
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._probs = probs
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         plan = C.c_void_p(0)
-        _lib.check(L.sss_batch_plan(probs, len(jobs), C.cast(out_ptrs, C.c_void_p), _ptr(self.workspace),
-                                    self.workspace.numel(), _ptr(self.status), C.byref(plan),
-                                    C.c_void_p(st.cuda_stream)))
+        if points is None:
+            _lib.check(L.sss_batch_plan(probs, len(jobs), C.cast(out_ptrs, C.c_void_p),
+                                        _ptr(self.workspace), self.workspace.numel(), _ptr(self.status),
+                                        C.byref(plan), C.c_void_p(st.cuda_stream)))
+        else:
+            counts = [np.ascontiguousarray(c, dtype=np.int64) for _, c in points]
+            self._points = (points, counts)
+            pts = (C.c_void_p * len(jobs))(*[pt.data_ptr() if pt.numel() else 0 for pt, _ in points])
+            cts = (C.c_void_p * len(jobs))(*[c.ctypes.data for c in counts])
+            _lib.check(L.sss_batch_plan_points(probs, len(jobs), C.cast(out_ptrs, C.c_void_p),
+                                               C.cast(pts, C.c_void_p), C.cast(cts, C.c_void_p),
+                                               _ptr(self.workspace), self.workspace.numel(),
+                                               _ptr(self.status), C.byref(plan),
+                                               C.c_void_p(st.cuda_stream)))
         self._plan = plan
         info = np.zeros(4, dtype=np.int64)
         _lib.check(L.sss_batch_info(plan, info.ctypes.data_as(C.c_void_p)))
@@ -90,6 +109,15 @@ class BatchSSS:
             st.synchronize()
             _lib.check_status(int(self.status.item()))
         return self.outs
+
+    def run_waves(self, first: int, count: int, stream=None):
+        """Enqueue waves [first, first + count) (in order; wave 0 zeroes the
+        outputs).  No synchronisation, no status check."""
+        if self._plan is None:
+            raise RuntimeError("batch plan was freed")
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(_lib.lib().sss_batch_run_waves(self._plan, int(first), int(count),
+                                                  C.c_void_p(st.cuda_stream)))
 
     def capture(self):
         """Record one run in a CUDA graph; ``replay()`` then enqueues the whole

@@ -171,6 +171,7 @@ struct sss_batch {
         const LegItem* legs;    // device
         int nlegs;
         long long threads;
+        int ctr_first;          // the wave's launch counters: counters[ctr_first ..]
         std::vector<Launch> launches;
     };
     std::vector<sss_tof_problem> problems;
@@ -183,19 +184,40 @@ struct sss_batch {
     long long units = 0;
 };
 
-extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float* const* outs,
-                              void* workspace, size_t workspace_bytes, int32_t* status,
-                              sss_batch** plan, void* stream)
+namespace {
+
+// Checks shared by both planning entry points.
+int check_plan_args(const sss_tof_problem* problems, int32_t n, float* const* outs, void* workspace,
+                    sss_batch** plan)
 {
     if (!problems || n < 1 || !outs || !workspace || !plan)
         return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan: bad argument");
     *plan = nullptr;
-    cudaStream_t st = (cudaStream_t)stream;
     for (int i = 0; i < n; ++i) {
         int rc = sss_internal_validate(&problems[i]);
         if (rc) return rc;
         if (!outs[i]) return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan: null output %d", i);
     }
+    return SSS_OK;
+}
+
+// Items, waves and descriptors of a plan whose scatter points are known:
+// points[i] (device, [count][4]) and counts[i][z] (points of sampled slice z)
+// for every problem.  The descriptors go to the workspace from `off` on.
+int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
+               const std::vector<const double*>& points,
+               const std::vector<std::vector<unsigned long long>>& counts, char* ws, size_t off,
+               size_t workspace_bytes, int32_t* status, sss_batch** plan, cudaStream_t st);
+
+}  // namespace
+
+extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float* const* outs,
+                              void* workspace, size_t workspace_bytes, int32_t* status,
+                              sss_batch** plan, void* stream)
+{
+    int rc = check_plan_args(problems, n, outs, workspace, plan);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
     char* ws = (char*)workspace;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -222,15 +244,61 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
         if (rc) return rc;
     }
     std::vector<std::vector<unsigned long long>> counts(n);
+    std::vector<std::vector<unsigned long long>> raw(n);
     for (int i = 0; i < n; ++i) {
-        counts[i].resize((size_t)(1 + lat[i].lz));
-        if (cudaMemcpyAsync(counts[i].data(), ws + cnt_off[i], counts[i].size() * sizeof(unsigned long long),
+        raw[i].resize((size_t)(1 + lat[i].lz));
+        if (cudaMemcpyAsync(raw[i].data(), ws + cnt_off[i], raw[i].size() * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, st) != cudaSuccess)
             return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: count copy failed");
     }
     if (cudaStreamSynchronize(st) != cudaSuccess)
         return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: %s", cudaGetErrorString(cudaGetLastError()));
+    std::vector<const double*> points(n);
+    for (int i = 0; i < n; ++i) {
+        counts[i].assign(raw[i].begin() + 1, raw[i].end());
+        points[i] = (const double*)(ws + pts_off[i]);
+    }
+    return plan_items(problems, n, outs, points, counts, ws, off, workspace_bytes, status, plan, st);
+}
 
+extern "C" int sss_batch_plan_points(const sss_tof_problem* problems, int32_t n, float* const* outs,
+                                     const double* const* points, const int64_t* const* slice_counts,
+                                     void* workspace, size_t workspace_bytes, int32_t* status,
+                                     sss_batch** plan, void* stream)
+{
+    int rc = check_plan_args(problems, n, outs, workspace, plan);
+    if (rc) return rc;
+    if (!points || !slice_counts) return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan_points: bad argument");
+    std::vector<const double*> pts(n);
+    std::vector<std::vector<unsigned long long>> counts(n);
+    for (int i = 0; i < n; ++i) {
+        const LatticeSize lat = lattice_size(problems[i]);
+        if (!slice_counts[i] || (!points[i] && lat.capacity > 0))
+            return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan_points: null points of problem %d", i);
+        counts[i].resize((size_t)lat.lz);
+        for (long long z = 0; z < lat.lz; ++z) {
+            if (slice_counts[i][z] < 0)
+                return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan_points: negative count");
+            counts[i][(size_t)z] = (unsigned long long)slice_counts[i][z];
+        }
+        pts[i] = points[i];
+    }
+    return plan_items(problems, n, outs, pts, counts, (char*)workspace, 0, workspace_bytes, status, plan,
+                      (cudaStream_t)stream);
+}
+
+namespace {
+
+int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
+               const std::vector<const double*>& points,
+               const std::vector<std::vector<unsigned long long>>& counts, char* ws, size_t off,
+               size_t workspace_bytes, int32_t* status, sss_batch** plan, cudaStream_t st)
+{
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
     // 2. items = (problem, z-slice) with points
     struct Item {
         int prob;
@@ -243,8 +311,8 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
     B->status = status;
     for (int i = 0; i < n; ++i) {
         long long first = 0;
-        for (long long z = 0; z < lat[i].lz; ++z) {
-            const long long c = (long long)counts[i][1 + z];
+        for (size_t z = 0; z < counts[i].size(); ++z) {
+            const long long c = (long long)counts[i][z];
             if (c > 0) items.push_back({i, first, c});
             first += c;
         }
@@ -285,6 +353,7 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
                                  "only %zu available", items[k].prob,
                                  item_bytes(problems[items[k].prob], items[k].count), data_bytes);
         sss_batch::Wave W;
+        W.ctr_first = nctr;
         W.legs = dleg + k;
         W.nlegs = (int)(k_end - k);
         W.threads = 0;
@@ -312,7 +381,7 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
             L.p.nl = (int)nl;
             L.p.cap = (int)cap;
             L.p.nvox = (long long)p.nx * p.ny * p.nz;
-            L.p.points = (const double*)(ws + pts_off[it.prob]) + 4 * it.first;
+            L.p.points = points[it.prob] + 4 * it.first;
             L.p.npts = (int)it.count;
             L.p.legA = (float4*)(ws + doff);
             doff += align256(sizeof(float4) * it.count * nl);
@@ -389,20 +458,30 @@ extern "C" int sss_batch_plan(const sss_tof_problem* problems, int32_t n, float*
     return SSS_OK;
 }
 
-extern "C" int sss_batch_run(const sss_batch* B, void* stream)
+}  // namespace
+
+extern "C" int sss_batch_run_waves(const sss_batch* B, int32_t first, int32_t count, void* stream)
 {
     if (!B) return sss_set_error(SSS_ERR_INVALID, "sss_batch_run: null plan");
+    const int nw = (int)B->waves.size();
+    if (first < 0 || count < 0 || first > nw || count > nw - first)
+        return sss_set_error(SSS_ERR_INVALID, "sss_batch_run_waves: waves [%d, %d) outside [0, %d)", first,
+                             first + count, nw);
     cudaStream_t st = (cudaStream_t)stream;
-    for (size_t i = 0; i < B->problems.size(); ++i) {
-        const sss_tof_problem& p = B->problems[i];
-        const size_t nl = (size_t)p.nru * p.ndu;
-        if (cudaMemsetAsync(B->outs[i], 0, sizeof(float) * p.nbins * nl * nl, st) != cudaSuccess)
-            return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
+    if (first == 0) {
+        for (size_t i = 0; i < B->problems.size(); ++i) {
+            const sss_tof_problem& p = B->problems[i];
+            const size_t nl = (size_t)p.nru * p.ndu;
+            if (cudaMemsetAsync(B->outs[i], 0, sizeof(float) * p.nbins * nl * nl, st) != cudaSuccess)
+                return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
+        }
     }
-    if (B->ncounters > 0 &&
-        cudaMemsetAsync(B->counters, 0, sizeof(unsigned int) * B->ncounters, st) != cudaSuccess)
-        return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
-    for (const auto& W : B->waves) {
+    for (int w = first; w < first + count; ++w) {
+        const auto& W = B->waves[(size_t)w];
+        if (!W.launches.empty() &&
+            cudaMemsetAsync(B->counters + W.ctr_first, 0, sizeof(unsigned int) * W.launches.size(), st) !=
+                cudaSuccess)
+            return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
         batch_leg_kernel<<<(unsigned)((W.threads + 127) / 128), 128, 0, st>>>(W.legs, W.nlegs, W.threads);
         int rc = sss_check_launch("batch_leg_kernel");
         if (rc) return rc;
@@ -414,6 +493,12 @@ extern "C" int sss_batch_run(const sss_batch* B, void* stream)
         }
     }
     return SSS_OK;
+}
+
+extern "C" int sss_batch_run(const sss_batch* B, void* stream)
+{
+    if (!B) return sss_set_error(SSS_ERR_INVALID, "sss_batch_run: null plan");
+    return sss_batch_run_waves(B, 0, (int32_t)B->waves.size(), stream);
 }
 
 extern "C" int sss_batch_info(const sss_batch* B, int64_t* info)

@@ -234,3 +234,14 @@ def tiny_problem(nr_bins: int = 3, seed: int = 0, shape=(12, 12, 6), nd: int = 4
         width, res = 3.0, 214.0
     return make_problem(f"tiny-b{nr_bins}", shape, voxel_cm, nru, ndu, nr_bins, width, res,
                         seed=seed, scanner=scanner, radius_cm=8.0)
+
+
+def served_beds(seed: int = 0):
+    """Resident problems of the served workload: four small bed positions of
+    the plain non-TOF size (40x40x20 @ 1 cm, 8 rings x 32 crystals, phantoms
+    seeded per bed) and four large ones drawn by the uneven-batch generator
+    (seed 5).  Returns (small, large)."""
+    small = [dataclasses.replace(config1(seed=seed * 10 + b), name=f"bed{b}-small") for b in range(4)]
+    large = [dataclasses.replace(pr, name=f"bed{b}-large")
+             for b, pr in enumerate(config3_instances(4, seed=5))]
+    return small, large
