@@ -289,6 +289,7 @@ def run_ours(args, rank, world, local_rank):
     pipeline = None if args.no_pipeline else run_pipeline(eng, pr, out, dev, args)
     batch = None if args.no_batch or world > 1 else run_batch(dev, args, att)
     precision = None if args.no_precision or world > 1 else run_precision(dev, args, att)
+    serving = None if args.no_serving or world > 1 else run_serving(dev, args, att)
 
     ms = 1e3 * total_s / args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -303,7 +304,7 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
             "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
-            "batch": batch, "precision": precision}
+            "batch": batch, "precision": precision, "serving": serving}
     print(json.dumps(line), flush=True)
 
 
@@ -535,6 +536,59 @@ def run_precision(dev, args, att):
             "fp64_oracle": "oracle/sss_oracle.c (FP64 C restatement), host cores"}
 
 
+def run_serving(dev, args, att):
+    """The served workload: seeded Poisson arrivals (``--serve-rate`` req/s for
+    ``--serve-seconds``), 70% small requests (four plain non-TOF bed positions,
+    40x40x20 @ 1 cm, 8 x 32 virtual) and 30% large ones (four beds drawn by the
+    uneven-batch generator), each a scatter update with the bed's activity
+    times 1 +- 5% seeded noise.  The batching server (admission by an 80 GB
+    HBM budget, continuous batching at wave granularity) against the plain
+    path, one request at a time in arrival order, on the same stream."""
+    from opensss_gb300 import TofSSS, workloads as W
+    from opensss_gb300.engine import leg_pair_to_compact
+    from opensss_gb300.serving import (PlainServer, ScatterServer, latency_summary, make_bed,
+                                       poisson_stream, request_activity)
+    from oracle import oracle as O
+
+    small, large = W.served_beds()
+    beds = []
+    for pr, is_large in [(p, False) for p in small] + [(p, True) for p in large]:
+        e = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
+                   pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used,
+                   pr.sample_step, pr.tof_resolution, pr.tof_range, pr.nr_bins, device=dev)
+        beds.append(make_bed(e, pr.activity, pr.attenuation, pr.image_size, large=is_large))
+    problems = small + large
+    # warm-up stream (first launches of every kernel shape)
+    ScatterServer(beds).serve(poisson_stream(args.serve_rate, 0.05, beds, 0.7, seed=1))
+    PlainServer(beds).serve(poisson_stream(args.serve_rate, 0.02, beds, 0.7, seed=1))
+    with ClockSampler(dev.index or 0) as clk:
+        srv = ScatterServer(beds, hbm_budget=80 << 30)
+        served = srv.serve(poisson_stream(args.serve_rate, args.serve_seconds, beds, 0.7, seed=2026))
+        plain = PlainServer(beds).serve(poisson_stream(args.serve_rate, args.serve_seconds, beds, 0.7,
+                                                       seed=2026))
+    s, p = latency_summary(served, beds), latency_summary(plain, beds)
+    offered = sum(beds[r.bed].units for r in served) / args.serve_seconds
+    # error of served results against the FP64 oracle, for the first small requests
+    errs = []
+    for r in [r for r in served if not beds[r.bed].large][:args.serve_check]:
+        bed, pr = beds[r.bed], problems[r.bed]
+        act = request_activity(bed, r.seed).cpu().numpy().reshape(bed.shape, order="F")
+        ref = O.sss_compact(act, pr.attenuation, pr.image_size, pr.scanner.geometry, pr.scanner.normals,
+                            pr.scanner.detector_size_mm, att, pr.energy_resolution, pr.energy_threshold,
+                            pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step, pr.tof_resolution,
+                            pr.tof_range, pr.nr_bins, nthreads=cpu_threads())
+        got = leg_pair_to_compact(r.out.cpu().numpy(), pr.nr_rings_used, pr.nr_detectors_used)
+        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    return {"workload": f"Poisson {args.serve_rate:g} req/s for {args.serve_seconds:g} s (seed 2026), "
+                        "70% small / 30% large over 8 resident beds",
+            "beds": [{"name": pr.name, "volume": list(pr.grid), "rings": pr.nr_rings_used,
+                      "crystals": pr.nr_detectors_used, "bins": pr.nr_bins, "units": b.units}
+                     for pr, b in zip(problems, beds)],
+            "offered_units_per_s": offered, "hbm_budget_gb": 80, "served": s, "plain": p,
+            "p99_speedup": p["p99_ms"] / s["p99_ms"], "throughput_ratio": s["units_per_s"] / p["units_per_s"],
+            "server_stats": dict(srv.stats), "rel_l2_vs_fp64_small": errs, "clocks": clk.summary()}
+
+
 def _sfu_peak(clocks):
     """SFU 2^x peak measured in this process (sss_probe_ex2_rate: every SM
     issuing independent ex2 chains), else 152 SMs x 16 results/clk x max clock."""
@@ -580,6 +634,11 @@ def main():
                     help="scatter points of the FP64 oracle sample in the precision study")
     ap.add_argument("--precision-steps", type=int, default=1)
     ap.add_argument("--precision-warmup", type=int, default=1)
+    ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="length of the arrival window")
+    ap.add_argument("--serve-check", type=int, default=2,
+                    help="served small requests checked against the FP64 oracle")
     ap.add_argument("--max-points", type=int, default=None,
                     help="limit each step to the first scatter points (profiling runs only)")
     args = ap.parse_args()

@@ -193,7 +193,7 @@ class ScatterServer:
         running_small: list[_Batch] = []
         current_large: _Batch | None = None
         in_flight: list[_Batch] = []
-        retired: list[_Batch] = []
+        retired: list[torch.Tensor] = []  # status words of finished batches
         queue: collections.deque = collections.deque()
         start = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(self.dev)
@@ -213,7 +213,11 @@ class ScatterServer:
                     for r in b.reqs:
                         r.done = t_done
                     in_flight.remove(b)
-                    retired.append(b)
+                    retired.append(b.plan.status)
+                    b.plan.close()  # the workspace goes back to the allocator
+                    b.plan = None
+                    if current_large is b:
+                        current_large = None
                     finished += len(b.reqs)
             while queue and queue[0].query():
                 queue.popleft()
@@ -251,9 +255,8 @@ class ScatterServer:
             if i < len(reqs) or in_flight:
                 time.sleep(5e-5)
         torch.cuda.synchronize(self.dev)
-        for b in retired:
-            _lib.check_status(int(b.plan.status.item()))
-            b.plan.close()
+        for status in retired:
+            _lib.check_status(int(status.item()))
         return reqs
 
 
