@@ -198,8 +198,8 @@ def config3_instances(count: int = 64, seed: int = 0):
     faces ((x+1)*FOV/n - FOV/2, SingleScatterSimulationTOF.py:388, :394); a
     leg from such a point to a crystal on an axis (x or y exactly 0 or
     +-41 cm) can pass exactly through voxel corners, where the reference's
-    traversal runs past Nx+Ny+Nz voxels and raises IndexError (seen on several
-    of these volumes with the unrotated ring).  No crystal sits on an axis
+    traversal runs past Nx+Ny+Nz voxels and raises IndexError (on 15 of these 64
+    volumes with the unrotated ring).  No crystal sits on an axis
     after the half-crystal rotation."""
     rng = np.random.default_rng(seed)
     scanner = ring_scanner(phase=0.5)
