@@ -209,6 +209,18 @@ int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float *ma
                   int32_t nr, int32_t nd, const double *geometry, const int16_t *lor,
                   const int16_t *sino_index, int32_t af, uint8_t *out, int32_t *status, void *stream);
 
+/* Tail mask with span.  Replaces MaskGeneratorMashing / MaskDetectorsMashing
+ * (Python/openSSS/TailsMask.py:230-377): the LORs are those of the npairs ring
+ * pairs pairs[p] = (Ring1, Ring2, slice) (device int32 [npairs][3]) on the
+ * expanded geometry (nr = 2*rings - 1, Python/openSSS/Geometry.py:161-197),
+ * crystal pairs as in sss_tail_mask; LOR (p, d1, d2) marks
+ * out[cell*nslices + slice].  out (device uint8 [(nd+1)*(nd/2)][nslices])
+ * must be zeroed by the caller. */
+int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const float *map, int32_t use_activity,
+                        int32_t nr, int32_t nd, const double *geometry, const int16_t *lor, const int32_t *pairs,
+                        int32_t npairs, int32_t nslices, int32_t af, uint8_t *out, int32_t *status,
+                        void *stream);
+
 /* Back-projection scale fit.  Replaces BackProjectionScatterRandFit
  * (Python/openSSS/BackProjection.py:115-215) and BackProjection (:31-113).
  * The LOR (Ring1, d1, Ring2, d2) on the af lattice reads slice
@@ -226,6 +238,20 @@ int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t n
                         const uint8_t *mask_u8, const float *scatters, const int64_t *scat_cell,
                         const int64_t *scat_ring, int32_t scat_clamp, float *images, double *sums,
                         float *scale, int32_t *status, void *stream);
+
+/* Fit with span.  Replaces BackProjectionScatterRandFitMashing /
+ * BackProjectionMashing (Python/openSSS/BackProjection.py:217-393): LORs of
+ * the ring pairs pairs[p] = (Ring1, Ring2, slice) on the expanded geometry,
+ * reading slice `slice` of the [cell][nslices] sinograms.  length_weighted:
+ * each voxel gets value * length / sum(lengths) (:294-297) instead of
+ * value / voxels.  Other arguments and outputs as sss_backproject_fit. */
+int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
+                              const double *geometry, const int16_t *lor, const int32_t *pairs, int32_t npairs,
+                              int32_t nslices, int32_t length_weighted, int32_t af, const float *prompts,
+                              const float *randoms, const float *mask_f32, const uint8_t *mask_u8,
+                              const float *scatters, const int64_t *scat_cell, const int64_t *scat_ring,
+                              int32_t scat_clamp, float *images, double *sums, float *scale, int32_t *status,
+                              void *stream);
 
 /* ---------------------------------------------------------------------------
  * Stage timing (no reference counterpart: instrumentation for benchmarks).

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, geometry
 from .engine import as_device
 
 
@@ -23,16 +23,23 @@ def _ptr(t):
 
 def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize, ImageSize, Geometry,
                SinogramCoordinates, SinogramOrder, AccelerationFactor, scat_clamp=False,
-               device="cuda", return_images=False):
+               device="cuda", return_images=False, span: bool = False):
     """All sinogram arguments are CUDA tensors [cell, slice] (float32; mask
-    float32, or uint8 meaning mask >= 1).  Returns the scale as a float."""
+    float32, or uint8 meaning mask >= 1).  Returns the scale as a float.
+    With ``span``, ``Geometry`` is the expanded geometry, ``SinogramOrder`` the
+    mashed SinogramIndex (float [n, 2]) and the back-projection is
+    length-weighted (BackProjection.py:217-393)."""
     geom = np.asarray(Geometry, dtype=np.float64)
     nr, nd = geom.shape[:2]
     grid = np.ascontiguousarray(np.asarray(GridSize).reshape(-1)[:3], dtype=np.int32)
     bounds = np.ascontiguousarray(np.asarray(ImageSize, dtype=np.float64).reshape(-1)[:6])
     g = as_device(geom, torch.float64, device)
     lor = as_device(np.asarray(SinogramCoordinates, dtype=np.int16), torch.int16, device)
-    order = as_device(np.asarray(SinogramOrder, dtype=np.int16)[:nr, :nr], torch.int16, device)
+    if span:
+        pairs_np = geometry.span_ring_pairs(SinogramOrder)
+        pairs = as_device(pairs_np, torch.int32, device)
+    else:
+        order = as_device(np.asarray(SinogramOrder, dtype=np.int16)[:nr, :nr], torch.int16, device)
     cs = as_device(scat_cell, torch.int64, device)
     rs = as_device(scat_ring, torch.int64, device)
     nvox = int(np.prod(grid))
@@ -43,11 +50,19 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
     m_u8 = mask if mask.dtype == torch.uint8 else None
     m_f = None if m_u8 is not None else mask
     st = torch.cuda.current_stream(device)
-    _lib.check(_lib.lib().sss_backproject_fit(
-        grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), nr, nd, _ptr(g), _ptr(lor),
-        _ptr(order), int(AccelerationFactor or 1), _ptr(prompts), _ptr(randoms), _ptr(m_f), _ptr(m_u8),
-        _ptr(scatters), _ptr(cs), _ptr(rs), int(bool(scat_clamp)), _ptr(images), _ptr(sums),
-        _ptr(scale), _ptr(status), C.c_void_p(st.cuda_stream)))
+    if span:
+        n = pairs_np.shape[0]
+        _lib.check(_lib.lib().sss_backproject_fit_pairs(
+            grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), nr, nd, _ptr(g), _ptr(lor),
+            _ptr(pairs), n, n, 1, int(AccelerationFactor or 1), _ptr(prompts), _ptr(randoms), _ptr(m_f),
+            _ptr(m_u8), _ptr(scatters), _ptr(cs), _ptr(rs), int(bool(scat_clamp)), _ptr(images), _ptr(sums),
+            _ptr(scale), _ptr(status), C.c_void_p(st.cuda_stream)))
+    else:
+        _lib.check(_lib.lib().sss_backproject_fit(
+            grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), nr, nd, _ptr(g), _ptr(lor),
+            _ptr(order), int(AccelerationFactor or 1), _ptr(prompts), _ptr(randoms), _ptr(m_f), _ptr(m_u8),
+            _ptr(scatters), _ptr(cs), _ptr(rs), int(bool(scat_clamp)), _ptr(images), _ptr(sums),
+            _ptr(scale), _ptr(status), C.c_void_p(st.cuda_stream)))
     st.synchronize()
     _lib.check_status(int(status.item()))
     if return_images:
@@ -74,4 +89,28 @@ def BackProjectionScatterRandFit(PromptSinogram, ScatterSinogram, RandomSinogram
     s = fit_device(dev(PromptSinogram), dev(RandomSinogram), dev(MaskSinogram), dev(ScatterSinogram),
                    cell, ring, GridSize, ImageSize, Geometry, SinogramCoordinates, SinogramOrder,
                    AccelerationFactor, device=device)
+    return np.array([s], dtype=np.float32)
+
+
+def BackProjectionScatterRandFitMashing(PromptSinogram, ScatterSinogram, RandomSinogram, MaskSinogram,
+                                        GridSize, ImageSize, Geometry, SinogramCoordinates, AccelerationFactor,
+                                        MashedSinogramIndices, device="cuda"):
+    """Scale fit with span (``BackProjection.py:302-393``): ``Geometry`` is
+    the expanded geometry; sinograms are (ND+1, ND//2, mashed sinograms)."""
+    if not torch.cuda.is_available():
+        raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
+    geom = np.asarray(Geometry)
+    nd = geom.shape[1]
+    nsl = np.asarray(MashedSinogramIndices).shape[0]
+    shp = ((nd + 1) * (nd // 2), nsl)
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(shp))
+                                ).to(device)
+
+    cell = np.arange(shp[0], dtype=np.int64) * nsl
+    ring = np.arange(nsl, dtype=np.int64)
+    s = fit_device(dev(PromptSinogram), dev(RandomSinogram), dev(MaskSinogram), dev(ScatterSinogram),
+                   cell, ring, GridSize, ImageSize, Geometry, SinogramCoordinates, MashedSinogramIndices,
+                   AccelerationFactor, device=device, span=True)
     return np.array([s], dtype=np.float32)

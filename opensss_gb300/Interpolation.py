@@ -46,18 +46,25 @@ def upsample_device(sampled: torch.Tensor, tables, nbins: int, ncell: int, nslic
 
 def InterpolateScatters(Scatters, NrRings, NrRingsUsed, NrDetectors, NrDetectorsUsed,
                         SinogramCoordinates, SinogramIndex, SavePath, SpanFlag, device="cuda"):
-    """Upsample the sampled scatter sinogram (see the module docstring)."""
-    if SpanFlag:
-        raise NotImplementedError("the span (axial mashing) upsampling is not part of this engine yet")
+    """Upsample the sampled scatter sinogram (see the module docstring).
+    With ``SpanFlag`` the slices are the mashed sinograms of SinogramIndex
+    (float [n, 2], mean rings, from SinogramLUT), as InterpolateAllBinsSpan
+    (Interpolation.py:321-399) evaluates them."""
     if not torch.cuda.is_available():
         raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
     t0 = time.time()
     nd, nr = int(NrDetectors), int(NrRings)
     nbins = Scatters.shape[0]
     dense = torch.from_numpy(np.ascontiguousarray(Scatters, dtype=np.float32)).to(device)
-    tables = geometry.upsample_tables(SinogramCoordinates, np.asarray(SinogramIndex)[:nr, :nr],
-                                      int(NrRingsUsed), int(NrDetectorsUsed), "dense")
-    ncell, nslices = (nd + 1) * (nd // 2), nr * nr
+    if SpanFlag:
+        tables = geometry.span_upsample_tables(SinogramCoordinates, SinogramIndex, nr, int(NrRingsUsed),
+                                               int(NrDetectorsUsed), "dense")
+        nslices = int(np.asarray(SinogramIndex).shape[0])
+    else:
+        tables = geometry.upsample_tables(SinogramCoordinates, np.asarray(SinogramIndex)[:nr, :nr],
+                                          int(NrRingsUsed), int(NrDetectorsUsed), "dense")
+        nslices = nr * nr
+    ncell = (nd + 1) * (nd // 2)
     if SavePath:
         buf = torch.empty((ncell, nslices), dtype=torch.float32, device=device)
         for b in range(nbins):

@@ -3,7 +3,9 @@
 Same arguments and result as the reference (``Python/openSSS/TailsMask.py:28-82,165-228``):
 uint8 ``(ND+1, ND//2, NR**2)``, 1 where the LOR's attenuation correction
 factor is exactly 1 (or, with ``UseAttenuation=False``, where it sees no
-activity), for the LORs on the AccelerationFactor lattice.
+activity), for the LORs on the AccelerationFactor lattice.  With span
+(``MaskGeneratorMashing``, :230-377) the slices are the mashed sinograms,
+each traced once at its mean ring pair on the expanded geometry.
 """
 
 from __future__ import annotations
@@ -15,7 +17,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, geometry
 from .engine import as_device, fortran_flat
 
 
@@ -24,8 +26,10 @@ def _ptr(t):
 
 
 def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramIndex,
-                     AccelerationFactor=1, use_activity=False, device="cuda") -> torch.Tensor:
-    """uint8 CUDA tensor [(ND+1)*(ND//2), NR*NR]."""
+                     AccelerationFactor=1, use_activity=False, device="cuda", span: bool = False) -> torch.Tensor:
+    """uint8 CUDA tensor [(ND+1)*(ND//2), slices]: NR*NR slices, or with
+    ``span`` the mashed sinograms of ``SinogramIndex`` (float [n, 2], from
+    SinogramLUT) on the expanded ``Geometry``."""
     if not torch.cuda.is_available():
         raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
     geom = np.asarray(Geometry, dtype=np.float64)
@@ -34,17 +38,27 @@ def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramI
     vol = fortran_flat(volume, device)
     g = as_device(geom, torch.float64, device)
     lor = as_device(np.asarray(SinogramCoordinates, dtype=np.int16), torch.int16, device)
-    si = as_device(np.asarray(SinogramIndex, dtype=np.int16)[:nr, :nr], torch.int16, device)
-    out = torch.zeros(((nd + 1) * (nd // 2), nr * nr), dtype=torch.uint8, device=device)
     status = torch.zeros(1, dtype=torch.int32, device=device)
     grid = np.array(shape, dtype=np.int32)
     bounds = np.ascontiguousarray(np.asarray(ImageSize, dtype=np.float64).reshape(-1)[:6])
     st = torch.cuda.current_stream(device)
-    _lib.check(_lib.lib().sss_tail_mask(grid.ctypes.data_as(C.c_void_p),
-                                        bounds.ctypes.data_as(C.c_void_p), _ptr(vol),
-                                        int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(si),
-                                        int(AccelerationFactor or 1), _ptr(out), _ptr(status),
-                                        C.c_void_p(st.cuda_stream)))
+    if span:
+        pairs_np = geometry.span_ring_pairs(SinogramIndex)
+        nslices = pairs_np.shape[0]
+        pairs = as_device(pairs_np, torch.int32, device)
+        out = torch.zeros(((nd + 1) * (nd // 2), nslices), dtype=torch.uint8, device=device)
+        _lib.check(_lib.lib().sss_tail_mask_pairs(
+            grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), _ptr(vol),
+            int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(pairs), nslices, nslices,
+            int(AccelerationFactor or 1), _ptr(out), _ptr(status), C.c_void_p(st.cuda_stream)))
+    else:
+        si = as_device(np.asarray(SinogramIndex, dtype=np.int16)[:nr, :nr], torch.int16, device)
+        out = torch.zeros(((nd + 1) * (nd // 2), nr * nr), dtype=torch.uint8, device=device)
+        _lib.check(_lib.lib().sss_tail_mask(grid.ctypes.data_as(C.c_void_p),
+                                            bounds.ctypes.data_as(C.c_void_p), _ptr(vol),
+                                            int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(si),
+                                            int(AccelerationFactor or 1), _ptr(out), _ptr(status),
+                                            C.c_void_p(st.cuda_stream)))
     st.synchronize()
     _lib.check_status(int(status.item()))
     return out
@@ -62,15 +76,33 @@ def MaskGenerator(ActivityMap, AttenuationMap, ImageSize, Geometry, SinogramCoor
     return m.cpu().numpy().reshape(nd + 1, nd // 2, nr * nr)
 
 
+def MaskGeneratorMashing(ActivityMap, AttenuationMap, ImageSize, Geometry, SinogramCoordinates,
+                         MashedSinogramIndices, UseAttenuation, AccelerationFactor=1, device="cuda"):
+    """Tail mask with span (``TailsMask.py:311-377``): ``Geometry`` is the
+    expanded geometry and ``MashedSinogramIndices`` the mashed SinogramIndex
+    of SinogramLUT.  uint8 (ND+1, ND//2, mashed sinograms)."""
+    t0 = time.time()
+    geom = np.asarray(Geometry)
+    nd = geom.shape[1]
+    vol = AttenuationMap if UseAttenuation else ActivityMap
+    m = tail_mask_device(vol, ImageSize, geom, SinogramCoordinates, MashedSinogramIndices,
+                         AccelerationFactor, use_activity=not UseAttenuation, device=device, span=True)
+    print("Time for Generate Tail Mask:", time.time() - t0, "seconds")
+    return m.cpu().numpy().reshape(nd + 1, nd // 2, -1)
+
+
 def GenerateTailsMask(SavePath, ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
                       extendedGeometry, LORCoordinates, SinogramIndex, AccelerationFactor,
                       UseAttenuation=True, Overwrite=False, device="cuda"):
     path = os.path.join(SavePath, "AttenuationMask.npy")
     if os.path.isfile(path) and not Overwrite:
         return np.load(path)
-    if np.asarray(extendedGeometry).shape[0] != 0:
-        raise NotImplementedError("the span (axial mashing) tail mask is not part of this engine yet")
-    mask = MaskGenerator(ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
-                         LORCoordinates, SinogramIndex, UseAttenuation, AccelerationFactor, device)
+    if np.asarray(extendedGeometry).shape[0] != 0:  # span (TailsMask.py:70-74)
+        mask = MaskGeneratorMashing(ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize,
+                                    extendedGeometry, LORCoordinates, SinogramIndex, UseAttenuation,
+                                    AccelerationFactor, device)
+    else:
+        mask = MaskGenerator(ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
+                             LORCoordinates, SinogramIndex, UseAttenuation, AccelerationFactor, device)
     np.save(path, mask)
     return mask

@@ -79,6 +79,10 @@ SIGNATURES = {
     "sss_batch_free": (None, [_P]),
     "sss_upsample": (C.c_int, [_P, _I64, _I32, _P, _I64, _P, _I32, _P, _I32, _P, _P]),
     "sss_tail_mask": (C.c_int, [_P, _P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P]),
+    "sss_tail_mask_pairs": (C.c_int, [_P, _P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _I32, _I32, _P, _P,
+                                      _P]),
+    "sss_backproject_fit_pairs": (C.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _I32, _I32, _I32, _I32, _P, _P,
+                                            _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P]),
     "sss_backproject_fit": (C.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _P,
                                       _P, _I32, _P, _P, _P, _P, _P]),
     "sss_set_timing": (None, [C.c_int]),

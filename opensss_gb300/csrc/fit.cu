@@ -40,6 +40,38 @@ __device__ __forceinline__ LorIndex lor_of(long long id, int nr, int na)
     return L;
 }
 
+// LOR number -> rings, crystal indices and sinogram slice.  Without a pair
+// list every ring pair (r1, r2) of the geometry is used and `slice_of`
+// ([nr][nr]) gives its slice; with one (span: the mashed sinograms on the
+// expanded geometry) the LOR's ring pair is pairs[p] = (Ring1, Ring2, slice),
+// p fastest.
+struct LorRef {
+    int r1, r2, i1, i2, slice;
+};
+
+__device__ __forceinline__ LorRef lor_ref(long long id, int nr, int na, const int16_t* slice_of,
+                                          const int32_t* pairs, int npairs)
+{
+    LorRef R;
+    if (pairs) {
+        const int p = (int)(id % npairs);
+        id /= npairs;
+        R.i2 = (int)(id % na);
+        R.i1 = (int)(id / na);
+        R.r1 = pairs[3 * p];
+        R.r2 = pairs[3 * p + 1];
+        R.slice = pairs[3 * p + 2];
+    } else {
+        const LorIndex L = lor_of(id, nr, na);
+        R.r1 = L.r1;
+        R.r2 = L.r2;
+        R.i1 = L.i1;
+        R.i2 = L.i2;
+        R.slice = slice_of[L.r1 * nr + L.r2];
+    }
+    return R;
+}
+
 __device__ __forceinline__ void lor_line(const double* geom, int nd, int r1, int d1, int r2, int d2,
                                          double* lc)
 {
@@ -93,6 +125,8 @@ struct MaskParams {
     const double* geom;
     const int16_t* lor;
     const int16_t* sino;
+    const int32_t* pairs;       // span: [npairs][3] (Ring1, Ring2, slice), else null
+    int npairs, nslices;
     int nr, nd, na, af, cap;
     uint8_t* out;
     int32_t* status;
@@ -100,12 +134,12 @@ struct MaskParams {
 
 __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
 {
-    const long long n = (long long)P.nr * P.nr * P.na * P.na;
+    const long long n = (long long)(P.pairs ? P.npairs : P.nr * P.nr) * P.na * P.na;
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n) return;
-    const LorIndex L = lor_of(id, P.nr, P.na);
+    const LorRef L = lor_ref(id, P.nr, P.na, P.sino, P.pairs, P.npairs);
     const int d1 = L.i1 * P.af, d2 = L.i2 * P.af;
-    if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // TailsMask.py:129
+    if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // TailsMask.py:129, :273
     double lc[6];
     lor_line(P.geom, P.nd, L.r1, d1, L.r2, d2, lc);
     double acf = 1.0;  // a miss gives Attenuation = 1 (:146-148)
@@ -132,9 +166,8 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
             raise_error(P.status, kErrCapacity);
             return;
         }
-        const long long nsino = (long long)P.nr * P.nr;
         const long long cell = (long long)rad * (P.nd / 2) + ang;
-        P.out[cell * nsino + P.sino[L.r1 * P.nr + L.r2]] = 1;
+        P.out[cell * P.nslices + L.slice] = 1;
     }
 }
 
@@ -146,6 +179,9 @@ struct FitParams {
     const double* geom;
     const int16_t* lor;
     const int16_t* order;       // [nr][nr]: slice read by the LOR (Ring1, Ring2) (:157-176)
+    const int32_t* pairs;       // span: [npairs][3] (Ring1, Ring2, slice), else null
+    int npairs, nslices;
+    int length_weighted;        // span: value * length / sum(lengths) (:294-297), else value / n
     int nr, nd, na, af, cap;
     const float* prompts;       // [cell][slice]
     const float* randoms;
@@ -161,21 +197,21 @@ struct FitParams {
 
 __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
 {
-    const long long n = (long long)P.nr * P.nr * P.na * P.na;
+    const long long n = (long long)(P.pairs ? P.npairs : P.nr * P.nr) * P.na * P.na;
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= n) return;
-    const LorIndex L = lor_of(id, P.nr, P.na);
+    const LorRef L = lor_ref(id, P.nr, P.na, P.order, P.pairs, P.npairs);
     const int d1 = L.i1 * P.af, d2 = L.i2 * P.af;
-    if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // BackProjection.py:88
+    if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // BackProjection.py:88, :278
     const int ang = P.lor[2 * ((long long)d1 * P.nd + d2)];
     const int rad = P.lor[2 * ((long long)d1 * P.nd + d2) + 1];
-    const int slice = P.order[L.r1 * P.nr + L.r2];
-    if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2 || slice < 0 || slice >= P.nr * P.nr) {
+    const int slice = L.slice;
+    if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2 || slice < 0 || slice >= P.nslices) {
         raise_error(P.status, kErrCapacity);  // unset coordinates or a bad slice order
         return;
     }
     const long long cell = (long long)rad * (P.nd / 2) + ang;
-    const long long c = cell * ((long long)P.nr * P.nr) + slice;
+    const long long c = cell * (long long)P.nslices + slice;
     const float m = P.mask_u8 ? (P.mask_u8[c] >= 1 ? 1.f : 0.f) : P.mask_f32[c];
     float sv = P.scat[P.scat_cell[cell] + P.scat_ring[slice]];
     if (P.scat_clamp) sv = fmaxf(sv, 0.f);
@@ -187,8 +223,12 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     Ray r;
     if (!ray_setup(P.g, lc, 1e-20, r)) return;
     // first pass: voxel count (the reference divides by len(Lengths), :108-110)
+    // and, for the length-weighted back-projection, the summed length (:294-297)
     Ray r2 = r;
-    int n_vox = ray_walk(P.g, r2, P.cap, [](int, int64_t, double, double) {});
+    double total = 0.0;
+    int n_vox = ray_walk(P.g, r2, P.cap, [&](int, int64_t, double t0, double t1) {
+        if (P.length_weighted) total = add64(total, ref_length(r2, t0, t1));
+    });
     if (n_vox < 0) {
         raise_error(P.status, kErrOverrun);
         return;
@@ -197,15 +237,22 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     const float fn = (float)n_vox;
     const float ap = pv / fn, as = s / fn, ar = rv / fn;
     bool bad = false;
-    ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double, double) {
+    ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
         const long long v = lin - 1;
         if (v < 0 || v >= P.nvox) {
             bad = true;
             return;
         }
-        atomicAdd(P.img + v, ap);
-        atomicAdd(P.img + P.nvox + v, as);
-        atomicAdd(P.img + 2 * P.nvox + v, ar);
+        if (P.length_weighted) {
+            const double w = div64(ref_length(r, t0, t1), total);
+            atomicAdd(P.img + v, (float)mul64((double)pv, w));
+            atomicAdd(P.img + P.nvox + v, (float)mul64((double)s, w));
+            atomicAdd(P.img + 2 * P.nvox + v, (float)mul64((double)rv, w));
+        } else {
+            atomicAdd(P.img + v, ap);
+            atomicAdd(P.img + P.nvox + v, as);
+            atomicAdd(P.img + 2 * P.nvox + v, ar);
+        }
         atomicAdd(P.img + 3 * P.nvox + v, 1.0f);
     });
     if (bad) raise_error(P.status, kErrVoxel);
@@ -291,16 +338,17 @@ extern "C" int sss_upsample(const float* sampled, int64_t bin_stride, int32_t nb
     return sss_check_launch("upsample_kernel");
 }
 
-extern "C" int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float* map,
-                             int32_t use_activity, int32_t nr, int32_t nd, const double* geometry,
-                             const int16_t* lor, const int16_t* sino_index, int32_t af, uint8_t* out,
-                             int32_t* status, void* stream)
+namespace {
+
+int tail_mask(const int32_t grid[3], const double bounds[6], const float* map, int32_t use_activity, int32_t nr,
+              int32_t nd, const double* geometry, const int16_t* lor, const int16_t* sino_index,
+              const int32_t* pairs, int32_t npairs, int32_t nslices, int32_t af, uint8_t* out, int32_t* status,
+              void* stream)
 {
-    int rc = check_grid(grid, bounds, "sss_tail_mask");
-    if (rc) return rc;
-    if (!map || !geometry || !lor || !sino_index || !out || nr < 1 || nd < 2 || af < 1)
-        return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask: bad argument");
     MaskParams P;
+    P.pairs = pairs;
+    P.npairs = npairs;
+    P.nslices = pairs ? nslices : nr * nr;
     P.g = make_grid(grid, bounds);
     P.mu = map;
     P.use_activity = use_activity;
@@ -315,28 +363,59 @@ extern "C" int sss_tail_mask(const int32_t grid[3], const double bounds[6], cons
     P.cap = grid[0] + grid[1] + grid[2];
     P.out = out;
     P.status = status;
-    const long long n = (long long)nr * nr * P.na * P.na;
+    const long long n = (long long)(pairs ? npairs : nr * nr) * P.na * P.na;
+    if (n == 0) return SSS_OK;
     mask_kernel<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(P);
     return sss_check_launch("mask_kernel");
 }
 
-extern "C" int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr,
-                                   int32_t nd, const double* geometry, const int16_t* lor,
-                                   const int16_t* sino_order, int32_t af, const float* prompts,
-                                   const float* randoms, const float* mask_f32,
-                                   const uint8_t* mask_u8, const float* scatters,
-                                   const int64_t* scat_cell, const int64_t* scat_ring,
-                                   int32_t scat_clamp, float* images, double* sums, float* scale,
-                                   int32_t* status, void* stream)
+}  // namespace
+
+extern "C" int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float* map,
+                             int32_t use_activity, int32_t nr, int32_t nd, const double* geometry,
+                             const int16_t* lor, const int16_t* sino_index, int32_t af, uint8_t* out,
+                             int32_t* status, void* stream)
 {
-    int rc = check_grid(grid, bounds, "sss_backproject_fit");
+    int rc = check_grid(grid, bounds, "sss_tail_mask");
     if (rc) return rc;
-    if (!geometry || !lor || !sino_order || !prompts || !randoms || (!mask_f32 && !mask_u8) ||
-        !scatters || !scat_cell || !scat_ring || !images || !sums || !scale || nr < 1 || nd < 2 ||
-        af < 1)
+    if (!map || !geometry || !lor || !sino_index || !out || nr < 1 || nd < 2 || af < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask: bad argument");
+    return tail_mask(grid, bounds, map, use_activity, nr, nd, geometry, lor, sino_index, nullptr, 0, 0, af, out,
+                     status, stream);
+}
+
+extern "C" int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const float* map,
+                                   int32_t use_activity, int32_t nr, int32_t nd, const double* geometry,
+                                   const int16_t* lor, const int32_t* pairs, int32_t npairs, int32_t nslices,
+                                   int32_t af, uint8_t* out, int32_t* status, void* stream)
+{
+    int rc = check_grid(grid, bounds, "sss_tail_mask_pairs");
+    if (rc) return rc;
+    if (!map || !geometry || !lor || !pairs || !out || nr < 1 || nd < 2 || af < 1 || npairs < 0 || nslices < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask_pairs: bad argument");
+    return tail_mask(grid, bounds, map, use_activity, nr, nd, geometry, lor, nullptr, pairs, npairs, nslices, af,
+                     out, status, stream);
+}
+
+namespace {
+
+int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd, const double* geometry,
+                    const int16_t* lor, const int16_t* sino_order, const int32_t* pairs, int32_t npairs,
+                    int32_t nslices, int32_t length_weighted, int32_t af, const float* prompts,
+                    const float* randoms, const float* mask_f32, const uint8_t* mask_u8, const float* scatters,
+                    const int64_t* scat_cell, const int64_t* scat_ring, int32_t scat_clamp, float* images,
+                    double* sums, float* scale, int32_t* status, void* stream)
+{
+    int rc;
+    if (!geometry || !lor || !prompts || !randoms || (!mask_f32 && !mask_u8) || !scatters || !scat_cell ||
+        !scat_ring || !images || !sums || !scale || nr < 1 || nd < 2 || af < 1)
         return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: bad argument");
     cudaStream_t st = (cudaStream_t)stream;
     FitParams P;
+    P.pairs = pairs;
+    P.npairs = npairs;
+    P.nslices = pairs ? nslices : nr * nr;
+    P.length_weighted = length_weighted;
     P.g = make_grid(grid, bounds);
     P.nvox = (long long)grid[0] * grid[1] * grid[2];
     P.geom = geometry;
@@ -360,9 +439,11 @@ extern "C" int sss_backproject_fit(const int32_t grid[3], const double bounds[6]
     if (cudaMemsetAsync(images, 0, sizeof(float) * 4 * P.nvox, st) != cudaSuccess ||
         cudaMemsetAsync(sums, 0, 2 * sizeof(double), st) != cudaSuccess)
         return sss_set_error(SSS_ERR_CUDA, "sss_backproject_fit: memset failed");
-    const long long n = (long long)nr * nr * P.na * P.na;
-    bp_kernel<<<blocks_for(n, 128), 128, 0, st>>>(P);
-    if ((rc = sss_check_launch("bp_kernel"))) return rc;
+    const long long n = (long long)(pairs ? npairs : nr * nr) * P.na * P.na;
+    if (n > 0) {
+        bp_kernel<<<blocks_for(n, 128), 128, 0, st>>>(P);
+        if ((rc = sss_check_launch("bp_kernel"))) return rc;
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -371,4 +452,40 @@ extern "C" int sss_backproject_fit(const int32_t grid[3], const double bounds[6]
     if ((rc = sss_check_launch("fit_reduce_kernel"))) return rc;
     fit_final_kernel<<<1, 1, 0, st>>>(sums, scale);
     return sss_check_launch("fit_final_kernel");
+}
+
+}  // namespace
+
+extern "C" int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr,
+                                   int32_t nd, const double* geometry, const int16_t* lor,
+                                   const int16_t* sino_order, int32_t af, const float* prompts,
+                                   const float* randoms, const float* mask_f32,
+                                   const uint8_t* mask_u8, const float* scatters,
+                                   const int64_t* scat_cell, const int64_t* scat_ring,
+                                   int32_t scat_clamp, float* images, double* sums, float* scale,
+                                   int32_t* status, void* stream)
+{
+    int rc = check_grid(grid, bounds, "sss_backproject_fit");
+    if (rc) return rc;
+    if (!sino_order) return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: bad argument");
+    return backproject_fit(grid, bounds, nr, nd, geometry, lor, sino_order, nullptr, 0, 0, 0, af, prompts, randoms,
+                           mask_f32, mask_u8, scatters, scat_cell, scat_ring, scat_clamp, images, sums, scale,
+                           status, stream);
+}
+
+extern "C" int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
+                                         const double* geometry, const int16_t* lor, const int32_t* pairs,
+                                         int32_t npairs, int32_t nslices, int32_t length_weighted, int32_t af,
+                                         const float* prompts, const float* randoms, const float* mask_f32,
+                                         const uint8_t* mask_u8, const float* scatters, const int64_t* scat_cell,
+                                         const int64_t* scat_ring, int32_t scat_clamp, float* images,
+                                         double* sums, float* scale, int32_t* status, void* stream)
+{
+    int rc = check_grid(grid, bounds, "sss_backproject_fit_pairs");
+    if (rc) return rc;
+    if (!pairs || npairs < 0 || nslices < 1)
+        return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit_pairs: bad argument");
+    return backproject_fit(grid, bounds, nr, nd, geometry, lor, nullptr, pairs, npairs, nslices, length_weighted,
+                           af, prompts, randoms, mask_f32, mask_u8, scatters, scat_cell, scat_ring, scat_clamp,
+                           images, sums, scale, status, stream);
 }

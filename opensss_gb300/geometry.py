@@ -104,21 +104,28 @@ def upsample_source(lor: np.ndarray, detectors: np.ndarray) -> np.ndarray:
     return _upsample_source_cached(lor.tobytes(), nd, tuple(int(d) for d in detectors))
 
 
+def nearest_grid_index(x, grid: np.ndarray) -> np.ndarray:
+    """RegularGridInterpolator 'nearest' along one axis (SciPy's published
+    rule): interval i with grid[i] <= x < grid[i+1] (clamped to the first and
+    last interval), then i if (x - grid[i]) / (grid[i+1] - grid[i]) <= 0.5
+    else i + 1; -1 where x lies outside [grid[0], grid[-1]] (the reference's
+    fill_value=0)."""
+    g = np.asarray(grid, dtype=np.float64)
+    x = np.atleast_1d(np.asarray(x, dtype=np.float64))
+    if len(g) == 1:
+        return np.where(x == g[0], 0, -1).astype(np.int32)
+    i = np.clip(np.searchsorted(g, x, side="right") - 1, 0, len(g) - 2)
+    frac = (x - g[i]) / (g[i + 1] - g[i])
+    out = np.where(frac <= 0.5, i, i + 1)
+    out[(x < g[0]) | (x > g[-1])] = -1
+    return out.astype(np.int32)
+
+
 def ring_nearest(nr_rings: int, rings: np.ndarray) -> np.ndarray:
     """Index of the sampled ring each ring copies from: RegularGridInterpolator
     'nearest' over the sampled ring numbers, ties to the lower ring
     (Interpolation.py:256)."""
-    rings = np.asarray(rings, dtype=np.float64)
-    out = np.zeros(nr_rings, dtype=np.int32)
-    for r in range(nr_rings):
-        i = int(np.searchsorted(rings, r, side="right") - 1)
-        i = min(max(i, 0), len(rings) - 2) if len(rings) > 1 else 0
-        if len(rings) == 1:
-            out[r] = 0
-            continue
-        frac = (r - rings[i]) / (rings[i + 1] - rings[i])
-        out[r] = i if frac <= 0.5 else i + 1
-    return out
+    return nearest_grid_index(np.arange(nr_rings), rings)
 
 
 def slice_rings(sino_index: np.ndarray) -> np.ndarray:
@@ -179,6 +186,149 @@ def upsample_tables(lor, sino_index, nru: int, ndu: int, layout: str = "dense"):
     inv = slice_rings(sino_index)
     # slice (r1, r2) copies the sampled pair (nearest(r1), nearest(r2)) (:251-310)
     ri1, ri2 = rmap[inv[:, 0]], rmap[inv[:, 1]]
+    if layout == "dense":
+        rad = lor[det[a], det[b], 1].astype(np.int64)
+        ang = lor[det[a], det[b], 0].astype(np.int64)
+        cell_src = (rad * (nd // 2) + ang) * (nru * nru)
+        ring_src = ri1 * nru + ri2
+        stride = (nd + 1) * (nd // 2) * nru * nru
+    elif layout == "legpair":
+        nl = nru * ndu
+        lo, hi = np.minimum(a, b), np.maximum(a, b)
+        cell_src = lo * nru * nl + hi * nru
+        ring_src = ri1 * nl + ri2
+        stride = nl * nl
+    else:
+        raise ValueError(layout)
+    return UpsampleTables(np.ascontiguousarray(cell_src.reshape(-1), dtype=np.int64),
+                          np.ascontiguousarray(ring_src, dtype=np.int64), int(stride))
+
+
+# ---------------------------------------------------------------- span / mash
+
+
+def SinogramLUT(NrRings: int, AxialMashing: int, MaxRingDifference: int | None = None):
+    """Axial mashing (span) tables, same outputs as the reference
+    (``Python/openSSS/DataReduction.py:102-172``): ``(SinogramIndex float32
+    [n, 2] = mean (Ring2, Ring1) of each mashed sinogram, RingLUT bool
+    [2NR-1, 2NR-1], LookUpTable int16 [NR, NR] = mashed sinogram of each ring
+    pair or -1, SinogramCounts float32 = ring pairs per mashed sinogram)``.
+
+    A ring pair closer than (span+1)/2 goes to sinogram Ring1 + Ring2 - 1 (the
+    sinograms of ring sum); farther pairs go to the segment of their ring
+    difference, segments of `span` differences each, alternating positive
+    and negative.  The reference's own sinogram count is kept, so ring counts
+    it cannot place raise IndexError here too."""
+    nr, span = int(NrRings), int(AxialMashing)
+    half = (span + 1) / 2
+    nseg = int(np.round(nr / span))
+    n = int(nr * 2 - 1 + np.sum(4 * (nr - half - span * (np.arange(1, nseg + 1) - 1)) - 2))
+    index = np.zeros((n, 2), dtype=np.float32)
+    counts = np.zeros(n, dtype=np.float32)
+    lut = np.full((nr, nr), -1, dtype=np.int16)
+    for r1 in range(1, nr + 1):
+        for r2 in range(1, nr + 1):
+            diff = r2 - r1
+            if MaxRingDifference is not None and abs(diff) > MaxRingDifference:
+                continue
+            if abs(diff) < half:
+                sino = r1 + r2 - 1
+            else:
+                seg = int(np.floor((abs(diff) - half) / span)) + 1
+                # first sinogram of the segment: all lower segments, both signs,
+                # and the negative half of this one for a positive difference
+                pos = 2 * nr - 1
+                last = seg + 1 if diff > 0 else seg
+                for k in range(1, last):
+                    width = (nr - half - span * (k - 1)) * 2 - 1
+                    pos += width * (1 if (k == last - 1 and diff > 0) else 2)
+                sino = (r1 + r2 - 1) - seg * span + (span - 1) / 2 + pos
+            j = int(sino - 1)
+            if j >= n:
+                raise IndexError(f"index {j} is out of bounds for axis 0 with size {n}")
+            index[j, 0] += r2 - 1
+            index[j, 1] += r1 - 1
+            counts[j] += 1
+            lut[r1 - 1, r2 - 1] = j
+    index[:, 0] /= counts + np.float32(1e-8)
+    index[:, 1] /= counts + np.float32(1e-8)
+    index = index[counts != 0, :]
+    ring_lut = np.zeros((nr * 2 - 1, nr * 2 - 1), dtype=bool)
+    for a, b in span_ring_pairs(index)[:, :2]:
+        ring_lut[a, b] = True
+    return index, ring_lut, lut, counts
+
+
+def span_ring_pairs(SinogramIndex) -> np.ndarray:
+    """int32 [n, 3] = (Ring1, Ring2, slice) of each mashed sinogram on the
+    expanded (2NR-1)-ring geometry: int(2 * mean ring) as the reference
+    computes it in float32 (TailsMask.py:370, BackProjection.py:373)."""
+    si = np.asarray(SinogramIndex, dtype=np.float32)
+    two = np.float32(2)
+    out = np.zeros((si.shape[0], 3), dtype=np.int32)
+    out[:, 0] = (si[:, 0] * two).astype(np.int64)
+    out[:, 1] = (si[:, 1] * two).astype(np.int64)
+    out[:, 2] = np.arange(si.shape[0])
+    return out
+
+
+def expandRings(Geometry, NormalVectors):
+    """Geometry with a virtual ring half-way between neighbouring rings (2NR-1
+    rings), and every ring's normals set to ring 0's, as the reference does
+    (``Python/openSSS/Geometry.py:161-197``)."""
+    g = np.asarray(Geometry, dtype=np.float64)
+    nv = np.asarray(NormalVectors, dtype=np.float64)
+    out = np.zeros((2 * g.shape[0] - 1,) + g.shape[1:])
+    out[0::2] = g
+    out[1::2] = (g[:-1] + g[1:]) / 2
+    normals = np.broadcast_to(nv[0], out.shape).copy()
+    return out, normals
+
+
+def mashDetectors(Geometry, NormalVectors, combineSize: int):
+    """Angular mashing: groups of ``combineSize`` neighbouring crystals become
+    one at their mean position and mean normal
+    (``Python/openSSS/Geometry.py:200-235``)."""
+    g = np.asarray(Geometry, dtype=np.float64)
+    nv = np.asarray(NormalVectors, dtype=np.float64)
+    nd = g.shape[1]
+    if nd % combineSize != 0:
+        raise Exception("Number of detectors not divisible by combineSize: ", nd, combineSize)
+    shape = (g.shape[0], nd // combineSize, combineSize, 3)
+    return np.nanmean(g.reshape(shape), axis=2), np.nanmean(nv.reshape(shape), axis=2)
+
+
+def SumLORsCounts(Geometry, LookUpTable, SinogramIndex, Mash: int, Span: int, NrSinograms: int):
+    """LORs mashed into each sinogram bin: Mash^2 per ring pair, summed over
+    the ring pairs of each slice (``Python/openSSS/DataReduction.py:174-215``).
+    A ring pair that the span table leaves out (-1) lands on the last slice,
+    as numpy's negative index does in the reference."""
+    g = np.asarray(Geometry)
+    nr, nd = g.shape[0], g.shape[1]
+    nslices = NrSinograms if Span > 1 else nr * nr
+    table = np.asarray(LookUpTable if Span > 1 else SinogramIndex)[:nr, :nr].astype(np.int64)
+    per_slice = np.bincount(np.mod(table.reshape(-1), nslices), minlength=nslices).astype(np.float32)
+    ring = np.float32(Mash ** 2)
+    return np.broadcast_to(per_slice * ring, (nd + 1, nd // 2, nslices)).astype(np.float32)
+
+
+def span_upsample_tables(lor, SinogramIndex, nr_rings: int, nru: int, ndu: int,
+                         layout: str = "dense") -> UpsampleTables:
+    """Gather tables of the span upsampling (``Interpolation.py:321-399``):
+    the (radial, angular) sources are those of the plain upsampling; mashed
+    sinogram i copies the sampled ring pair (nearest(mean Ring1), nearest(mean
+    Ring2)) of the RegularGridInterpolator over the sampled ring numbers."""
+    lor = np.asarray(lor)
+    nd = lor.shape[0]
+    det = sampled_detectors(nd, ndu)
+    rings = sampled_rings(nr_rings, nru)
+    si = np.asarray(SinogramIndex, dtype=np.float32)
+    ri2 = nearest_grid_index(si[:, 0].astype(np.float64), rings).astype(np.int64)
+    ri1 = nearest_grid_index(si[:, 1].astype(np.float64), rings).astype(np.int64)
+    if (ri1 < 0).any() or (ri2 < 0).any():
+        raise ValueError("a mashed sinogram lies outside the sampled rings")
+    src = upsample_source(lor, det).astype(np.int64)
+    a, b = np.divmod(src, ndu)
     if layout == "dense":
         rad = lor[det[a], det[b], 1].astype(np.int64)
         ang = lor[det[a], det[b], 0].astype(np.int64)

@@ -41,6 +41,8 @@ def load():
         "BackProjection",
         "Sinogram",
         "Support",
+        "DataReduction",
+        "Geometry",
     ):
         mods[name] = importlib.import_module(f"openSSS.{name}")
     return mods

@@ -351,7 +351,102 @@ def gen_fit(R):
     _save("fit", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit"]
+# ---------------------------------------------------------------- span / mash
+
+
+def _mashed(R, nr, span, mrd):
+    si, ring_lut, lut, counts = R["DataReduction"].SinogramLUT(nr, span, mrd)
+    return si, ring_lut, lut, counts
+
+
+def gen_span(R):
+    """The span (axial mashing) / mash (angular) path on small geometries:
+    SinogramLUT, expandRings, mashDetectors, SumLORsCounts,
+    InterpolateAllBinsSpan (through InterpolateScatters), MaskGeneratorMashing
+    and BackProjectionScatterRandFitMashing."""
+    D, G, I, T, B = (R[k] for k in ("DataReduction", "Geometry", "Interpolation", "TailsMask",
+                                    "BackProjection"))
+    out = {}
+    # look-up tables, including the demo's 80 rings / span 19 / MRD 79
+    for ci, (nr, span, mrd) in enumerate(((10, 3, 9), (12, 5, None), (9, 3, 4), (80, 19, 79))):
+        si, ring_lut, lut, counts = _mashed(R, nr, span, mrd)
+        out[f"lut{ci}_args"] = np.array([nr, span, -1 if mrd is None else mrd])
+        out[f"lut{ci}_index"] = si
+        out[f"lut{ci}_ringlut"] = ring_lut
+        out[f"lut{ci}_table"] = lut
+        out[f"lut{ci}_counts"] = counts
+        print(f"span lut {ci}: {si.shape[0]} mashed sinograms")
+    # geometry helpers
+    sc = _small_scan(48, 6)
+    eg, en = G.expandRings(sc.geometry, sc.normals)
+    mg, mn = G.mashDetectors(sc.geometry, sc.normals, 2)
+    out["geom_in"] = sc.geometry
+    out["normals_in"] = sc.normals
+    out["geom_expanded"] = eg
+    out["normals_expanded"] = en
+    out["geom_mashed2"] = mg
+    out["normals_mashed2"] = mn
+    si, _, lut, counts = _mashed(R, 6, 3, 5)
+    out["lorcounts"] = D.SumLORsCounts(sc.geometry, lut, si, 2, 3, counts.shape[0])
+    # upsampling with span
+    rng = np.random.default_rng(21)
+    nd, nr, nru, ndu, nb = 48, 10, 3, 8, 2
+    lc, _, _ = _sino(R, nd, nr)
+    msi, _, _, _ = _mashed(R, nr, 3, 9)
+    cmp = np.zeros((nb, nru * nru, ndu, ndu), np.float32)
+    a, b = np.triu_indices(ndu)
+    for s in range(nru * nru):
+        r1, r2 = divmod(s, nru)
+        v = rng.uniform(0.5, 2.0, size=(nb, len(a))).astype(np.float32)
+        v[:, (a == b) & (r1 == r2)] = 0
+        cmp[:, s, a, b] = v
+    dense = O.densify(cmp.astype(np.float64), lc, nd, nru, ndu)
+    with tempfile.TemporaryDirectory() as d:
+        up = I.InterpolateScatters(dense, nr, nru, nd, ndu, lc, msi, d, True)
+        per_bin = [np.load(os.path.join(d, f"SSS_mashed_bin{k}.npz"))["arr_0"] for k in range(nb)]
+    out["up_dims"] = np.array([nd, nr, nru, ndu, nb, 3, 9])
+    out["up_compact"] = cmp
+    out["up_sum"] = up
+    out["up_bins"] = np.stack(per_bin)
+    print(f"span upsample: out {up.shape}")
+    # tail mask and fit with span on the expanded geometry
+    for ci, (nd, nr, span, shape, vox, af, fgrid) in enumerate(((48, 6, 3, (12, 12, 6), 2.0, 1, (10, 10, 6)),
+                                                                 (64, 9, 3, (16, 16, 8), 1.5, 2, (12, 12, 8)))):
+        sc = _small_scan(nd, nr)
+        eg, _ = G.expandRings(sc.geometry, sc.normals)
+        act, mu, bounds = W.cylinder_phantom(shape, vox, seed=10 + ci, radius_cm=6.0)
+        lc, _, _ = _sino(R, nd, nr)
+        msi, _, _, _ = _mashed(R, nr, span, nr - 1)
+        m = T.MaskGeneratorMashing(act, mu, bounds, eg, lc, msi, True, af)
+        ma = T.MaskGeneratorMashing(act, mu, bounds, eg, lc, msi, False, af)
+        maskf = np.float32(m >= 1)
+        shp = (nd + 1, nd // 2, msi.shape[0])
+        scat = rng.uniform(0.2, 1.0, size=shp).astype(np.float32)
+        scat[rng.uniform(size=shp) < 0.1] = 0
+        rnd = np.full(shp, 0.1, np.float32)
+        prm = rng.poisson(3.0, size=shp).astype(np.float32)
+        fit_bounds = np.array([bounds[0], bounds[1], sc.geometry[0, 0, 2] - 0.5,
+                               bounds[3], bounds[4], sc.geometry[-1, 0, 2] + 0.5])
+        scale = B.BackProjectionScatterRandFitMashing(prm, scat, rnd, maskf, np.array(fgrid), fit_bounds, eg, lc,
+                                                      af, msi)
+        out[f"case{ci}_dims"] = np.array([nd, nr, span, af])
+        out[f"case{ci}_act"] = act
+        out[f"case{ci}_mu"] = mu
+        out[f"case{ci}_bounds"] = bounds
+        out[f"case{ci}_geometry"] = sc.geometry
+        out[f"case{ci}_mask"] = m
+        out[f"case{ci}_mask_activity"] = ma
+        out[f"case{ci}_grid"] = np.array(fgrid)
+        out[f"case{ci}_fit_bounds"] = fit_bounds
+        out[f"case{ci}_scatter"] = scat
+        out[f"case{ci}_randoms"] = rnd
+        out[f"case{ci}_prompts"] = prm
+        out[f"case{ci}_scale"] = np.asarray(scale, np.float32)
+        print(f"span case {ci}: {int(m.sum())} masked bins, scale {scale}")
+    _save("span", **out)
+
+
+ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit", "span"]
 
 
 def main():
@@ -381,6 +476,8 @@ def main():
         gen_mask(R)
     if "fit" in which:
         gen_fit(R)
+    if "span" in which:
+        gen_span(R)
 
 
 if __name__ == "__main__":
