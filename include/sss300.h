@@ -36,7 +36,9 @@ enum {
     SSS_ERR_ENERGY = 5,     /* scattered energy row outside the 2000-row tables */
     SSS_ERR_VOXEL = 6,      /* linear voxel index outside the volume (only if Nx != Ny) */
     SSS_ERR_WORKSPACE = 7,  /* workspace too small */
-    SSS_ERR_CAPACITY = 8    /* an output capacity was too small */
+    SSS_ERR_CAPACITY = 8,   /* an output capacity was too small */
+    SSS_ERR_EVENT = 9       /* a list-mode event addresses a crystal or ring outside the sinogram
+                               tables; the reference raises IndexError (Timber/Datafile.py:90-92) */
 };
 
 /* Thread-local text of the last error. */
@@ -252,6 +254,58 @@ int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int
                               const float *scatters, const int64_t *scat_cell, const int64_t *scat_ring,
                               int32_t scat_clamp, float *images, double *sums, float *scale, int32_t *status,
                               void *stream);
+
+/* ---------------------------------------------------------------------------
+ * CASToR list-mode events.  Replaces ExportPrompts and InjectScatters
+ * (Python/Timber/Datafile.py:29-240) with ParseCASToRIDs (Coincidence.py:97-159).
+ * Events are fixed-size little-endian records (GenerateListEventInfo,
+ * Coincidence.py:47-95) already in device memory. */
+typedef struct sss_listmode_layout {
+    int32_t record_bytes;    /* bytes per event, a multiple of 4 */
+    int32_t id_offset;       /* byte offset of the two uint32 CASToR crystal IDs */
+    int32_t tof_offset;      /* byte offset of the float32 TOF difference (ps) */
+    int32_t scatter_offset;  /* injection: byte offset the scatter rate is inserted at */
+} sss_listmode_layout;
+
+typedef struct sss_sino_map {
+    const int16_t *lor;      /* device [nd_lor][nd_lor][2] (angular, radial), -1 = no LOR */
+    int32_t nd_lor;          /* crystals of the LOR table (crystals per ring / mash) */
+    int32_t mash;            /* crystals per LOR-table crystal */
+    int32_t shift;           /* crystal ID shift of the first module */
+    const int16_t *slices;   /* device [nr_table][nr_table] slice of each ring pair, -1 = none
+                                (SinogramIndex, or LookUpTable with span) */
+    int32_t nr_table;
+    int32_t nrad, nang, nslices;  /* sinogram shape */
+    int32_t tof_bins;
+    double tof_range;        /* ps */
+} sss_sino_map;
+
+/* Prompt histogram: counts (device uint32 [nrad][nang][nslices][tof_bins],
+ * zeroed by the caller) += 1 per event in range.  last (device, zeroed,
+ * [nrad*nang*nslices], or NULL when no randoms / normalisation sinogram is
+ * wanted) records the last event of each cell for sss_histogram_finish. */
+int sss_histogram_prompts(const void *events, int64_t n_events, const sss_listmode_layout *layout,
+                          const sss_sino_map *map, uint32_t *counts, unsigned long long *last,
+                          int32_t *status, void *stream);
+/* prompts (device uint16, same shape as counts) = counts modulo 2^16, as the
+ * reference's uint16 histogram wraps; randoms / norm (device float32 per
+ * cell, each may be NULL) get the last event's event[0] * duration /
+ * tof_bins and event[1] (Datafile.py:94-99; norm must start at 1). */
+int sss_histogram_finish(const void *events, int64_t n_events, const sss_listmode_layout *layout,
+                         const sss_sino_map *map, const uint32_t *counts, const unsigned long long *last,
+                         double duration, uint16_t *prompts, float *randoms, float *norm, void *stream);
+/* Scatter injection: keeps the events the reference keeps, in file order,
+ * each with the float32 rate factor[bin] * scatters[bin][cell] inserted at
+ * scatter_offset (out_events: record_bytes + 4 per event; *out_count
+ * (device) = events written).  scatters: device float32
+ * [tof_bins][nrad][nang][nslices]; factor: device float32 [tof_bins] =
+ * Scale[b] * 2/c / duration as the reference rounds it.  workspace: at least
+ * sss_inject_workspace_size(n_events) device bytes. */
+size_t sss_inject_workspace_size(int64_t n_events);
+int sss_inject_scatters(const void *events, int64_t n_events, const sss_listmode_layout *layout,
+                        const sss_sino_map *map, const float *scatters, const float *factor, void *out_events,
+                        unsigned long long *out_count, void *workspace, size_t workspace_bytes,
+                        int32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Stage timing (no reference counterpart: instrumentation for benchmarks).

@@ -18,6 +18,7 @@ ABI_VERSION = 2  # SSS300_ABI_VERSION of include/sss300.h
 ERROR_NAMES = {
     1: "SSS_ERR_INVALID", 2: "SSS_ERR_CUDA", 3: "SSS_ERR_OVERRUN", 4: "SSS_ERR_TOF_RANGE",
     5: "SSS_ERR_ENERGY", 6: "SSS_ERR_VOXEL", 7: "SSS_ERR_WORKSPACE", 8: "SSS_ERR_CAPACITY",
+    9: "SSS_ERR_EVENT",
 }
 
 # every symbol the header declares, with (restype, argtypes)
@@ -57,6 +58,19 @@ class TofProblem(C.Structure):
 SSS_FLAG_KAHAN = 1
 
 
+class ListmodeLayout(C.Structure):
+    """Mirror of ``struct sss_listmode_layout``."""
+    _fields_ = [("record_bytes", _I32), ("id_offset", _I32), ("tof_offset", _I32),
+                ("scatter_offset", _I32)]
+
+
+class SinoMap(C.Structure):
+    """Mirror of ``struct sss_sino_map``."""
+    _fields_ = [("lor", _P), ("nd_lor", _I32), ("mash", _I32), ("shift", _I32), ("slices", _P),
+                ("nr_table", _I32), ("nrad", _I32), ("nang", _I32), ("nslices", _I32),
+                ("tof_bins", _I32), ("tof_range", _D)]
+
+
 SIGNATURES = {
     "sss_last_error": (C.c_char_p, []),
     "sss_abi_version": (C.c_int, []),
@@ -85,6 +99,13 @@ SIGNATURES = {
                                             _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P]),
     "sss_backproject_fit": (C.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _P,
                                       _P, _I32, _P, _P, _P, _P, _P]),
+    "sss_histogram_prompts": (C.c_int, [_P, _I64, C.POINTER(ListmodeLayout), C.POINTER(SinoMap), _P, _P,
+                                        _P, _P]),
+    "sss_histogram_finish": (C.c_int, [_P, _I64, C.POINTER(ListmodeLayout), C.POINTER(SinoMap), _P, _P,
+                                       _D, _P, _P, _P, _P]),
+    "sss_inject_workspace_size": (C.c_size_t, [_I64]),
+    "sss_inject_scatters": (C.c_int, [_P, _I64, C.POINTER(ListmodeLayout), C.POINTER(SinoMap), _P, _P,
+                                      _P, _P, _P, C.c_size_t, _P, _P]),
     "sss_set_timing": (None, [C.c_int]),
     "sss_get_timing": (C.c_int, [_P]),
     "sss_probe_ex2_rate": (C.c_int, [C.POINTER(_D), _P]),

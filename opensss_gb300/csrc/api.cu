@@ -46,6 +46,10 @@ extern "C" int sss_status_code(int32_t s)
         return sss_set_error(SSS_ERR_ENERGY, "a scattered energy row fell outside the tables");
     if (s & kErrCapacity)
         return sss_set_error(SSS_ERR_CAPACITY, "an internal capacity was exceeded");
+    if (s & kErrEvent)
+        return sss_set_error(SSS_ERR_EVENT,
+                             "a list-mode event addresses a crystal or ring outside the sinogram tables "
+                             "(the reference raises IndexError here)");
     return sss_set_error(SSS_ERR_INVALID, "unknown device status 0x%x", (unsigned)s);
 }
 

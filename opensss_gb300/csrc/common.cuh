@@ -16,6 +16,7 @@ enum DeviceError : int32_t {
     kErrEnergy = 1 << 2,     // scattered-energy row outside the 2000-row tables
     kErrVoxel = 1 << 3,      // linear voxel index outside the volume (Nx != Ny case)
     kErrCapacity = 1 << 4,   // an internal list capacity was exceeded
+    kErrEvent = 1 << 5,      // a list-mode event outside the sinogram tables (reference: IndexError)
 };
 
 constexpr int kTofEntries = 8001;  // -4000..4000 ps, SingleScatterSimulationTOF.py:145-147

@@ -245,3 +245,49 @@ def served_beds(seed: int = 0):
     large = [dataclasses.replace(pr, name=f"bed{b}-large")
              for b, pr in enumerate(config3_instances(4, seed=5))]
     return small, large
+
+
+def listmode_header(name: str, n_events: int, tof_range: float = 1000.0, random_flag: bool = True,
+                    normalization_flag: bool = True, attenuation_flag: bool = False,
+                    duration: float = 600.0) -> dict:
+    """CASToR header fields of the synthetic list-mode files (single line per
+    event, TOF)."""
+    return {"data_filename": f"{name}.Cdf", "nb_events": int(n_events), "data_mode": "list-mode",
+            "data_type": "PET", "start_time": 0.0, "duration": float(duration), "scanner_name": "SYNTH",
+            "isotope": "F18", "calibration_factor": 1.0, "nb_max_lines": 1,
+            "attenuation_flag": attenuation_flag, "normalization_flag": normalization_flag,
+            "scatter_flag": False, "random_flag": random_flag, "tof_flag": True, "tof_resolution": 214.0,
+            "tof_bin_size": None, "tof_nb_bins": None, "tof_range": float(tof_range)}
+
+
+def synthetic_listmode(directory: str, name: str, n_events: int, crystals_per_ring: int, rings: int,
+                       seed: int = 0, tof_range: float = 1000.0, tof_sigma: float = 400.0,
+                       random_flag: bool = True, normalization_flag: bool = True,
+                       attenuation_flag: bool = False, duration: float = 600.0) -> str:
+    """Writes a seeded CASToR list-mode file pair ``<name>.Cdh`` / ``<name>.Cdf``
+    (single line per event, TOF) and returns the header's file name.  Crystal
+    IDs are uniform over the scanner (ring * crystals_per_ring + crystal); TOF
+    differences are Gaussian with ``tof_sigma`` ps, so some fall outside
+    ``tof_range``; correction factors are seeded uniform values."""
+    import os
+
+    from . import Coincidence, Headerfile
+
+    rng = np.random.default_rng(seed)
+    header = listmode_header(name, n_events, tof_range, random_flag, normalization_flag, attenuation_flag,
+                             duration)
+    fmt, pos = Coincidence.GenerateEventClass(header)
+    ncorr = int(attenuation_flag) + int(random_flag) + int(normalization_flag) + 1
+    fields = [("time", "<u4")] + [(f"c{i}", "<f4") for i in range(ncorr)] + [("id1", "<u4"), ("id2", "<u4")]
+    ev = np.zeros(int(n_events), dtype=np.dtype(fields))
+    ev["time"] = np.sort(rng.integers(0, int(duration * 1000), size=n_events)).astype(np.uint32)
+    for i in range(ncorr - 1):
+        ev[f"c{i}"] = rng.uniform(0.5, 2.0, size=n_events).astype(np.float32)
+    ev[f"c{ncorr - 1}"] = (rng.normal(0.0, tof_sigma, size=n_events)).astype(np.float32)
+    ncrystals = crystals_per_ring * rings
+    ev["id1"] = rng.integers(0, ncrystals, size=n_events).astype(np.uint32)
+    ev["id2"] = rng.integers(0, ncrystals, size=n_events).astype(np.uint32)
+    assert ev.dtype.itemsize == Coincidence.record_bytes(fmt)
+    ev.tofile(os.path.join(directory, header["data_filename"]))
+    Headerfile.WriteHeaderFile(header, os.path.join(directory, f"{name}.Cdh"))
+    return f"{name}.Cdh"

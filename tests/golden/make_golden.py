@@ -446,7 +446,60 @@ def gen_span(R):
     _save("span", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit", "span"]
+# ---------------------------------------------------------------- list-mode
+
+
+def gen_listmode(R):
+    """ExportPrompts and InjectScatters (the reference's Timber package) on
+    seeded synthetic list-mode files: plain, with mash 2 and a crystal
+    shift, and with span (LookUpTable slices)."""
+    sys.path.insert(0, refpy.REFERENCE_PY)
+    from Timber import Datafile as TD
+
+    out = {}
+    cases = (("plain", 48, 6, 1, 0, None), ("mash_shift", 48, 6, 2, 3, None), ("span", 48, 10, 1, 0, (3, 9)))
+    for ci, (tag, ncr, nr, mash, shift, span) in enumerate(cases):
+        with tempfile.TemporaryDirectory() as d:
+            hdr = W.synthetic_listmode(d, f"case{ci}_df", 20000, ncr, nr, seed=30 + ci, tof_range=1000.0)
+            lor, si, _ = R["Sinogram"].SinogramCoordinates(1, 1, 1, 1, ncr // mash, nr, ID_Shidt=False)
+            if span:
+                msi, _, lut, _ = R["DataReduction"].SinogramLUT(nr, span[0], span[1])
+                table = lut
+            else:
+                msi, lut, table = si, np.array([]), si
+            p, r, n = TD.ExportPrompts(d, hdr, lor, table, 5, 1000.0, mash=mash, Shift=shift)
+            out[f"case{ci}_args"] = np.array([ncr, nr, mash, shift, -1 if not span else span[0],
+                                              -1 if not span else span[1]])
+            out[f"case{ci}_events"] = np.fromfile(os.path.join(d, f"case{ci}_df.Cdf"), dtype=np.uint8)
+            out[f"case{ci}_prompts"] = p
+            out[f"case{ci}_randoms"] = r
+            out[f"case{ci}_norm"] = n
+            # injection of a seeded scatter estimate
+            rng = np.random.default_rng(40 + ci)
+            nsl = msi.shape[0] if span else int(np.max(si)) + 1
+            shp = (int(lor[:, :, 1].max()) + 1, int(lor[:, :, 0].max()) + 1, nsl)
+            scale = rng.uniform(0.5, 2.0, size=5).astype(np.float32)
+            np.save(os.path.join(d, "ScaleFactors.npy"), scale)
+            sc = []
+            for b in range(5):
+                arr = rng.uniform(0.0, 1.0, size=shp).astype(np.float32)
+                np.savez_compressed(os.path.join(d, f"SSS_mashed_bin{b}"), arr)
+                sc.append(arr)
+            TD.InjectScatters(d, hdr, lor, msi, d, lut, bool(span), 1000.0, None, mash=mash, Shift=shift)
+            out[f"case{ci}_scale"] = scale
+            out[f"case{ci}_scatters"] = np.stack(sc)
+            new_name = hdr[:-6] + "scatter_" + hdr[-6:]
+            with open(os.path.join(d, new_name)) as f:
+                out[f"case{ci}_injected_header"] = np.frombuffer(f.read().encode(), dtype=np.uint8)
+            dname = f"case{ci}_df.Cdf"
+            out[f"case{ci}_injected"] = np.fromfile(os.path.join(d, dname[:-6] + "scatter_" + dname[-6:]),
+                                                    dtype=np.uint8)
+            print(f"listmode case {ci} ({tag}): {int(p.sum())} prompts, {out[f'case{ci}_injected'].size} "
+                  "injected bytes")
+    _save("listmode", **out)
+
+
+ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit", "span", "listmode"]
 
 
 def main():
@@ -478,6 +531,8 @@ def main():
         gen_fit(R)
     if "span" in which:
         gen_span(R)
+    if "listmode" in which:
+        gen_listmode(R)
 
 
 if __name__ == "__main__":
