@@ -290,6 +290,7 @@ def run_ours(args, rank, world, local_rank):
     batch = None if args.no_batch or world > 1 else run_batch(dev, args, att)
     precision = None if args.no_precision or world > 1 else run_precision(dev, args, att)
     serving = None if args.no_serving or world > 1 else run_serving(dev, args, att)
+    listmode = None if args.no_listmode or world > 1 else run_listmode(dev, args)
 
     ms = 1e3 * total_s / args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -304,7 +305,7 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
             "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
-            "batch": batch, "precision": precision, "serving": serving}
+            "batch": batch, "precision": precision, "serving": serving, "listmode": listmode}
     print(json.dumps(line), flush=True)
 
 
@@ -589,6 +590,78 @@ def run_serving(dev, args, att):
             "server_stats": dict(srv.stats), "rel_l2_vs_fp64_small": errs, "clocks": clk.summary()}
 
 
+def run_listmode(dev, args):
+    """Prompt histogramming of ``--listmode-events`` seeded list-mode events
+    (TOF, randoms and normalisation fields, 24-byte records) of the
+    760-crystal x 80-ring scanner with the demo's data reduction (mash 2,
+    span 19, MRD 79: 381 x 190 x 815 cells) into 6 TOF bins.  Device-resident
+    events (``value``) and through the drop-in path with the events in pinned
+    host memory and the uint16 sinogram copied back (``e2e``); the CPU
+    baseline is the host restatement of the reference's per-event loop on
+    the first ``--listmode-cpu-events`` events."""
+    import struct
+
+    import torch
+
+    from opensss_gb300 import Coincidence, Datafile, geometry as G, workloads as W
+
+    n = args.listmode_events
+    header = W.listmode_header("bench_df", n)
+    ev = W.synthetic_events(header, 760, 80, seed=2026)
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, 80, ID_Shidt=False)
+    _, _, lut, _ = G.SinogramLUT(80, 19, 79)
+    raw = torch.from_numpy(ev.view(np.uint8).reshape(-1))
+    ev_h = raw.pin_memory()
+    ev_d = ev_h.to(dev)
+    st = torch.cuda.current_stream(dev)
+
+    def once(events):
+        return Datafile.histogram_device(events, header, lor, lut, 6, 1000.0, mash=2, Shift=0, device=dev)
+
+    for _ in range(args.warmup):
+        once(ev_d)
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        once(ev_d)
+        e1.record(st)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        p, r, nrm = once(ev_h.to(dev, non_blocking=True))
+        host = (p.cpu(), r.cpu(), nrm.cpu())
+        e2e.append(time.perf_counter() - t0)
+    out_bytes = sum(t.numel() * t.element_size() for t in host)
+    # CPU: the reference's loop restated (struct.iter_unpack + ParseCASToRIDs per event)
+    m = min(n, args.listmode_cpu_events)
+    fmt, pos = Coincidence.GenerateEventClass(header)
+    table = lut
+    t0 = time.perf_counter()
+    acc = 0
+    for e in struct.iter_unpack(fmt, ev[:m].tobytes()):
+        d1, r1, d2, r2, tof = Coincidence.ParseCASToRIDs(e, pos, 760, 0)
+        a, rr = lor[d1 // 2, d2 // 2]
+        s = table[r1, r2]
+        if s == -1 or rr == -1 or a == -1 or abs(tof) > 1000.0:
+            continue
+        t = (tof + 1000.0) / (2 * 1000.0 / 6)
+        acc += 0 <= t < 6
+    cpu_s = time.perf_counter() - t0
+    mean_ms = statistics.mean(ms)
+    return {"workload": f"{n} seeded list-mode events, 760 x 80 scanner, mash 2, span 19 (381x190x815 cells), "
+                        "6 TOF bins", "unit": "events/s", "value": n / (mean_ms / 1e3), "ms_per_step": mean_ms,
+            "steps": args.steps, "warmup": args.warmup,
+            "e2e": {"value": n / statistics.mean(e2e), "unit": "events/s", "h2d_bytes_per_step": int(raw.numel()),
+                    "d2h_bytes_per_step": int(out_bytes)},
+            "gbs_event_read": raw.numel() / (mean_ms / 1e3) / 1e9,
+            "cpu_baseline": {"value": m / cpu_s, "unit": "events/s", "cores": 1, "kind": "port",
+                             "sample": f"first {m} events, per-event Python loop as the reference's"}}
+
+
 def _sfu_peak(clocks):
     """SFU 2^x peak measured in this process (sss_probe_ex2_rate: every SM
     issuing independent ex2 chains), else 152 SMs x 16 results/clk x max clock."""
@@ -639,6 +712,9 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="length of the arrival window")
     ap.add_argument("--serve-check", type=int, default=2,
                     help="served small requests checked against the FP64 oracle")
+    ap.add_argument("--no-listmode", action="store_true", help="skip the list-mode histogramming")
+    ap.add_argument("--listmode-events", type=int, default=50_000_000)
+    ap.add_argument("--listmode-cpu-events", type=int, default=200_000)
     ap.add_argument("--max-points", type=int, default=None,
                     help="limit each step to the first scatter points (profiling runs only)")
     args = ap.parse_args()

@@ -271,13 +271,28 @@ def synthetic_listmode(directory: str, name: str, n_events: int, crystals_per_ri
     ``tof_range``; correction factors are seeded uniform values."""
     import os
 
-    from . import Coincidence, Headerfile
+    from . import Headerfile
 
-    rng = np.random.default_rng(seed)
     header = listmode_header(name, n_events, tof_range, random_flag, normalization_flag, attenuation_flag,
                              duration)
-    fmt, pos = Coincidence.GenerateEventClass(header)
-    ncorr = int(attenuation_flag) + int(random_flag) + int(normalization_flag) + 1
+    ev = synthetic_events(header, crystals_per_ring, rings, seed, tof_sigma)
+    ev.tofile(os.path.join(directory, header["data_filename"]))
+    Headerfile.WriteHeaderFile(header, os.path.join(directory, f"{name}.Cdh"))
+    return f"{name}.Cdh"
+
+
+def synthetic_events(header: dict, crystals_per_ring: int, rings: int, seed: int = 0,
+                     tof_sigma: float = 400.0) -> np.ndarray:
+    """Seeded event records for ``header`` (see ``synthetic_listmode``) as a
+    structured array whose bytes are the data file."""
+    from . import Coincidence
+
+    rng = np.random.default_rng(seed)
+    n_events = header["nb_events"]
+    fmt, _ = Coincidence.GenerateEventClass(header)
+    ncorr = (int(header["attenuation_flag"]) + int(header["random_flag"]) + int(header["normalization_flag"])
+             + 1)
+    duration = header["duration"]
     fields = [("time", "<u4")] + [(f"c{i}", "<f4") for i in range(ncorr)] + [("id1", "<u4"), ("id2", "<u4")]
     ev = np.zeros(int(n_events), dtype=np.dtype(fields))
     ev["time"] = np.sort(rng.integers(0, int(duration * 1000), size=n_events)).astype(np.uint32)
@@ -288,6 +303,4 @@ def synthetic_listmode(directory: str, name: str, n_events: int, crystals_per_ri
     ev["id1"] = rng.integers(0, ncrystals, size=n_events).astype(np.uint32)
     ev["id2"] = rng.integers(0, ncrystals, size=n_events).astype(np.uint32)
     assert ev.dtype.itemsize == Coincidence.record_bytes(fmt)
-    ev.tofile(os.path.join(directory, header["data_filename"]))
-    Headerfile.WriteHeaderFile(header, os.path.join(directory, f"{name}.Cdh"))
-    return f"{name}.Cdh"
+    return ev
