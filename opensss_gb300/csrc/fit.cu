@@ -111,7 +111,17 @@ __global__ void __launch_bounds__(256) upsample_kernel(const float* __restrict__
         }
         __syncthreads();
         float* o = out + cell * nslices;
-        for (int sl = threadIdx.x; sl < nslices; sl += blockDim.x) __stcs(o + sl, vals[__ldg(ring_idx + sl)]);
+        if ((nslices & 3) == 0 && ((reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(ring_idx)) & 15) == 0) {
+            // four slices per store: the row start is 16-byte aligned
+            const int4* ri4 = reinterpret_cast<const int4*>(ring_idx);
+            float4* o4 = reinterpret_cast<float4*>(o);
+            for (int q = threadIdx.x; q < (nslices >> 2); q += blockDim.x) {
+                const int4 r = __ldg(ri4 + q);
+                __stcs(o4 + q, make_float4(vals[r.x], vals[r.y], vals[r.z], vals[r.w]));
+            }
+        } else {
+            for (int sl = threadIdx.x; sl < nslices; sl += blockDim.x) __stcs(o + sl, vals[__ldg(ring_idx + sl)]);
+        }
     }
 }
 
