@@ -231,9 +231,10 @@ int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const flo
  * mask: mask_f32 (multiplied) or, if not NULL, mask_u8 (mask >= 1).  The
  * scatter value is scatters[scat_cell[cell] + scat_ring[slice]] (clamped at
  * 0 when scat_clamp), so an upsampled sinogram can be read straight from
- * the sampled one.  images: device workspace 4 * Nx*Ny*Nz floats (P, S, R,
- * sensitivity); sums: device 2 doubles; scale: device float, the fitted
- * slope (reference: float32 array of shape (1,)). */
+ * the sampled one.  images: device workspace 8 * Nx*Ny*Nz floats (P, S, R,
+ * sensitivity, and the R and sensitivity shared by all bins); sums: device 2
+ * doubles; scale: device float, the fitted slope (reference: float32 array
+ * of shape (1,)). */
 int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
                         const double *geometry, const int16_t *lor, const int16_t *sino_order,
                         int32_t af, const float *prompts, const float *randoms, const float *mask_f32,
@@ -254,6 +255,27 @@ int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int
                               const float *scatters, const int64_t *scat_cell, const int64_t *scat_ring,
                               int32_t scat_clamp, float *images, double *sums, float *scale, int32_t *status,
                               void *stream);
+
+/* All TOF bins of a scale fit in one pass.  Replaces the per-bin loop of
+ * ScaleScattersToPrompts (Python/openSSS/Scaling.py:86-113): every LOR is
+ * walked once and back-projected into the images of each bin whose masked
+ * scatter is non-zero there; each bin gets the scale its own
+ * sss_backproject_fit(_pairs) call would give.  Bin b reads
+ * prompts[b*prompt_stride + cell*nslices + slice] and the scatter value
+ * scatters[b*scat_stride + scat_cell[cell] + scat_ring[slice]]; randoms and
+ * the mask are shared.  Either sino_order (all ring pairs) or pairs (span)
+ * is given.  images: device [nbins + 1][4][Nx*Ny*Nz] (block nbins: the
+ * randoms and sensitivity of the LORs every bin uses, so those are added
+ * once); sums: device [nbins][2]; scales: device float [nbins];
+ * 1 <= nbins <= 64. */
+int sss_backproject_fit_bins(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
+                             const double *geometry, const int16_t *lor, const int16_t *sino_order,
+                             const int32_t *pairs, int32_t npairs, int32_t nslices, int32_t length_weighted,
+                             int32_t af, int32_t nbins, const float *prompts, int64_t prompt_stride,
+                             const float *randoms, const float *mask_f32, const uint8_t *mask_u8,
+                             const float *scatters, int64_t scat_stride, const int64_t *scat_cell,
+                             const int64_t *scat_ring, int32_t scat_clamp, float *images, double *sums,
+                             float *scales, int32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------
  * CASToR list-mode events.  Replaces ExportPrompts and InjectScatters

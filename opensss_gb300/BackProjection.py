@@ -43,7 +43,7 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
     cs = as_device(scat_cell, torch.int64, device)
     rs = as_device(scat_ring, torch.int64, device)
     nvox = int(np.prod(grid))
-    images = torch.empty(4 * nvox, dtype=torch.float32, device=device)
+    images = torch.empty(8 * nvox, dtype=torch.float32, device=device)
     sums = torch.empty(2, dtype=torch.float64, device=device)
     scale = torch.empty(1, dtype=torch.float32, device=device)
     status = torch.zeros(1, dtype=torch.int32, device=device)
@@ -66,8 +66,53 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
     st.synchronize()
     _lib.check_status(int(status.item()))
     if return_images:
-        return float(scale.item()), images.reshape(4, nvox)
+        im = images.reshape(2, 4, nvox)
+        return float(scale.item()), torch.stack([im[0, 0], im[0, 1], im[0, 2] + im[1, 2], im[0, 3] + im[1, 3]])
     return float(scale.item())
+
+
+def fit_bins_device(prompts, randoms, mask, scatters, scat_stride: int, scat_cell, scat_ring, GridSize,
+                    ImageSize, Geometry, SinogramCoordinates, SinogramOrder, AccelerationFactor,
+                    scat_clamp=False, device="cuda", span: bool = False) -> np.ndarray:
+    """Scales of all TOF bins in one pass (``sss_backproject_fit_bins``).
+    prompts: CUDA float32 [bins, cell, slice]; scatters: CUDA float32 with
+    bin b's values from ``b * scat_stride`` (through the gather tables);
+    randoms / mask as in ``fit_device``.  Returns float32 [bins]."""
+    geom = np.asarray(Geometry, dtype=np.float64)
+    nr, nd = geom.shape[:2]
+    nbins = int(prompts.shape[0])
+    grid = np.ascontiguousarray(np.asarray(GridSize).reshape(-1)[:3], dtype=np.int32)
+    bounds = np.ascontiguousarray(np.asarray(ImageSize, dtype=np.float64).reshape(-1)[:6])
+    g = as_device(geom, torch.float64, device)
+    lor = as_device(np.asarray(SinogramCoordinates, dtype=np.int16), torch.int16, device)
+    order = pairs = None
+    npairs = nslices = 0
+    if span:
+        pairs_np = geometry.span_ring_pairs(SinogramOrder)
+        pairs = as_device(pairs_np, torch.int32, device)
+        npairs = nslices = pairs_np.shape[0]
+    else:
+        order = as_device(np.asarray(SinogramOrder, dtype=np.int16)[:nr, :nr], torch.int16, device)
+    cs = as_device(scat_cell, torch.int64, device)
+    rs = as_device(scat_ring, torch.int64, device)
+    nvox = int(np.prod(grid))
+    images = torch.empty((nbins + 1) * 4 * nvox, dtype=torch.float32, device=device)
+    sums = torch.empty(2 * nbins, dtype=torch.float64, device=device)
+    scales = torch.empty(nbins, dtype=torch.float32, device=device)
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    m_u8 = mask if mask.dtype == torch.uint8 else None
+    m_f = None if m_u8 is not None else mask
+    st = torch.cuda.current_stream(device)
+    stride = int(prompts[0].numel())
+    _lib.check(_lib.lib().sss_backproject_fit_bins(
+        grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), nr, nd, _ptr(g), _ptr(lor),
+        _ptr(order), _ptr(pairs), npairs, nslices, int(bool(span)), int(AccelerationFactor or 1), nbins,
+        _ptr(prompts), stride, _ptr(randoms), _ptr(m_f), _ptr(m_u8), _ptr(scatters), int(scat_stride), _ptr(cs),
+        _ptr(rs), int(bool(scat_clamp)), _ptr(images), _ptr(sums), _ptr(scales), _ptr(status),
+        C.c_void_p(st.cuda_stream)))
+    st.synchronize()
+    _lib.check_status(int(status.item()))
+    return scales.cpu().numpy()
 
 
 def BackProjectionScatterRandFit(PromptSinogram, ScatterSinogram, RandomSinogram, MaskSinogram,

@@ -99,6 +99,8 @@ SIGNATURES = {
                                             _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P]),
     "sss_backproject_fit": (C.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, _P, _P, _P,
                                       _P, _I32, _P, _P, _P, _P, _P]),
+    "sss_backproject_fit_bins": (C.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P, _I32, _I32, _I32, _I32, _I32,
+                                           _P, _I64, _P, _P, _P, _P, _I64, _P, _P, _I32, _P, _P, _P, _P, _P]),
     "sss_histogram_prompts": (C.c_int, [_P, _I64, C.POINTER(ListmodeLayout), C.POINTER(SinoMap), _P, _P,
                                         _P, _P]),
     "sss_histogram_finish": (C.c_int, [_P, _I64, C.POINTER(ListmodeLayout), C.POINTER(SinoMap), _P, _P,

@@ -193,17 +193,28 @@ struct FitParams {
     int npairs, nslices;
     int length_weighted;        // span: value * length / sum(lengths) (:294-297), else value / n
     int nr, nd, na, af, cap;
-    const float* prompts;       // [cell][slice]
-    const float* randoms;
+    int nbins;                  // bins fitted together (one walk per LOR serves all)
+    long long prompt_stride;    // elements between the bins' prompt sinograms
+    long long scat_stride;      // elements between the bins' scatter values
+    const float* prompts;       // [bin][cell][slice]
+    const float* randoms;       // [cell][slice], shared by the bins
     const float* mask_f32;      // either a float mask (multiplied, :157-167) ...
     const uint8_t* mask_u8;     // ... or a uint8 tail mask (mask >= 1, Scaling.py:76)
     const float* scat;          // scatter values, addressed through the tables below
     const long long* scat_cell; // [cell] offset of the scatter value's cell
     const long long* scat_ring; // [slice] offset of the scatter value's slice
     int scat_clamp;             // clamp the scatter value at 0 (upsampling's fill, :163)
-    float* img;                 // 4 x nvox: P, S, R, sensitivity
+    float* img;                 // [bin][4][nvox]: P, S, R, sensitivity; block nbins holds the R and
+                                // sensitivity of the LORs that every bin uses
     int32_t* status;
 };
+
+// Scatter value of bin b at (cell, slice), clamped as the upsampling fills it.
+__device__ __forceinline__ float fit_scatter(const FitParams& P, int b, long long cell, int slice)
+{
+    const float sv = P.scat[b * P.scat_stride + P.scat_cell[cell] + P.scat_ring[slice]];
+    return P.scat_clamp ? fmaxf(sv, 0.f) : sv;
+}
 
 __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
 {
@@ -223,11 +234,14 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     const long long cell = (long long)rad * (P.nd / 2) + ang;
     const long long c = cell * (long long)P.nslices + slice;
     const float m = P.mask_u8 ? (P.mask_u8[c] >= 1 ? 1.f : 0.f) : P.mask_f32[c];
-    float sv = P.scat[P.scat_cell[cell] + P.scat_ring[slice]];
-    if (P.scat_clamp) sv = fmaxf(sv, 0.f);
-    const float s = m * sv;
-    if (s == 0.f) return;  // :99-100
-    const float pv = m * P.prompts[c], rv = m * P.randoms[c];
+    // bins whose masked scatter is non-zero back-project this LOR (:99-100)
+    unsigned long long bins = 0;
+    for (int b = 0; b < P.nbins; ++b)
+        if (m * fit_scatter(P, b, cell, slice) != 0.f) bins |= 1ull << b;
+    if (!bins) return;
+    const unsigned long long all = P.nbins == 64 ? ~0ull : (1ull << P.nbins) - 1;
+    const float rv = m * P.randoms[c];
+    const float s0 = m * fit_scatter(P, 0, cell, slice), p0 = m * P.prompts[c];
     double lc[6];
     lor_line(P.geom, P.nd, L.r1, d1, L.r2, d2, lc);
     Ray r;
@@ -245,7 +259,7 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     }
     if (n_vox == 0) return;
     const float fn = (float)n_vox;
-    const float ap = pv / fn, as = s / fn, ar = rv / fn;
+    const float ar = rv / fn;
     bool bad = false;
     ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
         const long long v = lin - 1;
@@ -253,31 +267,50 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
             bad = true;
             return;
         }
-        if (P.length_weighted) {
-            const double w = div64(ref_length(r, t0, t1), total);
-            atomicAdd(P.img + v, (float)mul64((double)pv, w));
-            atomicAdd(P.img + P.nvox + v, (float)mul64((double)s, w));
-            atomicAdd(P.img + 2 * P.nvox + v, (float)mul64((double)rv, w));
-        } else {
-            atomicAdd(P.img + v, ap);
-            atomicAdd(P.img + P.nvox + v, as);
-            atomicAdd(P.img + 2 * P.nvox + v, ar);
+        const double w = P.length_weighted ? div64(ref_length(r, t0, t1), total) : 0.0;
+        const float rw = P.length_weighted ? (float)mul64((double)rv, w) : ar;
+        for (unsigned long long rest = bins; rest; rest &= rest - 1) {
+            const int b = __ffsll((long long)rest) - 1;
+            float* img = P.img + (long long)b * 4 * P.nvox;
+            // one bin: the LOR's values, else re-read per voxel (L1-resident)
+            const float s = P.nbins == 1 ? s0 : m * fit_scatter(P, b, cell, slice);
+            const float pv = P.nbins == 1 ? p0 : m * P.prompts[b * P.prompt_stride + c];
+            if (P.length_weighted) {
+                atomicAdd(img + v, (float)mul64((double)pv, w));
+                atomicAdd(img + P.nvox + v, (float)mul64((double)s, w));
+            } else {
+                atomicAdd(img + v, pv / fn);
+                atomicAdd(img + P.nvox + v, s / fn);
+            }
+            if (bins != all) {  // randoms and sensitivity of this bin alone
+                atomicAdd(img + 2 * P.nvox + v, rw);
+                atomicAdd(img + 3 * P.nvox + v, 1.0f);
+            }
         }
-        atomicAdd(P.img + 3 * P.nvox + v, 1.0f);
+        if (bins == all) {  // LORs every bin uses share one randoms / sensitivity image
+            float* img = P.img + (long long)P.nbins * 4 * P.nvox;
+            atomicAdd(img + 2 * P.nvox + v, rw);
+            atomicAdd(img + 3 * P.nvox + v, 1.0f);
+        }
     });
     if (bad) raise_error(P.status, kErrVoxel);
 }
 
-// per voxel: Sbp, T (BackProjection.py:191-204); sums of x*T and x*x in FP64
-__global__ void fit_reduce_kernel(const float* __restrict__ img, long long nvox, double* sums)
+// per voxel: Sbp, T (BackProjection.py:191-204); sums of x*T and x*x in FP64;
+// blockIdx.y = bin (images [bin][4][nvox], sums [bin][2])
+__global__ void fit_reduce_kernel(const float* __restrict__ img_all, long long nvox, int nbins,
+                                  double* sums_all)
 {
+    const float* img = img_all + (long long)blockIdx.y * 4 * nvox;
+    const float* common = img_all + (long long)nbins * 4 * nvox;
+    double* sums = sums_all + 2 * blockIdx.y;
     double sxt = 0.0, sxx = 0.0;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nvox;
          v += (long long)gridDim.x * blockDim.x) {
-        const float sens = img[3 * nvox + v];
+        const float sens = img[3 * nvox + v] + common[3 * nvox + v];
         float sb = img[nvox + v] / sens;
         float ab = img[v] / sens;
-        float rb = img[2 * nvox + v] / sens;
+        float rb = (img[2 * nvox + v] + common[2 * nvox + v]) / sens;
         if (isnan(sb) || isinf(sb)) sb = 0.f;
         if (isnan(ab) || isinf(ab)) ab = 0.f;
         if (isnan(rb) || isinf(rb)) rb = 0.f;
@@ -300,10 +333,12 @@ __global__ void fit_reduce_kernel(const float* __restrict__ img, long long nvox,
 
 // lstsq of one column through the origin (:207-210): minimum-norm solution
 // sum(xT)/sum(x^2) (0 when x is all zero), cast to float32, times 1e10.
-__global__ void fit_final_kernel(const double* sums, float* scale)
+__global__ void fit_final_kernel(const double* sums, float* scale, int nbins)
 {
-    const double a = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
-    *scale = (float)((double)(float)a * 1e10);
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    const double a = sums[2 * b + 1] > 0.0 ? sums[2 * b] / sums[2 * b + 1] : 0.0;
+    scale[b] = (float)((double)(float)a * 1e10);
 }
 
 int check_grid(const int32_t* grid, const double* bounds, const char* who)
@@ -411,14 +446,15 @@ namespace {
 
 int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd, const double* geometry,
                     const int16_t* lor, const int16_t* sino_order, const int32_t* pairs, int32_t npairs,
-                    int32_t nslices, int32_t length_weighted, int32_t af, const float* prompts,
-                    const float* randoms, const float* mask_f32, const uint8_t* mask_u8, const float* scatters,
-                    const int64_t* scat_cell, const int64_t* scat_ring, int32_t scat_clamp, float* images,
-                    double* sums, float* scale, int32_t* status, void* stream)
+                    int32_t nslices, int32_t length_weighted, int32_t af, int32_t nbins, const float* prompts,
+                    int64_t prompt_stride, const float* randoms, const float* mask_f32, const uint8_t* mask_u8,
+                    const float* scatters, int64_t scat_stride, const int64_t* scat_cell,
+                    const int64_t* scat_ring, int32_t scat_clamp, float* images, double* sums, float* scale,
+                    int32_t* status, void* stream)
 {
     int rc;
     if (!geometry || !lor || !prompts || !randoms || (!mask_f32 && !mask_u8) || !scatters || !scat_cell ||
-        !scat_ring || !images || !sums || !scale || nr < 1 || nd < 2 || af < 1)
+        !scat_ring || !images || !sums || !scale || nr < 1 || nd < 2 || af < 1 || nbins < 1 || nbins > 64)
         return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: bad argument");
     cudaStream_t st = (cudaStream_t)stream;
     FitParams P;
@@ -426,6 +462,9 @@ int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, i
     P.npairs = npairs;
     P.nslices = pairs ? nslices : nr * nr;
     P.length_weighted = length_weighted;
+    P.nbins = nbins;
+    P.prompt_stride = prompt_stride;
+    P.scat_stride = scat_stride;
     P.g = make_grid(grid, bounds);
     P.nvox = (long long)grid[0] * grid[1] * grid[2];
     P.geom = geometry;
@@ -446,8 +485,8 @@ int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, i
     P.scat_clamp = scat_clamp;
     P.img = images;
     P.status = status;
-    if (cudaMemsetAsync(images, 0, sizeof(float) * 4 * P.nvox, st) != cudaSuccess ||
-        cudaMemsetAsync(sums, 0, 2 * sizeof(double), st) != cudaSuccess)
+    if (cudaMemsetAsync(images, 0, sizeof(float) * 4 * P.nvox * (nbins + 1), st) != cudaSuccess ||
+        cudaMemsetAsync(sums, 0, 2 * sizeof(double) * nbins, st) != cudaSuccess)
         return sss_set_error(SSS_ERR_CUDA, "sss_backproject_fit: memset failed");
     const long long n = (long long)(pairs ? npairs : nr * nr) * P.na * P.na;
     if (n > 0) {
@@ -458,9 +497,10 @@ int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, i
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long want = (P.nvox + 255) / 256;
-    fit_reduce_kernel<<<(unsigned)(want < sms * 4 ? want : sms * 4), 256, 0, st>>>(images, P.nvox, sums);
+    const dim3 rgrid((unsigned)(want < sms * 4 ? want : sms * 4), (unsigned)nbins);
+    fit_reduce_kernel<<<rgrid, 256, 0, st>>>(images, P.nvox, nbins, sums);
     if ((rc = sss_check_launch("fit_reduce_kernel"))) return rc;
-    fit_final_kernel<<<1, 1, 0, st>>>(sums, scale);
+    fit_final_kernel<<<1, 64, 0, st>>>(sums, scale, nbins);
     return sss_check_launch("fit_final_kernel");
 }
 
@@ -478,9 +518,9 @@ extern "C" int sss_backproject_fit(const int32_t grid[3], const double bounds[6]
     int rc = check_grid(grid, bounds, "sss_backproject_fit");
     if (rc) return rc;
     if (!sino_order) return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: bad argument");
-    return backproject_fit(grid, bounds, nr, nd, geometry, lor, sino_order, nullptr, 0, 0, 0, af, prompts, randoms,
-                           mask_f32, mask_u8, scatters, scat_cell, scat_ring, scat_clamp, images, sums, scale,
-                           status, stream);
+    return backproject_fit(grid, bounds, nr, nd, geometry, lor, sino_order, nullptr, 0, 0, 0, af, 1, prompts, 0,
+                           randoms, mask_f32, mask_u8, scatters, 0, scat_cell, scat_ring, scat_clamp, images, sums,
+                           scale, status, stream);
 }
 
 extern "C" int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
@@ -496,6 +536,26 @@ extern "C" int sss_backproject_fit_pairs(const int32_t grid[3], const double bou
     if (!pairs || npairs < 0 || nslices < 1)
         return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit_pairs: bad argument");
     return backproject_fit(grid, bounds, nr, nd, geometry, lor, nullptr, pairs, npairs, nslices, length_weighted,
-                           af, prompts, randoms, mask_f32, mask_u8, scatters, scat_cell, scat_ring, scat_clamp,
-                           images, sums, scale, status, stream);
+                           af, 1, prompts, 0, randoms, mask_f32, mask_u8, scatters, 0, scat_cell, scat_ring,
+                           scat_clamp, images, sums, scale, status, stream);
+}
+
+extern "C" int sss_backproject_fit_bins(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
+                                        const double* geometry, const int16_t* lor, const int16_t* sino_order,
+                                        const int32_t* pairs, int32_t npairs, int32_t nslices,
+                                        int32_t length_weighted, int32_t af, int32_t nbins, const float* prompts,
+                                        int64_t prompt_stride, const float* randoms, const float* mask_f32,
+                                        const uint8_t* mask_u8, const float* scatters, int64_t scat_stride,
+                                        const int64_t* scat_cell, const int64_t* scat_ring, int32_t scat_clamp,
+                                        float* images, double* sums, float* scales, int32_t* status,
+                                        void* stream)
+{
+    int rc = check_grid(grid, bounds, "sss_backproject_fit_bins");
+    if (rc) return rc;
+    if ((!sino_order && !pairs) || (pairs && (npairs < 0 || nslices < 1)))
+        return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit_bins: bad argument");
+    return backproject_fit(grid, bounds, nr, nd, geometry, lor, pairs ? nullptr : sino_order, pairs,
+                           pairs ? npairs : 0, pairs ? nslices : 0, length_weighted, af, nbins, prompts,
+                           prompt_stride, randoms, mask_f32, mask_u8, scatters, scat_stride, scat_cell, scat_ring,
+                           scat_clamp, images, sums, scales, status, stream);
 }

@@ -128,3 +128,64 @@ def test_fit_reads_upsampled_scatter_without_materialising(cuda_ok):
                    torch.from_numpy(np.ascontiguousarray(lp[0])).to(dev), cell, ring, grid, bounds,
                    sc.geometry, lor, order, 1, scat_clamp=True)
     assert abs(s - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_all_bins_in_one_pass_match_per_bin_fits(cuda_ok, case):
+    """sss_backproject_fit_bins gives every bin the scale of its own fit."""
+    import torch
+
+    from opensss_gb300.BackProjection import fit_bins_device, fit_device
+
+    g = golden("fit")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = _sino(nd, nr)
+    shp = g[f"case{case}_scatter"].shape
+    ncell, nsl = shp[0] * shp[1], shp[2]
+    rng = np.random.default_rng(case)
+    scat = np.stack([g[f"case{case}_scatter"] * f for f in (1.0, 0.5, 2.0)])
+    scat[1][rng.uniform(size=shp) < 0.2] = 0  # bins skip different LORs
+    prm = np.stack([rng.poisson(3.0 * f, size=shp).astype(np.float32) for f in (1.0, 0.7, 1.5)])
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a.reshape(-1, ncell, nsl))).cuda()  # noqa: E731
+    cell = np.arange(ncell, dtype=np.int64) * nsl
+    ring = np.arange(nsl, dtype=np.int64)
+    rnd = dev(g[f"case{case}_randoms"])[0]
+    mask = dev(g[f"case{case}_mask"])[0]
+    order = si[:nr, :nr].T
+    got = fit_bins_device(dev(prm), rnd, mask, dev(scat).reshape(-1), ncell * nsl, cell, ring,
+                          g[f"case{case}_grid"], g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, order, af)
+    for b in range(3):
+        ref = fit_device(dev(prm)[b], rnd, mask, dev(scat)[b], cell, ring, g[f"case{case}_grid"],
+                         g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, order, af)
+        assert abs(float(got[b]) - ref) <= 1e-5 * abs(ref)
+
+
+def test_scale_scatters_to_prompts_dropin(cuda_ok, tmp_path):
+    """Scaling.ScaleScattersToPrompts from the saved files equals the per-bin
+    BackProjectionScatterRandFit calls of the reference's loop."""
+    from opensss_gb300.BackProjection import BackProjectionScatterRandFit
+    from opensss_gb300.Scaling import ScaleScattersToPrompts
+
+    g = golden("fit")
+    nd, nr, af = (int(v) for v in g["case1_dims"])
+    lor, si, _ = _sino(nd, nr)
+    shp = g["case1_scatter"].shape
+    rng = np.random.default_rng(9)
+    bins = 3
+    prompts = rng.poisson(3.0, size=shp + (bins,)).astype(np.uint16)
+    lorcounts = np.full(shp, 1.0, np.float32)
+    np.savez_compressed(tmp_path / "PromptsSinogram.npz", prompts)
+    np.savez_compressed(tmp_path / "RandomsSinogram.npz", g["case1_randoms"])
+    np.save(tmp_path / "AttenuationMask.npy", (g["case1_mask"] >= 1).astype(np.uint8))
+    for b in range(bins):
+        np.savez_compressed(tmp_path / f"SSS_mashed_bin{b}", g["case1_scatter"] * (b + 1))
+    s = ScaleScattersToPrompts(si, lor, str(tmp_path), g["case1_grid"], g["case1_bounds"], g["case1_geometry"],
+                               np.array([]), af, False, lorcounts)
+    assert s.dtype == np.float32 and s.shape == (bins,)
+    order = si[:nr, :nr].T
+    for b in range(bins):
+        ref = BackProjectionScatterRandFit(prompts[..., b] / lorcounts, g["case1_scatter"] * (b + 1),
+                                           g["case1_randoms"], np.float32(g["case1_mask"] >= 1), g["case1_grid"],
+                                           g["case1_bounds"], g["case1_geometry"], lor, order, af)
+        assert abs(float(s[b]) - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
+    assert np.array_equal(np.load(tmp_path / "ScaleFactors.npy"), s)
