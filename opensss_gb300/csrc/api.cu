@@ -32,6 +32,7 @@ extern "C" int sss_abi_version(void) { return SSS300_ABI_VERSION; }
 extern "C" int sss_status_code(int32_t s)
 {
     using namespace sss;
+    s &= ~kNoteMapSigned;
     if (s == 0) return SSS_OK;
     if (s & kErrOverrun)
         return sss_set_error(SSS_ERR_OVERRUN,

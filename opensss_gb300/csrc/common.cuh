@@ -17,6 +17,9 @@ enum DeviceError : int32_t {
     kErrVoxel = 1 << 3,      // linear voxel index outside the volume (Nx != Ny case)
     kErrCapacity = 1 << 4,   // an internal list capacity was exceeded
     kErrEvent = 1 << 5,      // a list-mode event outside the sinogram tables (reference: IndexError)
+    // not an error: set by the tail mask's pre-pass when the map has a negative
+    // or NaN value (its line integrals can then shrink); sss_status_code ignores it
+    kNoteMapSigned = 1 << 30,
 };
 
 constexpr int kTofEntries = 8001;  // -4000..4000 ps, SingleScatterSimulationTOF.py:145-147

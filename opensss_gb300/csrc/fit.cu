@@ -142,6 +142,19 @@ struct MaskParams {
     int32_t* status;
 };
 
+constexpr double kDecided = 1e-6;  // far above the 2^-53 where 1/exp(-s) stops being 1
+
+// Pre-pass of the tail mask: notes a negative or NaN map value in the status word.
+__global__ void map_sign_kernel(const float* __restrict__ map, long long n, int32_t* status)
+{
+    bool signed_value = false;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float v = map[i];
+        if (!(v >= 0.f)) signed_value = true;
+    }
+    if (__syncthreads_or(signed_value) && threadIdx.x == 0) atomicOr(status, kNoteMapSigned);
+}
+
 __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
 {
     const long long n = (long long)(P.pairs ? P.npairs : P.nr * P.nr) * P.na * P.na;
@@ -157,13 +170,21 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
     if (ray_setup(P.g, lc, 1e-20, r)) {
         double sum = 0.0;
         bool bad = false;
+        // With a map of non-negative values the sum only grows: once it is
+        // above kDecided the mask value is fixed (1/exp(-s) != 1, activity > 0)
+        // and the remaining lengths need not be evaluated.  The walk itself
+        // always runs to the end, so an overrun is still reported.
+        const bool nonneg = !(*(volatile const int32_t*)P.status & kNoteMapSigned);
         int c = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
             const long long v = lin - 1;
             if (v < 0 || v >= P.nvox) {
                 bad = true;
                 return;
             }
-            sum = add64(sum, mul64((double)__ldg(P.mu + v), ref_length(r, t0, t1)));
+            // a zero voxel adds exactly +0 whatever its length, so the FP64
+            // length (the walk's dominant cost) is evaluated only where it counts
+            const float mu = __ldg(P.mu + v);
+            if (mu != 0.f && !(nonneg && sum > kDecided)) sum = add64(sum, mul64((double)mu, ref_length(r, t0, t1)));
         });
         if (c < 0) raise_error(P.status, kErrOverrun);
         if (bad) raise_error(P.status, kErrVoxel);
@@ -410,6 +431,11 @@ int tail_mask(const int32_t grid[3], const double bounds[6], const float* map, i
     P.status = status;
     const long long n = (long long)(pairs ? npairs : nr * nr) * P.na * P.na;
     if (n == 0) return SSS_OK;
+    if (!status) return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask: status word required");
+    const long long nb = (P.nvox + 255) / 256;
+    map_sign_kernel<<<(unsigned)(nb < 1024 ? nb : 1024), 256, 0, (cudaStream_t)stream>>>(map, P.nvox, status);
+    int rc = sss_check_launch("map_sign_kernel");
+    if (rc) return rc;
     mask_kernel<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(P);
     return sss_check_launch("mask_kernel");
 }

@@ -189,3 +189,20 @@ def test_scale_scatters_to_prompts_dropin(cuda_ok, tmp_path):
                                            g["case1_bounds"], g["case1_geometry"], lor, order, af)
         assert abs(float(s[b]) - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
     assert np.array_equal(np.load(tmp_path / "ScaleFactors.npy"), s)
+
+
+def test_tail_mask_with_signed_map_matches_oracle(cuda_ok):
+    """A map with negative values disables the early decision (the line
+    integral can shrink back); the mask still equals the FP64 oracle's."""
+    from opensss_gb300.TailsMask import MaskGenerator
+
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g["case0_dims"])
+    lor, si, _ = _sino(nd, nr)
+    mu = g["case0_mu"].copy()
+    rng = np.random.default_rng(4)
+    flip = rng.uniform(size=mu.shape) < 0.3
+    mu[flip] = -mu[flip]  # lines through both signs can cancel
+    m = MaskGenerator(np.ones_like(mu), mu, g["case0_bounds"], g["case0_geometry"], lor, si, True, af)
+    ref = O.mask(mu, g["case0_bounds"], g["case0_geometry"], lor, si, af)
+    assert np.array_equal(m, ref)
