@@ -62,8 +62,9 @@ def case_mask(reps):
 
 
 def case_fit(reps):
-    """Back-projection fit of seeded sinograms on a 380 x 40 scanner, AF 4."""
-    from .BackProjection import fit_device
+    """Back-projection fit of four TOF bins of seeded sinograms in one pass on
+    a 380 x 40 scanner, AF 4."""
+    from .BackProjection import fit_bins_device
 
     pr = W.config2()
     sc = W.ring_scanner(380, 40, radius_cm=41.0, ring_pitch_cm=0.64)
@@ -71,17 +72,17 @@ def case_fit(reps):
     shp = (381 * 190, 1600)
     g = torch.Generator(device="cuda")
     g.manual_seed(1)
-    prm = torch.poisson(torch.full(shp, 3.0, device="cuda"), generator=g)
+    prm = torch.poisson(torch.full((4,) + shp, 3.0, device="cuda"), generator=g)
     rnd = torch.full(shp, 0.3, device="cuda")
-    scat = torch.rand(shp, device="cuda", generator=g)
+    scat = torch.rand((4,) + shp, device="cuda", generator=g)
     mask = (torch.rand(shp, device="cuda", generator=g) < 0.3).to(torch.uint8)
     cell = np.arange(shp[0], dtype=np.int64) * shp[1]
     ring = np.arange(shp[1], dtype=np.int64)
     zr = float(sc.geometry[-1, 0, 2]) + 0.3
     bounds = np.array([pr.image_size[0], pr.image_size[1], -zr, pr.image_size[3], pr.image_size[4], zr])
     for _ in range(reps):
-        fit_device(prm, rnd, mask, scat, cell, ring, np.array([40, 40, 26]), bounds, sc.geometry, lor,
-                   si[:40, :40].T, 4)
+        fit_bins_device(prm, rnd, mask, scat, shp[0] * shp[1], cell, ring, np.array([40, 40, 26]), bounds,
+                        sc.geometry, lor, si[:40, :40].T, 4)
 
 
 def case_listmode(reps):
