@@ -285,3 +285,40 @@ def upsample_bin(sampled_bin, nru, ndu, nr, nd, lut, ringmap, sino_index):
     lib().orc_upsample_bin(_p(s), C.c_int64(nru), C.c_int64(ndu), C.c_int64(nr), C.c_int64(nd),
                            _p(lut), _p(rm), _p(si), _p(out))
     return out
+
+
+def mask_pairs(mu, image_size, geometry, lor, pairs, nslices, af, nthreads=0, use_activity=False):
+    """Span tail mask on the expanded geometry (TailsMask.py:230-377)."""
+    grid = np.ascontiguousarray(mu.shape, dtype=np.int64)
+    muf = np.ascontiguousarray(mu.flatten(order="F"), dtype=np.float32)
+    gb = np.ascontiguousarray(image_size, dtype=np.float64)
+    geom = np.ascontiguousarray(geometry, dtype=np.float64)
+    lor = np.ascontiguousarray(lor, dtype=np.int16)
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+    nr, nd = geom.shape[:2]
+    out = np.zeros((nd + 1, nd // 2, nslices), np.uint8)
+    st = lib().orc_mask_pairs(_p(grid), _p(muf), _p(gb), C.c_int64(nr), C.c_int64(nd), _p(geom), _p(lor),
+                              _p(pairs), C.c_int64(pairs.shape[0]), C.c_int64(nslices), C.c_int64(af),
+                              C.c_int(int(use_activity)), _p(out), C.c_int(nthreads))
+    if st:
+        raise RuntimeError(f"oracle span mask failed {st}")
+    return out
+
+
+def fit_pairs(prompts, scatters, randoms, mask_f32, grid, bounds, geometry, lor, pairs, af, nthreads=0):
+    """Span scale fit, length-weighted (BackProjection.py:217-393)."""
+    grid = np.ascontiguousarray(grid, dtype=np.int64)
+    gb = np.ascontiguousarray(bounds, dtype=np.float64)
+    geom = np.ascontiguousarray(geometry, dtype=np.float64)
+    lor = np.ascontiguousarray(lor, dtype=np.int16)
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+    nr, nd = geom.shape[:2]
+    f = [np.ascontiguousarray(a, dtype=np.float32) for a in (prompts, scatters, randoms, mask_f32)]
+    nslices = f[0].shape[2]
+    out = np.zeros(1, np.float32)
+    st = lib().orc_fit_pairs(_p(grid), _p(gb), C.c_int64(nr), C.c_int64(nd), _p(geom), _p(lor), _p(pairs),
+                             C.c_int64(pairs.shape[0]), C.c_int64(nslices), C.c_int64(af), _p(f[0]), _p(f[1]),
+                             _p(f[2]), _p(f[3]), _p(out), C.c_int(nthreads))
+    if st:
+        raise RuntimeError(f"oracle span fit failed {st}")
+    return out

@@ -630,6 +630,146 @@ int orc_fit(const int64_t *grid, const double *gb, int64_t nr, int64_t nd, const
     return status;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Span variants: MaskDetectorsMashing (TailsMask.py:230-309) and
+ * BackProjectionMashing + BackProjectionScatterRandFitMashing
+ * (BackProjection.py:217-393).  Each mashed sinogram i is traced at the ring
+ * pair pairs[3i], pairs[3i+1] of the expanded geometry `geom` (nr rings) and
+ * reads / writes slice pairs[3i+2] of [(nd+1)][nd/2][nslices] sinograms.  The
+ * back-projection weights each voxel by len / sum(len) (:294-297) and the
+ * per-sinogram images are summed in sinogram order (:381-385). */
+int orc_mask_pairs(const int64_t *grid, const float *mu, const double *gb, int64_t nr, int64_t nd,
+                   const double *geom, const int16_t *lor, const int32_t *pairs, int64_t npairs,
+                   int64_t nslices, int64_t af, int use_activity, uint8_t *out, int nthreads)
+{
+    const int64_t nang = nd / 2;
+    const int cap = (int)(grid[0] + grid[1] + grid[2]);
+    int status = 0;
+    memset(out, 0, (size_t)(nd + 1) * nang * nslices);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int64_t i = 0; i < npairs; ++i) {
+        const int64_t ring1 = pairs[3 * i], ring2 = pairs[3 * i + 1], slice = pairs[3 * i + 2];
+        double *len = (double *)malloc(sizeof(double) * cap);
+        int32_t *ix = (int32_t *)malloc(sizeof(int32_t) * cap);
+        double *sm = (double *)malloc(sizeof(double) * cap);
+        const double z1 = geom[3 * (ring1 * nd) + 2], z2 = geom[3 * (ring2 * nd) + 2];
+        for (int64_t d1 = 0; d1 < nd; d1 += af) {
+            const double *p1 = geom + 3 * (ring1 * nd + d1);
+            for (int64_t d2 = 0; d2 < nd; d2 += af) {
+                if ((d1 == d2 && ring2 == ring1) || d1 > d2) continue;
+                const double *p2 = geom + 3 * (ring2 * nd + d2);
+                int64_t ang = lor[(d1 * nd + d2) * 2 + 0];
+                int64_t rad = lor[(d1 * nd + d2) * 2 + 1];
+                double lc[6] = {p1[0], p1[1], z1, p2[0], p2[1], z2};
+                int n = orc_trace(grid, gb, lc, 1e-20, len, ix, sm, cap);
+                if (n < 0) { status = -3; continue; }
+                if (!orc_indices_ok(ix, n, grid[0] * grid[1] * grid[2])) { status = -6; continue; }
+                double att = 1;
+                if (n != 0) {
+                    double s = 0;
+                    for (int k = 0; k < n; ++k) s += (double)mu[ix[k] - 1] * len[k];
+                    att = use_activity ? (s > 0 ? 0.0 : 1.0) : 1 / exp(-s);  /* :289-301 */
+                }
+                if (att != 1) att = 0;
+                uint8_t *cell = out + ((rad * nang + ang) * nslices + slice);
+                *cell = (uint8_t)(*cell + (uint8_t)att);
+            }
+        }
+        free(len);
+        free(ix);
+        free(sm);
+    }
+    return status;
+}
+
+int orc_fit_pairs(const int64_t *grid, const double *gb, int64_t nr, int64_t nd, const double *geom,
+                  const int16_t *lor, const int32_t *pairs, int64_t npairs, int64_t nslices, int64_t af,
+                  const float *prompts, const float *scatters, const float *randoms, const float *mask,
+                  float *scale_out, int nthreads)
+{
+    const int64_t nang = nd / 2;
+    const int64_t nvox = grid[0] * grid[1] * grid[2];
+    const int cap = (int)(grid[0] + grid[1] + grid[2]);
+    int status = 0;
+    float *part = (float *)calloc((size_t)npairs * 4 * nvox, sizeof(float));
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int64_t i = 0; i < npairs; ++i) {
+        const int64_t ring1 = pairs[3 * i], ring2 = pairs[3 * i + 1], slice = pairs[3 * i + 2];
+        float *iP = part + (size_t)i * 4 * nvox, *iS = iP + nvox, *iR = iS + nvox, *iN = iR + nvox;
+        double *len = (double *)malloc(sizeof(double) * cap);
+        int32_t *ix = (int32_t *)malloc(sizeof(int32_t) * cap);
+        double *sm = (double *)malloc(sizeof(double) * cap);
+        const double z1 = geom[3 * (ring1 * nd) + 2], z2 = geom[3 * (ring2 * nd) + 2];
+        for (int64_t d1 = 0; d1 < nd; d1 += af) {
+            const double *p1 = geom + 3 * (ring1 * nd + d1);
+            for (int64_t d2 = 0; d2 < nd; d2 += af) {
+                if ((d1 == d2 && ring2 == ring1) || d1 > d2) continue;
+                int64_t ang = lor[(d1 * nd + d2) * 2 + 0];
+                int64_t rad = lor[(d1 * nd + d2) * 2 + 1];
+                size_t c = (size_t)((rad * nang + ang) * nslices + slice);
+                float m = mask[c];
+                float sv = m * scatters[c];
+                if (sv == 0) continue;
+                float pv = m * prompts[c], rv = m * randoms[c];
+                const double *p2 = geom + 3 * (ring2 * nd + d2);
+                double lc[6] = {p1[0], p1[1], z1, p2[0], p2[1], z2};
+                int n = orc_trace(grid, gb, lc, 1e-20, len, ix, sm, cap);
+                if (n < 0) { status = -3; continue; }
+                if (!orc_indices_ok(ix, n, nvox)) { status = -6; continue; }
+                if (n > 0) {
+                    /* value * Lengths / np.sum(Lengths) in FP64, added to the FP32
+                     * image and rounded back (numpy sums pairwise; the sequential
+                     * sum differs from it in the last bits only) */
+                    double total = 0;
+                    for (int k = 0; k < n; ++k) total += len[k];
+                    for (int k = 0; k < n; ++k) {
+                        int64_t v = ix[k] - 1;
+                        iP[v] = (float)((double)iP[v] + (double)pv * len[k] / total);
+                        iS[v] = (float)((double)iS[v] + (double)sv * len[k] / total);
+                        iR[v] = (float)((double)iR[v] + (double)rv * len[k] / total);
+                        iN[v] = iN[v] + 1.0f;
+                    }
+                }
+            }
+        }
+        free(len);
+        free(ix);
+        free(sm);
+    }
+    float *tot = (float *)calloc((size_t)4 * nvox, sizeof(float));
+    for (int64_t i = 0; i < npairs; ++i) {
+        const float *src = part + (size_t)i * 4 * nvox;
+        for (int64_t k = 0; k < 4 * nvox; ++k) tot[k] = tot[k] + src[k];
+    }
+    double sxt = 0, sxx = 0;
+    for (int64_t v = 0; v < nvox; ++v) {
+        /* S / (sens + 1e-15) in float32 (:358-369): the 1e-15 only matters where sens is 0 */
+        float sens = tot[3 * nvox + v] + 1e-15f;
+        float sb = tot[nvox + v] / sens;
+        float ab = tot[v] / sens;
+        float rb = tot[2 * nvox + v] / sens;
+        if (isnan(sb) || isinf(sb)) sb = 0;
+        if (isnan(ab) || isinf(ab)) ab = 0;
+        if (isnan(rb) || isinf(rb)) rb = 0;
+        float tl = ab - rb;
+        if (tl < 0) tl = 0;
+        float x = (float)((double)sb * 1e10);
+        sxt += (double)x * (double)tl;
+        sxx += (double)x * (double)x;
+    }
+    double a = (sxx > 0) ? sxt / sxx : 0.0;
+    *scale_out = (float)((double)(float)a * 1e10);
+    free(tot);
+    free(part);
+    return status;
+}
+
 /* InterpolateAllBins gather (Interpolation.py:197-319) given the nearest
  * source tables: lut[rad*nang+ang] = griddata point index p (p = a*ndu + b,
  * a/b indexing the sampled detectors of the two rings), ringmap[r] = nearest

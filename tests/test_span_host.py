@@ -88,3 +88,27 @@ def test_span_upsampling_tables_reproduce_reference(layout):
         assert np.array_equal(vb.reshape(nd + 1, nd // 2, -1), g["up_bins"][b])
         total += vb
     assert np.array_equal(total.reshape(nd + 1, nd // 2, -1), g["up_sum"])
+
+
+@pytest.mark.parametrize("ci", range(2))
+def test_oracle_span_mask_and_fit_match_reference(ci):
+    """The C oracle's span mask (bit-exact, both rules) and length-weighted
+    fit (1e-5) against the reference's outputs."""
+    from opensss_gb300 import geometry as G
+
+    g = golden("span")
+    nd, nr, span, af = (int(v) for v in g[f"case{ci}_dims"])
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    si, _, _, _ = G.SinogramLUT(nr, span, nr - 1)
+    eg, _ = G.expandRings(g[f"case{ci}_geometry"], np.zeros_like(g[f"case{ci}_geometry"]))
+    pairs = G.span_ring_pairs(si)
+    m = O.mask_pairs(g[f"case{ci}_mu"], g[f"case{ci}_bounds"], eg, lor, pairs, si.shape[0], af)
+    assert np.array_equal(m, g[f"case{ci}_mask"])
+    ma = O.mask_pairs(g[f"case{ci}_act"], g[f"case{ci}_bounds"], eg, lor, pairs, si.shape[0], af,
+                      use_activity=True)
+    assert np.array_equal(ma, g[f"case{ci}_mask_activity"])
+    s = O.fit_pairs(g[f"case{ci}_prompts"], g[f"case{ci}_scatter"], g[f"case{ci}_randoms"],
+                    np.float32(g[f"case{ci}_mask"] >= 1), g[f"case{ci}_grid"], g[f"case{ci}_fit_bounds"], eg, lor,
+                    pairs, af)
+    ref = float(g[f"case{ci}_scale"][0])
+    assert abs(float(s[0]) - ref) <= 1e-5 * abs(ref)
