@@ -448,7 +448,60 @@ def run_batch(dev, args, att):
     b.close()
     del b
     torch.cuda.empty_cache()
+    res["small_instances"] = _small_batch(dev, args, att)
     return res
+
+
+def _small_batch(dev, args, att):
+    """64 bed positions of the plain non-TOF size (40x40x20 @ 1 cm, 8 x 32
+    virtual, phantoms seeded per bed): one graph replay of the batch against
+    the same problems one after another through TofSSS.run_flat."""
+    import torch
+
+    from opensss_gb300 import TofSSS, workloads as W
+    from opensss_gb300.batch import BatchSSS
+    from opensss_gb300.engine import fortran_flat
+
+    inst = [W.config1(seed=100 + i) for i in range(64)]
+    pr0 = inst[0]
+    e = TofSSS(pr0.scanner.geometry, pr0.scanner.normals, pr0.scanner.detector_size_mm, att,
+               pr0.energy_resolution, pr0.energy_threshold, pr0.nr_rings_used, pr0.nr_detectors_used,
+               pr0.sample_step, pr0.tof_resolution, pr0.tof_range, pr0.nr_bins, device=dev)
+    jobs = [(e, fortran_flat(pr.activity, dev), fortran_flat(pr.attenuation, dev), pr.image_size, pr.grid)
+            for pr in inst]
+    b = BatchSSS(jobs)
+    b.run()
+    b.capture()
+    st = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        b.replay(check=False)
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.replay(check=False)
+        e1.record(st)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    b.replay(check=True)
+    for (_, a, m, size, shape) in jobs[:4]:
+        e.run_flat(a, m, shape, size, check=False)  # warm-up of the plain path
+    plain = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for (_, a, m, size, shape) in jobs:
+            e.run_flat(a, m, shape, size, check=False)
+        torch.cuda.synchronize(dev)
+        plain.append((time.perf_counter() - t0) * 1e3)
+    mean_ms, plain_ms = statistics.mean(ms), statistics.mean(plain)
+    out = {"workload": "64 plain non-TOF beds, 40x40x20 @ 1 cm, 8 x 32 virtual", "units_per_step": b.units,
+           "waves": b.waves, "launches_per_step": b.launches, "ms_per_step": mean_ms,
+           "value": b.units / (mean_ms / 1e3), "plain_sequential_ms": plain_ms,
+           "plain_note": "wall time of 64 TofSSS.run_flat calls (each synchronises once for its scatter points)",
+           "speedup_vs_plain": plain_ms / mean_ms}
+    b.close()
+    return out
 
 
 def run_precision(dev, args, att):

@@ -99,6 +99,14 @@ typedef struct sss_tof_problem {
  * (the reference sums them in FP32 too, :551).  Honoured by sss_tof_run;
  * sss_batch_* always uses the plain reduction. */
 #define SSS_FLAG_KAHAN 1
+/* sss_tof_problem.flags.  SSS_FLAG_UNIT_TOF: the caller asserts that every
+ * tof_log2w entry is (0, 0), i.e. one bin whose normalised TOF weight is
+ * exactly 1 at every offset (the non-TOF SingleScatterSimulation, a kernel
+ * of 1e6 ps).  Each pair then takes its legs' activity integrals instead of
+ * walking their voxels (the reference's dot product with a row of ones,
+ * :521-522), and no voxel lists are built.  Honoured by sss_tof_run and
+ * sss_batch_*; the Python engine sets it when its table has that form. */
+#define SSS_FLAG_UNIT_TOF 2
 
 /* Scatter points on the SampleStep lattice with mu > 0, z-slice major, in the
  * reference's order (:182, :381-394).  points (device) receives [count][4]

@@ -56,6 +56,7 @@ class TofProblem(C.Structure):
 
 
 SSS_FLAG_KAHAN = 1
+SSS_FLAG_UNIT_TOF = 2
 
 
 class ListmodeLayout(C.Structure):

@@ -150,7 +150,8 @@ size_t item_bytes(const sss_tof_problem& p, long long npts)
 {
     const long long nl = (long long)p.nru * p.ndu;
     const long long cap = (long long)p.nx + p.ny + p.nz;
-    return 2 * align256(sizeof(float4) * npts * nl) + align256(sizeof(float2) * npts * nl * cap);
+    const size_t lists = (p.flags & SSS_FLAG_UNIT_TOF) ? 0 : align256(sizeof(float2) * npts * nl * cap);
+    return 2 * align256(sizeof(float4) * npts * nl) + lists;
 }
 
 }  // namespace
@@ -387,8 +388,12 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
             doff += align256(sizeof(float4) * it.count * nl);
             L.p.legB = (float4*)(ws + doff);
             doff += align256(sizeof(float4) * it.count * nl);
-            L.p.vox = (float2*)(ws + doff);
-            doff += align256(sizeof(float2) * it.count * nl * cap);
+            if (p.flags & SSS_FLAG_UNIT_TOF) {
+                L.p.vox = nullptr;  // every TOF weight is 1: the pairs use the leg integrals
+            } else {
+                L.p.vox = (float2*)(ws + doff);
+                doff += align256(sizeof(float2) * it.count * nl * cap);
+            }
             L.p.status = status;
             L.thread_begin = W.threads;
             W.threads += it.count * nl;
@@ -430,6 +435,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
                 C.legA = hleg[j].p.legA;
                 C.legB = hleg[j].p.legB;
                 C.vox = hleg[j].p.vox;
+                C.unit_tof = (p.flags & SSS_FLAG_UNIT_TOF) != 0;
                 C.out = outs[it.prob];
                 P.npts = (int)it.count;
                 P.nchunks = pair_chunks(p.nru, p.ndu);

@@ -23,7 +23,7 @@ struct LegParams {
     int npts;
     float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
     float4* legB;   // [npts][nl]: unit vector to the crystal, voxel-list length (int bits)
-    float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major
+    float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major; null: no lists
     int32_t* status;
 };
 
@@ -52,7 +52,7 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
         const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
         const float inv_c = (float)(1.0 / kLightCmPerPs);
         const double t0 = r.tmin;
-        float2* out = P.vox + ((long long)s * P.nl + l) * P.cap;
+        float2* out = P.vox ? P.vox + ((long long)s * P.nl + l) * P.cap : nullptr;
         int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
             long long v = lin - 1;
             if (v < 0 || v >= P.nvox) {
@@ -67,7 +67,7 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
             float a = __ldg(P.act + v) * len;
             musum = fmaf(__ldg(P.mu + v), len, musum);
             asum += a;
-            if (a != 0.f) {
+            if (a != 0.f && out) {
                 // sample = half the distance walked to the voxel's exit (:155-156)
                 float rho = vlen * (float)(tb - t0) * inv_c;
                 out[nlist] = make_float2(a, rho);

@@ -48,6 +48,7 @@ struct PairCtx {
     const float4* legB;
     const float2* vox;       // [point][nl][cap]
     float* out;              // [nbins][nl][nl]
+    int unit_tof;            // one bin, every TOF weight exactly 1: AB = the leg's activity integral
 };
 
 // Launch constants of a problem's TOF table (:98, :282) and Watson factors.
@@ -256,7 +257,10 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
         }
         // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
         const float u = fmaf(A1.x - A2.x, inv_c, 4000.5f);
-        if (__any_sync(0xffffffffu, c != 0.f)) {
+        if (SINGLE && C.unit_tof) {
+            // weights of exactly 1: sum(a_v * 1) is the walking leg's activity integral
+            acc[0].x = fmaf(c, Aw.y, acc[0].x);
+        } else if (__any_sync(0xffffffffu, c != 0.f)) {
             const int nw = __float_as_int(Bw.w);
             if (c != 0.f) walked += nw;
             const float2* vw = C.vox + (lo + lw) * C.cap;

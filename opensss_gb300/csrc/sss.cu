@@ -181,8 +181,8 @@ WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
     off = align_up(off + sizeof(float4) * wave_points * nl);
     w.legB = off;
     off = align_up(off + sizeof(float4) * wave_points * nl);
-    w.vox = off;
-    off = align_up(off + sizeof(float2) * wave_points * cap * nl);
+    w.vox = off;  // no voxel lists when every TOF weight is 1
+    if (!(p.flags & SSS_FLAG_UNIT_TOF)) off = align_up(off + sizeof(float2) * wave_points * cap * nl);
     w.counter = off;
     off = align_up(off + 256);
     w.total = off;
@@ -202,6 +202,8 @@ int validate(const sss_tof_problem* p)
     if (p->sample_step[0] < 1 || p->sample_step[1] < 1 || p->sample_step[2] < 1)
         return sss_set_error(SSS_ERR_INVALID, "sample_step must be >= 1");
     if (p->nbins < 1 || p->nbins > 64) return sss_set_error(SSS_ERR_INVALID, "nbins must be 1..64");
+    if ((p->flags & SSS_FLAG_UNIT_TOF) && p->nbins != 1)
+        return sss_set_error(SSS_ERR_INVALID, "SSS_FLAG_UNIT_TOF needs nbins == 1");
     if (!(p->image_size[3] > p->image_size[0] && p->image_size[4] > p->image_size[1] &&
           p->image_size[5] > p->image_size[2]))
         return sss_set_error(SSS_ERR_INVALID, "image_size must satisfy max > min");
@@ -324,7 +326,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     LP.nvox = (long long)p->nx * p->ny * p->nz;
     LP.legA = (float4*)(ws + w.legA);
     LP.legB = (float4*)(ws + w.legB);
-    LP.vox = (float2*)(ws + w.vox);
+    LP.vox = (p->flags & SSS_FLAG_UNIT_TOF) ? nullptr : (float2*)(ws + w.vox);
     LP.status = status;
 
     PairParams PP;
@@ -345,6 +347,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     C.legA = LP.legA;
     C.legB = LP.legB;
     C.vox = LP.vox;
+    C.unit_tof = (p->flags & SSS_FLAG_UNIT_TOF) != 0;
     C.out = out;
     PP.T = tof_const(*p);
     PP.tof_log2w = p->tof_log2w;

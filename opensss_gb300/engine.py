@@ -72,8 +72,10 @@ class TofSSS:
         self.normals = as_device(np.asarray(NormalVectors, dtype=np.float64), torch.float64, dev)
         self.rings = as_device(self.rings_np, torch.int32, dev)
         self.dets = as_device(self.dets_np, torch.int32, dev)
-        self.tof_log2w = as_device(tables.tof_log2_table(self.nbins, self.tof_range,
-                                                         self.tof_resolution), torch.float32, dev)
+        log2w = tables.tof_log2_table(self.nbins, self.tof_range, self.tof_resolution)
+        # one bin whose normalised weight is exactly 1 everywhere (the non-TOF case)
+        self.unit_tof = self.nbins == 1 and not np.any(log2w)
+        self.tof_log2w = as_device(log2w, torch.float32, dev)
         self.eff = as_device(tables.pair_efficiency_f32(att, float(EnergyThreshold),
                                                         float(EnergyResolution)), torch.float32, dev)
         self.ratio = as_device(tables.attenuation_ratio(att), torch.float32, dev)
@@ -81,9 +83,13 @@ class TofSSS:
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
 
     # ------------------------------------------------------------------
-    def problem(self, act_flat, mu_flat, shape, image_size, kahan: bool = False) -> _lib.TofProblem:
+    def problem(self, act_flat, mu_flat, shape, image_size, kahan: bool = False,
+                unit_tof: bool | None = None) -> _lib.TofProblem:
+        """``unit_tof`` None: use the leg integrals when the TOF table is all
+        ones (``self.unit_tof``); False forces the voxel walk."""
         p = _lib.TofProblem()
-        p.flags = _lib.SSS_FLAG_KAHAN if kahan else 0
+        unit = self.unit_tof if unit_tof is None else (unit_tof and self.unit_tof)
+        p.flags = (_lib.SSS_FLAG_KAHAN if kahan else 0) | (_lib.SSS_FLAG_UNIT_TOF if unit else 0)
         p.nx, p.ny, p.nz = (int(s) for s in shape)
         p.activity = act_flat.data_ptr()
         p.attenuation = mu_flat.data_ptr()
@@ -122,7 +128,7 @@ class TofSSS:
 
     def run(self, ActivityMap, AttenuationMap, ImageSize, max_points: int | None = None,
             wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
-            check: bool = True, kahan: bool = False) -> torch.Tensor:
+            check: bool = True, kahan: bool = False, unit_tof: bool | None = None) -> torch.Tensor:
         """Sampled scatter sinogram, leg-pair layout [B, NL, NL] float32 (CUDA).
 
         ``max_points`` restricts the run to the first scatter points in
@@ -134,15 +140,15 @@ class TofSSS:
         act = fortran_flat(ActivityMap, dev)
         mu = fortran_flat(AttenuationMap, dev)
         return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, stream, check,
-                             kahan)
+                             kahan, unit_tof)
 
     def run_flat(self, act, mu, shape, ImageSize, max_points: int | None = None,
                  wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
-                 check: bool = True, kahan: bool = False) -> torch.Tensor:
+                 check: bool = True, kahan: bool = False, unit_tof: bool | None = None) -> torch.Tensor:
         """``run`` on device-resident maps already flattened in Fortran order
         (float32, Nx*Ny*Nz)."""
         dev = self.device
-        p = self.problem(act, mu, shape, ImageSize, kahan)
+        p = self.problem(act, mu, shape, ImageSize, kahan, unit_tof)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         pts, counts = self.scatter_points(p, st)
         if max_points is not None:

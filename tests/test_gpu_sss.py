@@ -168,3 +168,17 @@ def test_kahan_on_config4_sample(cuda_ok, att_table):
     ref = _oracle_compact(pr, att_table, sp_end=6)
     assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
+
+
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_c1"])
+def test_unit_tof_fast_path_matches_voxel_walk(cuda_ok, att_table, name):
+    """With one bin of unit weights the pairs take the legs' activity
+    integrals instead of walking the voxels: same sinogram to FP32 rounding."""
+    g = golden(name)
+    pr = problem_from_golden(g)
+    eng = _engine(pr, att_table)
+    assert eng.unit_tof
+    fast = eng.run(pr.activity, pr.attenuation, pr.image_size).cpu().numpy()
+    walk = eng.run(pr.activity, pr.attenuation, pr.image_size, unit_tof=False).cpu().numpy()
+    assert rel_l2(fast, walk) < 1e-6
+    assert_same_support(fast, walk)

@@ -120,3 +120,14 @@ def test_upsample_gather_tables_reproduce_reference(case, layout):
         assert np.array_equal(vb.reshape(nd + 1, nd // 2, nr * nr), g[f"case{case}_bins"][b])
         total += vb
     assert np.array_equal(total.reshape(nd + 1, nd // 2, nr * nr), g[f"case{case}_sum"])
+
+
+def test_unit_tof_table_detection():
+    """One bin with a 1e6 ps kernel: every normalised weight is exactly 1, so
+    the table is all (0, 0) and the engine may use the leg integrals; a real
+    timing kernel or more bins never give that form."""
+    from opensss_gb300 import tables
+
+    assert not np.any(tables.tof_log2_table(1, 1000.0, 1.0e6))
+    assert np.any(tables.tof_log2_table(1, 1000.0, 214.0))
+    assert np.any(tables.tof_log2_table(3, 1000.0, 1.0e6))
