@@ -175,6 +175,7 @@ def run_ours(args, rank, world, local_rank):
 
     from opensss_gb300 import TofSSS, _lib
     from opensss_gb300.engine import fortran_flat, leg_pair_to_compact
+    from opensss_gb300.replicas import max_over_ranks
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
@@ -230,11 +231,7 @@ def run_ours(args, rank, world, local_rank):
         barrier()
     _lib.check_status(int(eng._status.item()))
     clocks = clk.summary()
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dev)
     value = world * units * args.steps / total_s
 
     # ---- end to end through the public API, host buffers, copies inside
@@ -252,11 +249,7 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
         if i >= args.warmup:
             e2e_s.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_s)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = max_over_ranks(sum(e2e_s), dev)
     e2e_value = world * units * args.steps / e2e_total
     h2d = act_h.numel() * 4 + mu_h.numel() * 4
     d2h = res_h.numel() * 4

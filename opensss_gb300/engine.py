@@ -128,7 +128,8 @@ class TofSSS:
 
     def run(self, ActivityMap, AttenuationMap, ImageSize, max_points: int | None = None,
             wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
-            check: bool = True, kahan: bool = False, unit_tof: bool | None = None) -> torch.Tensor:
+            check: bool = True, kahan: bool = False, unit_tof: bool | None = None,
+            slice_range=None) -> torch.Tensor:
         """Sampled scatter sinogram, leg-pair layout [B, NL, NL] float32 (CUDA).
 
         ``max_points`` restricts the run to the first scatter points in
@@ -140,17 +141,27 @@ class TofSSS:
         act = fortran_flat(ActivityMap, dev)
         mu = fortran_flat(AttenuationMap, dev)
         return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, stream, check,
-                             kahan, unit_tof)
+                             kahan, unit_tof, slice_range)
 
     def run_flat(self, act, mu, shape, ImageSize, max_points: int | None = None,
                  wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
-                 check: bool = True, kahan: bool = False, unit_tof: bool | None = None) -> torch.Tensor:
+                 check: bool = True, kahan: bool = False, unit_tof: bool | None = None,
+                 slice_range=None) -> torch.Tensor:
         """``run`` on device-resident maps already flattened in Fortran order
-        (float32, Nx*Ny*Nz)."""
+        (float32, Nx*Ny*Nz).  ``slice_range`` = (a, b) keeps the sampled
+        z-slices a..b-1 only (a shard: the slice terms add up, :201)."""
         dev = self.device
         p = self.problem(act, mu, shape, ImageSize, kahan, unit_tof)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         pts, counts = self.scatter_points(p, st)
+        if slice_range is not None:
+            # whole sampled z-slices [a, b): the points of the other slices are dropped
+            a, b = (int(v) for v in slice_range)
+            first = int(counts[:a].sum())
+            keep = np.zeros_like(counts)
+            keep[a:b] = counts[a:b]
+            pts = pts[first:first + int(keep.sum())]
+            counts = keep
         if max_points is not None:
             keep = np.minimum(counts, np.maximum(0, max_points - np.concatenate([[0], np.cumsum(counts)[:-1]])))
             counts = keep
