@@ -63,7 +63,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB)
     float* sY = smem;
     unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
+    float* sG = smem + kSmemGFloats;
     load_tof_table(tof_log2w, sY, sN);
+    if (T.factored) load_g_table(T, sG);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     bool tof_bad = false, energy_bad = false;
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB)
         const PairItem& it = items[lo];
         const int rem = (int)(task - it.task_begin);
         walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sY,
-                                          sN, vbuf, nullptr, tof_bad, energy_bad, walked, npairs);
+                                          sN, sG, vbuf, nullptr, tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
 }

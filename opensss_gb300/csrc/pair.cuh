@@ -17,8 +17,12 @@ constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
 constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
 static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
-// Kahan running sums and compensations: float2 [2 * NP][threads], after the voxel buffers
-constexpr int kSmemKahanFloats = kSmemVbufFloats + 2 * 32 * kPairWarps;
+// Gaussian factors 2^(-gamma (n-b)^2) of the factored weights: [n][b], rows of
+// kGRow floats (at most 64 bins), after the voxel buffers
+constexpr int kGRow = 64;
+constexpr int kSmemGFloats = kSmemVbufFloats + 2 * 32 * kPairWarps;
+// Kahan running sums and compensations: float2 [2 * NP][threads], after the G table
+constexpr int kSmemKahanFloats = kSmemGFloats + 64 * kGRow;
 
 // Dynamic shared memory of a pair launch; kahan_np = bin pairs of a
 // Kahan-compensated launch, 0 otherwise.
@@ -31,6 +35,8 @@ inline size_t pair_smem_bytes(int kahan_np = 0)
 struct TofConst {
     float s0, w;           // first bin centre offset and bin width (ps)
     float kappa2w, gamma;  // 2 kappa w and kappa w^2, kappa = 4/FWHM^2 (log2 units)
+    int factored;          // weights as 2^(Y - n beta) r^b G[n][b] (see accumulate_voxel)
+    int nbins;
 };
 
 // Everything one task needs about its problem and z-slice.
@@ -61,6 +67,12 @@ inline TofConst tof_const(const sss_tof_problem& p)
     T.w = (float)w;
     T.kappa2w = (float)(2.0 * kappa * w);
     T.gamma = (float)(kappa * w * w);
+    // The factored form multiplies powers of 2^beta: every product stays below
+    // 2^127 when gamma (B-1) < 100 (in-span offsets, |beta| <= gamma) and
+    // w / FWHM < 1.33 (offsets whose column is still above 2^-126 have
+    // beta < 45 w / FWHM, so r^2 = 2^(2 beta) < 2^120).
+    T.factored = p.nbins > 1 && (kappa * w * w) * (p.nbins - 1) < 100.0 && w / p.tof_resolution < 1.33;
+    T.nbins = p.nbins;
     return T;
 }
 inline float geo_const(const sss_tof_problem& p)
@@ -82,6 +94,16 @@ __device__ __forceinline__ void load_tof_table(const float* g, float* sY, unsign
     for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
         sY[i] = g[2 * i];
         sN[i] = (unsigned char)g[2 * i + 1];
+    }
+}
+
+// G[n][b] = 2^(-gamma (n - b)^2) for the bins of a launch (0 past the last bin).
+__device__ __forceinline__ void load_g_table(const TofConst& T, float* sG)
+{
+    for (int i = threadIdx.x; i < T.nbins * kGRow; i += blockDim.x) {
+        const int n = i / kGRow, b = i % kGRow;
+        const float d = (float)(n - b);
+        sG[i] = b < T.nbins ? exp2f(-T.gamma * d * d) : 0.f;
     }
 }
 
@@ -121,7 +143,7 @@ static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int 
 // at a time through packed FP32x2 instructions; NP = number of bin pairs.
 template <int NP, bool SINGLE, bool ODD>
 __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
-                                                 const float* sY, const unsigned char* sN,
+                                                 const float* sY, const unsigned char* sN, const float* sG,
                                                  const TofConst& T, bool& tof_bad)
 {
     // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
@@ -143,6 +165,24 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
     const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));
     if constexpr (SINGLE) {
         acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(T.gamma, n, beta), Y)), acc[0].x);
+    } else if (T.factored) {
+        // w_b = 2^(Y - (n-b) beta - gamma (n-b)^2) = [2^(Y - n beta) r^b] G[n][b],
+        // r = 2^beta: two 2^x per voxel, then two multiplies per bin
+        // (ca times the power of r carried along: one FFMA2 and one FMUL2 per bin pair)
+        const float r = ex2(beta);
+        float2 P2 = make_float2(ca * ex2(fmaf(-n, beta, Y)), 0.f);
+        P2.y = P2.x * r;
+        const float r2 = r * r;
+        const float2 R2 = make_float2(r2, r2);
+        const float4* G4 = reinterpret_cast<const float4*>(sG + (int)n * kGRow);
+        float4 g4;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            if ((k & 1) == 0) g4 = G4[k >> 1];
+            const float2 g2 = (k & 1) ? make_float2(g4.z, g4.w) : make_float2(g4.x, g4.y);
+            acc[k] = __ffma2_rn(P2, g2, acc[k]);
+            if (k + 1 < NP) P2 = __fmul2_rn(P2, R2);
+        }
     } else {
         const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
         const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-T.gamma, -T.gamma);
@@ -171,7 +211,8 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
 template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int s_first, int s_count,
                                           int lw, int chunk, int lane, const float* sY, const unsigned char* sN,
-                                          float2* vbuf, float2* kahan, bool& tof_bad, bool& energy_bad,
+                                          const float* sG, float2* vbuf, float2* kahan, bool& tof_bad,
+                                          bool& energy_bad,
                                           unsigned long long& walked, unsigned long long& npairs)
 {
     const float inv_c = (float)(1.0 / kLightCmPerPs);
@@ -273,7 +314,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
 #pragma unroll 2
                     for (int j = 0; j < jn; ++j) {
                         const float2 v = vbuf[j];
-                        accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sY, sN,
+                        accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sY, sN, sG,
                                                           T, tof_bad);
                     }
                 }

@@ -34,7 +34,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
     unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
     float2* kahan = reinterpret_cast<float2*>(smem + kSmemKahanFloats) + threadIdx.x;
+    float* sG = smem + kSmemGFloats;
     load_tof_table(P.tof_log2w, sY, sN);
+    if (P.T.factored) load_g_table(P.T, sG);
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -50,7 +52,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
         const int slice = (int)(task / per_slice);
         const int rem = (int)(task % per_slice);
         walk_task<NP, SINGLE, ODD, KAHAN>(P.ctx, P.T, P.slice_first[slice], P.slice_count[slice],
-                                          rem / P.nchunks, rem % P.nchunks, lane, sY, sN, vbuf, kahan,
+                                          rem / P.nchunks, rem % P.nchunks, lane, sY, sN, sG, vbuf, kahan,
                                           tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, P.status, P.work);
