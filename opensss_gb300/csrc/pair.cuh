@@ -18,8 +18,10 @@ constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
 static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
 
 // Gaussian factors 2^(-gamma (n-b)^2) of the factored weights: [n][b], rows of
-// kGRow floats (at most 64 bins), after the voxel buffers
-constexpr int kGRow = 64;
+// kGRow floats (at most 64 bins plus 4 of padding, so that lanes reading the
+// same bins of different rows fall in different shared-memory banks), after
+// the voxel buffers
+constexpr int kGRow = 68;
 constexpr int kSmemGFloats = kSmemVbufFloats + 2 * 32 * kPairWarps;
 // Kahan running sums and compensations: float2 [2 * NP][threads], after the G table
 constexpr int kSmemKahanFloats = kSmemGFloats + 64 * kGRow;
@@ -103,7 +105,7 @@ __device__ __forceinline__ void load_g_table(const TofConst& T, float* sG)
     for (int i = threadIdx.x; i < T.nbins * kGRow; i += blockDim.x) {
         const int n = i / kGRow, b = i % kGRow;
         const float d = (float)(n - b);
-        sG[i] = b < T.nbins ? exp2f(-T.gamma * d * d) : 0.f;
+        sG[i] = b < T.nbins ? exp2f(-T.gamma * d * d) : 0.f;  // 0 past the last bin and in the padding
     }
 }
 
