@@ -55,17 +55,16 @@ __global__ void __launch_bounds__(128) batch_leg_kernel(const LegItem* __restric
 }
 
 template <int NP, bool SINGLE, bool ODD, int MINB>
-__global__ void __launch_bounds__(kPairWarps * 32, MINB)
+__global__ void __launch_bounds__(pair_block_warps(NP, false) * 32, MINB)
     batch_pair_kernel(const PairItem* __restrict__ items, int nitems, long long ntasks, TofConst T,
                       const float* tof_log2w, unsigned int* counter, int32_t* status)
 {
-    extern __shared__ float smem[];
-    float* sY = smem;
-    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
-    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
-    float* sG = smem + kSmemGFloats;
-    load_tof_table(tof_log2w, sY, sN);
-    if (T.factored) load_g_table(T, sG);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* sAR = reinterpret_cast<float2*>(smem);
+    unsigned char* sN = smem + kSmemNOff;
+    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufOff) + (threadIdx.x >> 5) * 32;
+    float* sG = reinterpret_cast<float*>(smem + kSmemGOff);
+    load_pair_tables(tof_log2w, T, sAR, sN, sG);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     bool tof_bad = false, energy_bad = false;
@@ -83,7 +82,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB)
         }
         const PairItem& it = items[lo];
         const int rem = (int)(task - it.task_begin);
-        walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sY,
+        walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sAR,
                                           sN, sG, vbuf, nullptr, tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
@@ -95,7 +94,7 @@ using BatchPairFn = void (*)(const PairItem*, int, long long, TofConst, const fl
 template <int NP, bool SINGLE, bool ODD>
 BatchPairFn batch_pair_fn()
 {
-    return batch_pair_kernel<NP, SINGLE, ODD, (NP <= 8 ? 3 : 2)>;
+    return batch_pair_kernel<NP, SINGLE, ODD, 2>;
 }
 
 // The pair kernel of a bin count (same register / occupancy choices as sss_tof_run).
@@ -117,19 +116,19 @@ BatchPairFn pick_batch_pairs(int nbins)
 
 // Shared-memory opt-in and persistent grid size of a pair launch, decided at
 // plan time so that a run only enqueues launches (and can be captured).
-int prepare_batch_pairs(BatchPairFn fn, long long ntasks, long long* blocks)
+int prepare_batch_pairs(BatchPairFn fn, int nbins, long long ntasks, long long* blocks)
 {
-    const size_t smem = pair_smem_bytes();
+    const size_t smem = pair_smem_bytes(nbins);
     if (cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return sss_set_error(SSS_ERR_CUDA, "sss_batch_plan: %s", cudaGetErrorString(cudaGetLastError()));
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kPairWarps * 32, smem);
+    const int warps = pair_block_warps((nbins + 1) / 2, false);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, warps * 32, smem);
     if (per_sm < 1) per_sm = 1;
-    *blocks = std::max<long long>(
-        1, std::min<long long>((long long)sms * per_sm, (ntasks + kPairWarps - 1) / kPairWarps));
+    *blocks = std::max<long long>(1, std::min<long long>((long long)sms * per_sm, (ntasks + warps - 1) / warps));
     return SSS_OK;
 }
 
@@ -444,7 +443,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
                 P.task_begin = Lc.ntasks;
                 Lc.ntasks += (long long)C.nl * P.nchunks;
             }
-            int rc = prepare_batch_pairs(Lc.fn, Lc.ntasks, &Lc.blocks);
+            int rc = prepare_batch_pairs(Lc.fn, Lc.nbins, Lc.ntasks, &Lc.blocks);
             if (rc) return rc;
             W.launches.push_back(Lc);
         }
@@ -494,7 +493,8 @@ extern "C" int sss_batch_run_waves(const sss_batch* B, int32_t first, int32_t co
         int rc = sss_check_launch("batch_leg_kernel");
         if (rc) return rc;
         for (const auto& L : W.launches) {
-            L.fn<<<(unsigned)L.blocks, kPairWarps * 32, pair_smem_bytes(), st>>>(
+            L.fn<<<(unsigned)L.blocks, pair_block_warps((L.nbins + 1) / 2, false) * 32, pair_smem_bytes(L.nbins),
+                   st>>>(
                 L.items, L.nitems, L.ntasks, L.T, L.tof, L.counter, B->status);
             rc = sss_check_launch("batch_pair_kernel");
             if (rc) return rc;

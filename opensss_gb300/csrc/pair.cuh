@@ -10,27 +10,41 @@
 namespace sss {
 
 constexpr double kLightCmPerPs = 299792458.0 * 1e-10;  // :144
-constexpr int kPairWarps = 8;                           // warps per pair-kernel block
-// pair-kernel shared memory: log2 largest weight per TOF offset (floats),
-// its bin (bytes), then 32 float2 voxels per warp on a 16-byte boundary
-constexpr int kSmemNFloats = (kTofEntries + 3) / 4;
-constexpr int kSmemVbufFloats = (kTofEntries + kSmemNFloats + 3) & ~3;
-static_assert((kSmemVbufFloats * sizeof(float)) % 16 == 0, "voxel buffer must be 16-byte aligned");
+constexpr int kPairWarps = 12;  // most warps of a pair-kernel block
+constexpr int kKahanWarps = 8;  // warps of a Kahan-compensated pair block
 
+// Warps of a pair block of np bin pairs: 12 up to 8 pairs (two blocks a
+// multiprocessor, 80 registers a thread); 8 above, where the accumulators want
+// 128 registers (two blocks); kKahanWarps for Kahan-compensated launches (one
+// block, the partial sums in shared memory).
+__host__ __device__ constexpr int pair_block_warps(int np, bool kahan)
+{
+    return kahan ? kKahanWarps : (np <= 8 ? kPairWarps : 8);
+}
 // Gaussian factors 2^(-gamma (n-b)^2) of the factored weights: [n][b], rows of
 // kGRow floats (at most 64 bins plus 4 of padding, so that lanes reading the
-// same bins of different rows fall in different shared-memory banks), after
-// the voxel buffers
+// same bins of different rows fall in different shared-memory banks)
 constexpr int kGRow = 68;
-constexpr int kSmemGFloats = kSmemVbufFloats + 2 * 32 * kPairWarps;
-// Kahan running sums and compensations: float2 [2 * NP][threads], after the G table
-constexpr int kSmemKahanFloats = kSmemGFloats + 64 * kGRow;
+
+// Shared memory of a pair block, in this order:
+//   ar    float2 [8001]  (A, r) of each TOF offset (factored weights) or (Y, 0)
+//   n     u8     [8001]  bin of the column's largest weight
+//   vbuf  float2 [warps][32]  staged voxels of each warp's walk
+//   g     float  [nbins][kGRow]
+//   kahan float2 [2 NP][32 kKahanWarps]  (Kahan-compensated launches only,
+//         which run kKahanWarps warps so that 64 bins still fit)
+constexpr int kSmemNOff = (8 * kTofEntries + 15) & ~15;
+constexpr int kSmemVbufOff = (kSmemNOff + kTofEntries + 15) & ~15;
+constexpr int kSmemGOff = kSmemVbufOff + 8 * 32 * kPairWarps;
+static_assert(kSmemGOff % 16 == 0, "shared-memory sections must be 16-byte aligned");
+
+__host__ __device__ inline int pair_smem_kahan_off(int nbins) { return kSmemGOff + 4 * kGRow * nbins; }
 
 // Dynamic shared memory of a pair launch; kahan_np = bin pairs of a
 // Kahan-compensated launch, 0 otherwise.
-inline size_t pair_smem_bytes(int kahan_np = 0)
+inline size_t pair_smem_bytes(int nbins, int kahan_np = 0)
 {
-    return sizeof(float) * kSmemKahanFloats + sizeof(float2) * 2 * kahan_np * 32 * kPairWarps;
+    return (size_t)pair_smem_kahan_off(nbins) + sizeof(float2) * 2 * kahan_np * 32 * kKahanWarps;
 }
 
 // TOF constants of one launch (every task of a launch shares one TOF table)
@@ -90,23 +104,38 @@ inline float gamma_kn_const()
 // 32-partner chunks per walking leg: nl legs plus nru same-crystal entries
 __host__ __device__ inline int pair_chunks(int nru, int ndu) { return (nru * ndu + nru + 31) / 32; }
 
-// Block-wide load of the (log2 largest weight, bin) table into shared memory.
-__device__ __forceinline__ void load_tof_table(const float* g, float* sY, unsigned char* sN)
+// Block-wide set-up of the shared tables.  From the (log2 largest weight Y,
+// bin n) table: for the factored weights, per TOF offset t, beta(t) = 2 kappa
+// w (t - 4000 - s_n) rounded to float once, r = 2^beta and A = 2^(Y - n beta)
+// with the same beta (so that A r^n = 2^Y up to rounding); otherwise (Y, 0).
+// G[n][b] = 2^(-gamma (n - b)^2), 0 past the last bin and in the padding.
+__device__ __forceinline__ void load_pair_tables(const float* g, const TofConst& T, float2* sAR,
+                                                 unsigned char* sN, float* sG)
 {
     for (int i = threadIdx.x; i < kTofEntries; i += blockDim.x) {
-        sY[i] = g[2 * i];
-        sN[i] = (unsigned char)g[2 * i + 1];
+        const float Y = g[2 * i];
+        const float n = g[2 * i + 1];
+        sN[i] = (unsigned char)n;
+        if (T.factored) {
+            const float off = (float)(i - kTimeRange);
+            const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));  // as the per-voxel form rounds it
+            const double e = (double)Y - (double)n * (double)beta;     // -inf stays -inf
+            float a = 0.f;
+            if (e > -1000.0) {
+                const double k = floor(e);
+                a = ldexpf(exp2f((float)(e - k)), (int)k);
+            }
+            sAR[i] = make_float2(a, exp2f(beta));
+        } else {
+            sAR[i] = make_float2(Y, 0.f);
+        }
     }
-}
-
-// G[n][b] = 2^(-gamma (n - b)^2) for the bins of a launch (0 past the last bin).
-__device__ __forceinline__ void load_g_table(const TofConst& T, float* sG)
-{
-    for (int i = threadIdx.x; i < T.nbins * kGRow; i += blockDim.x) {
-        const int n = i / kGRow, b = i % kGRow;
-        const float d = (float)(n - b);
-        sG[i] = b < T.nbins ? exp2f(-T.gamma * d * d) : 0.f;  // 0 past the last bin and in the padding
-    }
+    if (T.factored)
+        for (int i = threadIdx.x; i < T.nbins * kGRow; i += blockDim.x) {
+            const int n = i / kGRow, b = i % kGRow;
+            const float d = (float)(n - b);
+            sG[i] = b < T.nbins ? exp2f(-T.gamma * d * d) : 0.f;
+        }
 }
 
 // Energy row of a pair exactly as the reference computes it in FP64
@@ -145,7 +174,7 @@ static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int 
 // at a time through packed FP32x2 instructions; NP = number of bin pairs.
 template <int NP, bool SINGLE, bool ODD>
 __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
-                                                 const float* sY, const unsigned char* sN, const float* sG,
+                                                 const float2* sAR, const unsigned char* sN, const float* sG,
                                                  const TofConst& T, bool& tof_bad)
 {
     // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
@@ -161,22 +190,16 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
             return;
         }
     }
-    const float Y = sY[t];
-    const float n = (float)sN[t];
-    // beta = 2 kappa w (off - s_n), s_n = s0 + n w
-    const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));
-    if constexpr (SINGLE) {
-        acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(T.gamma, n, beta), Y)), acc[0].x);
-    } else if (T.factored) {
-        // w_b = 2^(Y - (n-b) beta - gamma (n-b)^2) = [2^(Y - n beta) r^b] G[n][b],
-        // r = 2^beta: two 2^x per voxel, then two multiplies per bin
-        // (ca times the power of r carried along: one FFMA2 and one FMUL2 per bin pair)
-        const float r = ex2(beta);
-        float2 P2 = make_float2(ca * ex2(fmaf(-n, beta, Y)), 0.f);
-        P2.y = P2.x * r;
-        const float r2 = r * r;
+    if (!SINGLE && T.factored) {
+        // w_b = 2^(Y - (n-b) beta - gamma (n-b)^2) = [A r^b] G[n][b], A = 2^(Y - n beta),
+        // r = 2^beta, both tabled per offset; ca times the power of r is carried
+        // along: one FFMA2 and one FMUL2 per bin pair
+        const float2 ar = sAR[t];
+        float2 P2 = make_float2(ca * ar.x, 0.f);
+        P2.y = P2.x * ar.y;
+        const float r2 = ar.y * ar.y;
         const float2 R2 = make_float2(r2, r2);
-        const float4* G4 = reinterpret_cast<const float4*>(sG + (int)n * kGRow);
+        const float4* G4 = reinterpret_cast<const float4*>(sG + (int)sN[t] * kGRow);
         float4 g4;
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
@@ -185,6 +208,14 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
             acc[k] = __ffma2_rn(P2, g2, acc[k]);
             if (k + 1 < NP) P2 = __fmul2_rn(P2, R2);
         }
+        return;
+    }
+    const float Y = sAR[t].x;
+    const float n = (float)sN[t];
+    // beta = 2 kappa w (off - s_n), s_n = s0 + n w
+    const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));
+    if constexpr (SINGLE) {
+        acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(T.gamma, n, beta), Y)), acc[0].x);
     } else {
         const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
         const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-T.gamma, -T.gamma);
@@ -212,9 +243,9 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
 // buffer and read back as broadcasts, so the trip count is uniform.
 template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int s_first, int s_count,
-                                          int lw, int chunk, int lane, const float* sY, const unsigned char* sN,
-                                          const float* sG, float2* vbuf, float2* kahan, bool& tof_bad,
-                                          bool& energy_bad,
+                                          int lw, int chunk, int lane, const float2* sAR,
+                                          const unsigned char* sN, const float* sG, float2* vbuf, float2* kahan,
+                                          bool& tof_bad, bool& energy_bad,
                                           unsigned long long& walked, unsigned long long& npairs)
 {
     const float inv_c = (float)(1.0 / kLightCmPerPs);
@@ -248,7 +279,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
 #pragma unroll
     for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);
     float cnt = 0.f;
-    constexpr int kStride = 32 * kPairWarps;  // this thread's Kahan column: [j * kStride]
+    constexpr int kStride = 32 * kKahanWarps;  // this thread's Kahan column: [j * kStride]
     if constexpr (KAHAN) {
 #pragma unroll
         for (int j = 0; j < 2 * NP; ++j) kahan[j * kStride] = make_float2(0.f, 0.f);
@@ -316,7 +347,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
 #pragma unroll 2
                     for (int j = 0; j < jn; ++j) {
                         const float2 v = vbuf[j];
-                        accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sY, sN, sG,
+                        accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sAR, sN, sG,
                                                           T, tof_bad);
                     }
                 }

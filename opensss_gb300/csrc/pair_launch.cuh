@@ -27,16 +27,15 @@ struct PairParams {
 };
 
 template <int NP, bool SINGLE, bool ODD, bool KAHAN, int MINB>
-__global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
+__global__ void __launch_bounds__(pair_block_warps(NP, KAHAN) * 32, MINB) pair_kernel(const __grid_constant__ PairParams P)
 {
-    extern __shared__ float smem[];
-    float* sY = smem;
-    unsigned char* sN = reinterpret_cast<unsigned char*>(smem + kTofEntries);
-    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufFloats) + (threadIdx.x >> 5) * 32;
-    float2* kahan = reinterpret_cast<float2*>(smem + kSmemKahanFloats) + threadIdx.x;
-    float* sG = smem + kSmemGFloats;
-    load_tof_table(P.tof_log2w, sY, sN);
-    if (P.T.factored) load_g_table(P.T, sG);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* sAR = reinterpret_cast<float2*>(smem);
+    unsigned char* sN = smem + kSmemNOff;
+    float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufOff) + (threadIdx.x >> 5) * 32;
+    float* sG = reinterpret_cast<float*>(smem + kSmemGOff);
+    float2* kahan = reinterpret_cast<float2*>(smem + pair_smem_kahan_off(P.ctx.nbins)) + threadIdx.x;
+    load_pair_tables(P.tof_log2w, P.T, sAR, sN, sG);
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -52,7 +51,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
         const int slice = (int)(task / per_slice);
         const int rem = (int)(task % per_slice);
         walk_task<NP, SINGLE, ODD, KAHAN>(P.ctx, P.T, P.slice_first[slice], P.slice_count[slice],
-                                          rem / P.nchunks, rem % P.nchunks, lane, sY, sN, sG, vbuf, kahan,
+                                          rem / P.nchunks, rem % P.nchunks, lane, sAR, sN, sG, vbuf, kahan,
                                           tof_bad, energy_bad, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, walked, npairs, P.status, P.work);
@@ -61,19 +60,20 @@ __global__ void __launch_bounds__(kPairWarps * 32, MINB) pair_kernel(const __gri
 template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 int launch_pairs(const PairParams& P, cudaStream_t st)
 {
-    constexpr int MINB = (NP <= 8 && !KAHAN) ? 3 : 2;
+    constexpr int MINB = KAHAN ? 1 : 2;
+    constexpr int kWarps = pair_block_warps(NP, KAHAN);
     auto kern = pair_kernel<NP, SINGLE, ODD, KAHAN, MINB>;
-    const size_t smem = pair_smem_bytes(KAHAN ? NP : 0);
+    const size_t smem = pair_smem_bytes(P.ctx.nbins, KAHAN ? NP : 0);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPairWarps * 32, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
     if (per_sm < 1) per_sm = 1;
     long long ntasks = (long long)P.nslices * P.ctx.nl * P.nchunks;
-    long long blocks = std::min<long long>((long long)sms * per_sm, (ntasks + kPairWarps - 1) / kPairWarps);
+    long long blocks = std::min<long long>((long long)sms * per_sm, (ntasks + kWarps - 1) / kWarps);
     if (blocks < 1) blocks = 1;
-    kern<<<(unsigned)blocks, kPairWarps * 32, smem, st>>>(P);
+    kern<<<(unsigned)blocks, kWarps * 32, smem, st>>>(P);
     return sss_check_launch("pair_kernel");
 }
 
