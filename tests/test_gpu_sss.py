@@ -199,3 +199,26 @@ def test_slice_shards_add_up_to_the_full_run(cuda_ok, att_table):
                      slice_range=partition_slices(counts, r, 2)).cpu().numpy() for r in range(2)]
     assert all(np.abs(p).max() > 0 for p in parts)
     assert rel_l2(parts[0] + parts[1], full) < 1e-6
+
+
+@pytest.mark.parametrize("bins", [63, 64])
+def test_widest_bin_counts_launch_and_match_oracle(cuda_ok, att_table, bins):
+    """The largest bin counts: a 64-row Gaussian table in shared memory, and
+    with Kahan's partial sums also there (the densest layout).  The plain,
+    compensated and batched runs all match the FP64 oracle."""
+    from opensss_gb300 import workloads as W
+    from opensss_gb300.batch import BatchSSS
+    from opensss_gb300.engine import leg_pair_to_compact
+
+    scanner = W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0)
+    pr = W.make_problem(f"tiny-b{bins}", (12, 12, 6), 2.0, 3, 8, bins, 1.5, 214.0, seed=4, scanner=scanner,
+                        radius_cm=8.0)
+    ref = _oracle_compact(pr, att_table)
+    assert np.abs(ref).max() > 0
+    runs = {k: _gpu_compact(pr, att_table, kahan=k) for k in (False, True)}
+    b = BatchSSS([(_engine(pr, att_table), pr.activity, pr.attenuation, pr.image_size)])
+    runs["batch"] = leg_pair_to_compact(b.run()[0].cpu().numpy(), pr.nr_rings_used, pr.nr_detectors_used)
+    b.close()
+    for name, got in runs.items():
+        assert_same_support(got, ref)
+        assert rel_l2(got, ref) < TOL, name
