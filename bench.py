@@ -257,14 +257,27 @@ def run_ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel (pair kernel: SFU-bound 2^x per voxel-bin)
+    # ---- roofline of the dominant kernel.  The pair kernel reads, per
+    # (voxel of a walked leg, detector pair), the bins' TOF factors (4 B a
+    # bin) and the voxel's activity x length and distance (8 B): the per-unit
+    # bytes of the reference's TOF-table gather, taken from shared memory.
     pair_s = statistics.mean(pair_ms) / 1e3
-    ex2_per_launch = stage[4] if stage[4] > 0 else None
-    peak = _sfu_peak(clocks)
-    roof = {"bound": "sfu", "unit": "Gex2/s", "kernel": "pair_kernel",
-            "achieved": (ex2_per_launch / pair_s / 1e9) if ex2_per_launch else None,
-            "peak": peak["value"], "peak_source": peak["source"], "traffic": _traffic()}
-    roof["frac"] = (roof["achieved"] / roof["peak"]) if roof["achieved"] and roof["peak"] else None
+    walked = stage[4] / pr.nr_bins if stage[4] > 0 else None  # (voxel, pair) terms of one step
+    alg_bytes = walked * (4 * pr.nr_bins + 8) if walked else None
+    peaks = _probe_peaks()
+    achieved = alg_bytes / pair_s / 1e9 if alg_bytes else None
+    roof = {"bound": "smem", "unit": "GB/s", "kernel": "pair_kernel", "achieved": achieved,
+            "peak": peaks["smem"], "peak_source": "measured (sss_probe_smem_rate, this run)",
+            "frac": achieved / peaks["smem"] if achieved and peaks["smem"] else None,
+            "traffic": _traffic(), "algorithmic_bytes_per_launch": alg_bytes,
+            "bytes_rule": "(4 B x bins + 8 B) per (voxel, detector pair) term walked",
+            "terms_per_launch": walked, "launch_ms": pair_s * 1e3,
+            "l2_reference_gather": {
+                "achieved": achieved, "peak": peaks["l2"], "unit": "GB/s",
+                "frac": achieved / peaks["l2"] if achieved and peaks["l2"] else None,
+                "peak_source": "measured (sss_probe_l2_rate, 32 MB L2-resident, this run)",
+                "note": "same bytes against the L2 load bandwidth a TOF-table gather would be bound by"},
+            "weights_per_s": stage[4] / pair_s if stage[4] > 0 else None}
 
     # ---- CPU baseline (oracle port on the host cores) and error vs FP64 on the same sample
     cpu = None
@@ -716,19 +729,19 @@ def run_listmode(dev, args):
                              "sample": f"first {m} events, per-event Python loop as the reference's"}}
 
 
-def _sfu_peak(clocks):
-    """SFU 2^x peak measured in this process (sss_probe_ex2_rate: every SM
-    issuing independent ex2 chains), else 152 SMs x 16 results/clk x max clock."""
+def _probe_peaks():
+    """Shared-memory and L2 load bandwidth (GB/s) measured on this device by
+    the library's probe kernels; None where a probe fails."""
     import torch
 
     from opensss_gb300 import _lib
 
-    v = C.c_double(0.0)
-    st = torch.cuda.current_stream()
-    if _lib.lib().sss_probe_ex2_rate(C.byref(v), C.c_void_p(st.cuda_stream)) == 0 and v.value > 0:
-        return {"value": v.value, "source": "measured (sss_probe_ex2_rate)"}
-    mhz = clocks.get("sm_max_mhz") or 2070.0
-    return {"value": 152 * 16 * mhz * 1e6 / 1e9, "source": "nominal 152 SM x 16/clk x max clock"}
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {}
+    for key, fn in (("smem", "sss_probe_smem_rate"), ("l2", "sss_probe_l2_rate")):
+        v = C.c_double(0.0)
+        out[key] = v.value if getattr(_lib.lib(), fn)(C.byref(v), st) == 0 and v.value > 0 else None
+    return out
 
 
 def _traffic():

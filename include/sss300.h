@@ -353,6 +353,13 @@ int sss_get_timing(double out[6]);
  * stage).  Synchronises `stream`. */
 int sss_probe_ex2_rate(double *gex2_per_s, void *stream);
 
+/* Measured shared-memory load bandwidth (conflict-free 16-byte loads on every
+ * multiprocessor) and L2 load bandwidth (a 32 MB L2-resident buffer read with
+ * L2-only loads) of the current device, in GB/s (no reference counterpart:
+ * roofline denominators of the pair stage).  Synchronise `stream`. */
+int sss_probe_smem_rate(double *gb_per_s, void *stream);
+int sss_probe_l2_rate(double *gb_per_s, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

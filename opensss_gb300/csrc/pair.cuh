@@ -167,6 +167,40 @@ static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int 
     return (int)mul64(es, 2.0) - 1;
 }
 
+// Factored weights of one voxel whose table entry is loaded: w_b =
+// 2^(Y - (n-b) beta - gamma (n-b)^2) = [A r^b] G[n][b], with ar = (A, r),
+// A = 2^(Y - n beta), r = 2^beta tabled per offset and nb = n; ca times the
+// power of r is carried along: one FFMA2 and one FMUL2 per bin pair.  Bins past
+// the last one have G = 0.
+template <int NP>
+__device__ __forceinline__ void accumulate_loaded(float2 (&acc)[NP], float ca, float2 ar, int nb, const float* sG)
+{
+    float2 P2 = make_float2(ca * ar.x, 0.f);
+    P2.y = P2.x * ar.y;
+    const float r2 = ar.y * ar.y;
+    const float2 R2 = make_float2(r2, r2);
+    const float4* G4 = reinterpret_cast<const float4*>(sG + nb * kGRow);
+    float4 g4;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        if ((k & 1) == 0) g4 = G4[k >> 1];
+        const float2 g2 = (k & 1) ? make_float2(g4.z, g4.w) : make_float2(g4.x, g4.y);
+        acc[k] = __ffma2_rn(P2, g2, acc[k]);
+        if (k + 1 < NP) P2 = __fmul2_rn(P2, R2);
+    }
+}
+
+// Table offset of x: floor(x), numpy's wrap of negative indices; an offset
+// past either end is flagged and replaced by 0 (its voxel then adds nothing).
+__device__ __forceinline__ int lookup_offset(float x, bool& ok, bool& tof_bad)
+{
+    int t = __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
+    t = t < 0 ? t + kTofEntries : t;
+    ok = (unsigned)t < (unsigned)kTofEntries;
+    tof_bad |= !ok;
+    return ok ? t : 0;
+}
+
 // Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
 // reference's 8001-entry TOF table, :520-528).  w_b is rebuilt from the
 // largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
@@ -191,23 +225,7 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
         }
     }
     if (!SINGLE && T.factored) {
-        // w_b = 2^(Y - (n-b) beta - gamma (n-b)^2) = [A r^b] G[n][b], A = 2^(Y - n beta),
-        // r = 2^beta, both tabled per offset; ca times the power of r is carried
-        // along: one FFMA2 and one FMUL2 per bin pair
-        const float2 ar = sAR[t];
-        float2 P2 = make_float2(ca * ar.x, 0.f);
-        P2.y = P2.x * ar.y;
-        const float r2 = ar.y * ar.y;
-        const float2 R2 = make_float2(r2, r2);
-        const float4* G4 = reinterpret_cast<const float4*>(sG + (int)sN[t] * kGRow);
-        float4 g4;
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-            if ((k & 1) == 0) g4 = G4[k >> 1];
-            const float2 g2 = (k & 1) ? make_float2(g4.z, g4.w) : make_float2(g4.x, g4.y);
-            acc[k] = __ffma2_rn(P2, g2, acc[k]);
-            if (k + 1 < NP) P2 = __fmul2_rn(P2, R2);
-        }
+        accumulate_loaded<NP>(acc, ca, sAR[t], (int)sN[t], sG);
         return;
     }
     const float Y = sAR[t].x;
@@ -344,11 +362,33 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                 __syncwarp();
                 const int jn = min(32, nw - k0);
                 if (c != 0.f) {
+                    if (!SINGLE && T.factored) {
+                        // the table lookup of voxel j+1 overlaps the accumulation of voxel j
+                        float2 v = vbuf[0];
+                        bool ok;
+                        int t = lookup_offset(fmaf(sigma, v.y, u), ok, tof_bad);
+                        float2 ar = sAR[t];
+                        int nb = sN[t];
+                        float ca = ok ? c * v.x : 0.f;
 #pragma unroll 2
-                    for (int j = 0; j < jn; ++j) {
-                        const float2 v = vbuf[j];
-                        accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sAR, sN, sG,
-                                                          T, tof_bad);
+                        for (int j = 0; j < jn; ++j) {
+                            const float2 v1 = vbuf[j + 1 < jn ? j + 1 : j];
+                            bool ok1;
+                            const int t1 = lookup_offset(fmaf(sigma, v1.y, u), ok1, tof_bad);
+                            const float2 ar1 = sAR[t1];
+                            const int nb1 = sN[t1];
+                            accumulate_loaded<NP>(acc, ca, ar, nb, sG);
+                            ar = ar1;
+                            nb = nb1;
+                            ca = ok1 ? c * v1.x : 0.f;
+                        }
+                    } else {
+#pragma unroll 2
+                        for (int j = 0; j < jn; ++j) {
+                            const float2 v = vbuf[j];
+                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sAR, sN, sG,
+                                                              T, tof_bad);
+                        }
                     }
                 }
             }

@@ -1,6 +1,8 @@
-// Throughput probe for the SFU 2^x instruction (ex2.approx.ftz.f32), the
-// instruction the pair kernel is bound by.  bench.py uses the measured rate
-// as the roofline denominator of that kernel.
+// Throughput probes for the roofline denominators of the pair stage, measured
+// on the device the engine runs on: the SFU 2^x instruction
+// (ex2.approx.ftz.f32), the shared-memory load bandwidth (the pair kernel
+// reads its TOF factors from shared memory) and the L2 load bandwidth (where
+// a TOF-table gather, as the reference does it, would read them from).
 #include "common.cuh"
 
 namespace {
@@ -22,7 +24,123 @@ __global__ void __launch_bounds__(256) ex2_probe_kernel(int iters, float* sink)
     if (s == 123.456f) sink[0] = s;  // keeps the chains alive
 }
 
+// Shared-memory loads: every warp reads 512 contiguous bytes per LDS.128
+// (no bank conflicts), eight independent loads per iteration, from a 32 KB
+// buffer; the loaded words are folded with XOR so that no load is dead.
+constexpr int kSmemVec = 2048;  // float4 entries (32 KB)
+__global__ void __launch_bounds__(256) smem_probe_kernel(int iters, unsigned* sink)
+{
+    __shared__ float4 buf[kSmemVec];
+    for (int i = threadIdx.x; i < kSmemVec; i += blockDim.x)
+        buf[i] = make_float4((float)i, (float)(i + 1), (float)(i + 2), (float)(i + 3));
+    __syncthreads();
+    unsigned acc = 0;
+    int idx = threadIdx.x & 1023;  // idx + 7 * 128 < kSmemVec
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float4 v = buf[idx + c * 128];
+            acc ^= __float_as_uint(v.x) ^ __float_as_uint(v.y) ^ __float_as_uint(v.z) ^ __float_as_uint(v.w);
+        }
+        idx = (idx + 32) & 1023;
+    }
+    if (acc == 0x9e3779b9u) sink[0] = acc;
+}
+
+// L2 loads: a buffer that fits in L2 is read with ld.global.cg (L2 only, no
+// L1), four independent 16-byte loads in flight per thread.
+__global__ void __launch_bounds__(256) l2_probe_kernel(const float4* __restrict__ buf, long long n4, int reps,
+                                                       unsigned* sink)
+{
+    unsigned acc = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int r = 0; r < reps; ++r) {
+        long long i = first;
+        for (; i + 3 * stride < n4; i += 4 * stride) {
+            const float4 a = __ldcg(buf + i), b = __ldcg(buf + i + stride);
+            const float4 c = __ldcg(buf + i + 2 * stride), d = __ldcg(buf + i + 3 * stride);
+            acc ^= __float_as_uint(a.x) ^ __float_as_uint(a.w) ^ __float_as_uint(b.x) ^ __float_as_uint(b.w) ^
+                   __float_as_uint(c.x) ^ __float_as_uint(c.w) ^ __float_as_uint(d.x) ^ __float_as_uint(d.w);
+        }
+        for (; i < n4; i += stride) {
+            const float4 a = __ldcg(buf + i);
+            acc ^= __float_as_uint(a.x) ^ __float_as_uint(a.w);
+        }
+    }
+    if (acc == 0x9e3779b9u) sink[0] = acc;
+}
+
+// Times one launch of a probe between two events on st (after one warm-up
+// launch); returns 0 and the milliseconds, or an SSS error code.
+template <typename Launch>
+int time_probe(const char* what, cudaStream_t st, Launch launch, float* ms)
+{
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) return sss_set_error(SSS_ERR_CUDA, "%s: event", what);
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return sss_set_error(SSS_ERR_CUDA, "%s: event", what);
+    }
+    launch(true);
+    cudaEventRecord(a, st);
+    launch(false);
+    cudaEventRecord(b, st);
+    int rc = sss_check_launch(what);
+    if (!rc && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(ms, a, b) != cudaSuccess))
+        rc = sss_set_error(SSS_ERR_CUDA, "%s: timing failed", what);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+}
+
 }  // namespace
+
+extern "C" int sss_probe_smem_rate(double* gb_per_s, void* stream)
+{
+    if (!gb_per_s) return sss_set_error(SSS_ERR_INVALID, "sss_probe_smem_rate: null output");
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 4, threads = 256, iters = 4096;
+    unsigned* sink = nullptr;
+    if (cudaMallocAsync(&sink, sizeof(unsigned), st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_probe_smem_rate: allocation failed");
+    float ms = 0.f;
+    int rc = time_probe("smem_probe_kernel", st, [&](bool warm) {
+        smem_probe_kernel<<<blocks, threads, 0, st>>>(warm ? iters / 8 : iters, sink);
+    }, &ms);
+    cudaFreeAsync(sink, st);
+    if (rc) return rc;
+    *gb_per_s = (double)blocks * threads * iters * 8 * 16 / (ms * 1e-3) / 1e9;
+    return SSS_OK;
+}
+
+extern "C" int sss_probe_l2_rate(double* gb_per_s, void* stream)
+{
+    if (!gb_per_s) return sss_set_error(SSS_ERR_INVALID, "sss_probe_l2_rate: null output");
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long n4 = (32ll << 20) / 16;  // 32 MB, L2-resident
+    const int blocks = sms * 8, threads = 256, reps = 256;
+    float4* buf = nullptr;
+    unsigned* sink = nullptr;
+    if (cudaMallocAsync(&buf, n4 * 16 + 256, st) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_probe_l2_rate: allocation failed");
+    sink = reinterpret_cast<unsigned*>(buf + n4);
+    cudaMemsetAsync(buf, 0, n4 * 16, st);
+    float ms = 0.f;
+    int rc = time_probe("l2_probe_kernel", st, [&](bool warm) {
+        l2_probe_kernel<<<blocks, threads, 0, st>>>(buf, n4, warm ? 2 : reps, sink);
+    }, &ms);
+    cudaFreeAsync(buf, st);
+    if (rc) return rc;
+    *gb_per_s = (double)n4 * 16 * reps / (ms * 1e-3) / 1e9;
+    return SSS_OK;
+}
 
 extern "C" int sss_probe_ex2_rate(double* gex2_per_s, void* stream)
 {
