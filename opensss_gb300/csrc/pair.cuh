@@ -27,7 +27,8 @@ __host__ __device__ constexpr int pair_block_warps(int np, bool kahan)
 constexpr int kGRow = 68;
 
 // Shared memory of a pair block, in this order:
-//   ar    float2 [8001]  (A, r) of each TOF offset (factored weights) or (Y, 0)
+//   ar    float2 [8001]  (A, r) of each TOF offset (factored weights; A carries
+//         the nearest bin n in its low mantissa bits) or (Y, 0)
 //   n     u8     [8001]  bin of the column's largest weight
 //   vbuf  float2 [warps][32]  staged voxels of each warp's walk
 //   g     float  [nbins][kGRow]
@@ -53,6 +54,7 @@ struct TofConst {
     float kappa2w, gamma;  // 2 kappa w and kappa w^2, kappa = 4/FWHM^2 (log2 units)
     int factored;          // weights as 2^(Y - n beta) r^b G[n][b] (see accumulate_voxel)
     int nbins;
+    int nmask;             // low mantissa bits of the tabled A that carry the nearest bin n
 };
 
 // Everything one task needs about its problem and z-slice.
@@ -89,6 +91,9 @@ inline TofConst tof_const(const sss_tof_problem& p)
     // beta < 45 w / FWHM, so r^2 = 2^(2 beta) < 2^120).
     T.factored = p.nbins > 1 && (kappa * w * w) * (p.nbins - 1) < 100.0 && w / p.tof_resolution < 1.33;
     T.nbins = p.nbins;
+    int bits = 1;
+    while ((1 << bits) < p.nbins) ++bits;
+    T.nmask = (1 << bits) - 1;
     return T;
 }
 inline float geo_const(const sss_tof_problem& p)
@@ -104,10 +109,23 @@ inline float gamma_kn_const()
 // 32-partner chunks per walking leg: nl legs plus nru same-crystal entries
 __host__ __device__ inline int pair_chunks(int nru, int ndu) { return (nru * ndu + nru + 31) / 32; }
 
+// A with the bin n in its low mantissa bits: the representable value nearest
+// to a whose bits & mask equal n (a >= 0; a == 0 stays 0, all weights zero).
+__device__ __forceinline__ float pack_bin(float a, int n, int mask)
+{
+    const int ai = __float_as_int(a);
+    if (ai == 0) return 0.f;
+    int p = ai - ((ai - n) & mask);
+    if (ai - p > (mask + 1) / 2 || p < 0) p += mask + 1;
+    return __int_as_float(p);
+}
+
 // Block-wide set-up of the shared tables.  From the (log2 largest weight Y,
 // bin n) table: for the factored weights, per TOF offset t, beta(t) = 2 kappa
 // w (t - 4000 - s_n) rounded to float once, r = 2^beta and A = 2^(Y - n beta)
-// with the same beta (so that A r^n = 2^Y up to rounding); otherwise (Y, 0).
+// with the same beta (so that A r^n = 2^Y up to rounding), A rounded to the
+// nearest value whose low bits hold n (relative change below 2^-(24 - bits),
+// bits = ceil(log2 nbins)); otherwise (Y, 0).
 // G[n][b] = 2^(-gamma (n - b)^2), 0 past the last bin and in the padding.
 __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst& T, float2* sAR,
                                                  unsigned char* sN, float* sG)
@@ -125,7 +143,7 @@ __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst&
                 const double k = floor(e);
                 a = ldexpf(exp2f((float)(e - k)), (int)k);
             }
-            sAR[i] = make_float2(a, exp2f(beta));
+            sAR[i] = make_float2(pack_bin(a, (int)n, T.nmask), exp2f(beta));
         } else {
             sAR[i] = make_float2(Y, 0.f);
         }
@@ -138,9 +156,13 @@ __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst&
         }
 }
 
-// Energy row of a pair exactly as the reference computes it in FP64
-// (:442-444, :474-475, :495-501), used when the FP32 estimate lies within
-// 1e-3 keV of a rounding boundary.
+// Energy row of a pair in FP64, used when the FP32 estimate lies within 1e-3
+// keV of a rounding boundary.  The law-of-cosines argument q is formed with the
+// reference's FP64 operations (:442-444, :474-475, :216-235).  The reference
+// then takes theta = 180 - degrees(acos(q)) and cos(deg2rad(theta)) (:498-499),
+// which is -q up to that round trip's own rounding (~1e-16); -q is used
+// directly, so the row can differ from the reference's only where 511/(2 + q)
+// + 0.5 lies within ~1e-13 of an integer.  Symmetric in the two legs.
 static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int ri1, int di1, int ri2,
                                             int di2)
 {
@@ -161,9 +183,9 @@ static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int 
                        mul64(sub64(z1, z2), sub64(z1, z2)));
     double a = mul64(sv1, sv1), b = mul64(sv2, sv2);
     double q = div64(sub64(add64(a, b), lor), mul64(2.0, __dsqrt_rn(mul64(a, b))));
-    double th = sub64(180.0, mul64(acos(q), 180.0 / 3.141592653589793));
-    double cth = cos(mul64(th, 3.141592653589793 / 180.0));
-    double es = floor(add64(div64(511.0, add64(1.0, mul64(1.0, sub64(1.0, cth)))), 0.5));
+    if (!(q >= -1.0 && q <= 1.0)) return -1;  // outside acos' domain: the reference fails too
+    // cos(deg2rad(180 - degrees(acos(q)))) is -q up to the round trip's rounding
+    double es = floor(add64(div64(511.0, add64(1.0, add64(1.0, q))), 0.5));
     return (int)mul64(es, 2.0) - 1;
 }
 
@@ -225,7 +247,7 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
         }
     }
     if (!SINGLE && T.factored) {
-        accumulate_loaded<NP>(acc, ca, sAR[t], (int)sN[t], sG);
+        accumulate_loaded<NP>(acc, ca, sAR[t], __float_as_int(sAR[t].x) & T.nmask, sG);
         return;
     }
     const float Y = sAR[t].x;
@@ -368,7 +390,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                         bool ok;
                         int t = lookup_offset(fmaf(sigma, v.y, u), ok, tof_bad);
                         float2 ar = sAR[t];
-                        int nb = sN[t];
+                        int nb = __float_as_int(ar.x) & T.nmask;
                         float ca = ok ? c * v.x : 0.f;
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
@@ -376,7 +398,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                             bool ok1;
                             const int t1 = lookup_offset(fmaf(sigma, v1.y, u), ok1, tof_bad);
                             const float2 ar1 = sAR[t1];
-                            const int nb1 = sN[t1];
+                            const int nb1 = __float_as_int(ar1.x) & T.nmask;
                             accumulate_loaded<NP>(acc, ca, ar, nb, sG);
                             ar = ar1;
                             nb = nb1;
