@@ -297,6 +297,7 @@ def run_ours(args, rank, world, local_rank):
     precision = None if args.no_precision or world > 1 else run_precision(dev, args, att)
     serving = None if args.no_serving or world > 1 else run_serving(dev, args, att)
     listmode = None if args.no_listmode or world > 1 else run_listmode(dev, args)
+    prep = None if args.no_prep or world > 1 else run_prep(dev, args)
 
     ms = 1e3 * total_s / args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -311,7 +312,8 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
             "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
-            "batch": batch, "precision": precision, "serving": serving, "listmode": listmode}
+            "batch": batch, "precision": precision, "serving": serving, "listmode": listmode,
+            "image_prep": prep}
     print(json.dumps(line), flush=True)
 
 
@@ -657,6 +659,55 @@ def run_serving(dev, args, att):
             "server_stats": dict(srv.stats), "rel_l2_vs_fp64_small": errs, "clocks": clk.summary()}
 
 
+def run_prep(dev, args):
+    """Image preparation (CropAndDownscale): a seeded 400x400x280 map of
+    1.6 mm x 1.6 mm x 2 mm voxels (179 MB, above the L2) cropped to
+    600 x 600 x 480 mm (376 x 376 x 240 voxels) and resized to 75 x 75 x 48
+    voxels of 8 x 8 x 10 mm (anti-aliasing sigma 2 voxels).  GPU time with the map resident, end to end from a host
+    array, and the scipy.ndimage restatement of the reference's resize on the
+    host (the oracle, one run)."""
+    import torch
+
+    from opensss_gb300 import Utils
+
+    rng = np.random.default_rng(3)
+    img = rng.gamma(2.0, 1.0, size=(400, 400, 280)).astype(np.float32)
+    vox, crop, dims = (1.6, 1.6, 2.0), (600.0, 600.0, 480.0), (75, 75, 48)
+    t = torch.from_numpy(img).to(dev)
+    win = Utils.crop_window(img.shape, vox, crop)
+    st = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        Utils.crop_downscale_device(t, win, dims)
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        out = Utils.crop_downscale_device(t, win, dims)
+        e1.record(st)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        host = Utils.CropAndDownscale(img, vox, crop, dims)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    res = {"workload": "400x400x280 float32 map, crop 600x600x480 mm, resize to 75x75x48 (order 3, anti-aliased)",
+           "ms": statistics.mean(ms), "e2e_ms": statistics.mean(e2e), "input_gb": img.nbytes / 1e9,
+           "h2d_bytes": img.nbytes, "d2h_bytes": int(np.prod(dims)) * 4}
+    if not args.no_cpu:
+        from oracle import prep as P
+
+        t0 = time.perf_counter()
+        ref = P.crop_and_downscale(img, vox, crop, dims)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        res["cpu_baseline"] = {"ms": cpu_ms, "cores": 1, "kind": "port",
+                               "sample": "the whole map, scipy.ndimage gaussian_filter + zoom (float32)"}
+        res["max_err_vs_oracle"] = float(np.abs(host.astype(np.float64) - ref).max() / np.abs(ref).max())
+        del out
+    return res
+
+
 def run_listmode(dev, args):
     """Prompt histogramming of ``--listmode-events`` seeded list-mode events
     (TOF, randoms and normalisation fields, 24-byte records) of the
@@ -780,6 +831,7 @@ def main():
     ap.add_argument("--serve-check", type=int, default=2,
                     help="served small requests checked against the FP64 oracle")
     ap.add_argument("--no-listmode", action="store_true", help="skip the list-mode histogramming")
+    ap.add_argument("--no-prep", action="store_true", help="skip the image preparation (CropAndDownscale)")
     ap.add_argument("--listmode-events", type=int, default=50_000_000)
     ap.add_argument("--listmode-cpu-events", type=int, default=200_000)
     ap.add_argument("--max-points", type=int, default=None,

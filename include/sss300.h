@@ -338,6 +338,25 @@ int sss_inject_scatters(const void *events, int64_t n_events, const sss_listmode
                         int32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Image preparation.  Replaces CropAndDownscale (Python/openSSS/Utils.py:212-267,
+ * used by PrepareImages :30-74): a crop or zero-pad window about the volume
+ * centre, then skimage.transform.resize(order=3, mode='edge',
+ * anti_aliasing=True, preserve_range=True) of that window.  Volumes are
+ * C-ordered float32 [n0][n1][n2] on the device.  The window (computed by the
+ * caller with the reference's slicing rules): crop[i] = image[i - before +
+ * start] per axis where that lies inside the image, else 0, for i <
+ * crop_dims.  sigma: the anti-aliasing Gaussian's sigma per axis in voxels
+ * (0 = no filter on that axis).  clip != 0 clips the result to the window's
+ * [min, max]; results below zero_below become 0 (-INFINITY: none).
+ * workspace: at least sss_crop_downscale_workspace_size(crop_dims) device
+ * bytes. */
+size_t sss_crop_downscale_workspace_size(const int crop_dims[3]);
+int sss_crop_downscale(const float *image, const int image_dims[3], const int crop_start[3],
+                       const int crop_before[3], const int crop_dims[3], const int out_dims[3],
+                       const double sigma[3], int clip, float zero_below, float *out, void *workspace,
+                       size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Stage timing (no reference counterpart: instrumentation for benchmarks).
  * When enabled, sss_tof_run records CUDA events around its kernels on the
  * caller's stream; sss_get_timing waits for them and returns, for the last

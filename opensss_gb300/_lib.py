@@ -109,6 +109,8 @@ SIGNATURES = {
     "sss_inject_workspace_size": (C.c_size_t, [_I64]),
     "sss_inject_scatters": (C.c_int, [_P, _I64, C.POINTER(ListmodeLayout), C.POINTER(SinoMap), _P, _P,
                                       _P, _P, _P, C.c_size_t, _P, _P]),
+    "sss_crop_downscale_workspace_size": (C.c_size_t, [_P]),
+    "sss_crop_downscale": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int, C.c_float, _P, _P, C.c_size_t, _P]),
     "sss_set_timing": (None, [C.c_int]),
     "sss_get_timing": (C.c_int, [_P]),
     "sss_probe_ex2_rate": (C.c_int, [C.POINTER(_D), _P]),

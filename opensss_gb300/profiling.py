@@ -3,7 +3,7 @@
     python -m opensss_gb300.profiling CASE [--reps N]
 
 CASE is one of ``upsample``, ``mask``, ``fit``, ``listmode``, ``pair``,
-``batch``.  Each case builds seeded inputs larger than the 129 MB L2 but a
+``batch``, ``prep``.  Each case builds seeded inputs larger than the 129 MB L2 but a
 few GB at most on the device, runs the kernel ``--reps`` times and checks
 the status word, so that a capture of one to three launches ends within a
 minute or two.
@@ -116,8 +116,21 @@ def case_batch(reps):
         b.run()
 
 
+def case_prep(reps):
+    """CropAndDownscale of a seeded 400x400x280 float32 map (1.6 x 1.6 x 2 mm)
+    cropped to 600 x 600 x 480 mm and resized to 75 x 75 x 48."""
+    from .Utils import crop_downscale_device, crop_window
+
+    rng = np.random.default_rng(3)
+    img = torch.from_numpy(rng.gamma(2.0, 1.0, size=(400, 400, 280)).astype(np.float32)).cuda()
+    win = crop_window(tuple(img.shape), (1.6, 1.6, 2.0), (600.0, 600.0, 480.0))
+    for _ in range(reps):
+        crop_downscale_device(img, win, (75, 75, 48))
+    torch.cuda.synchronize()
+
+
 CASES = {"upsample": case_upsample, "mask": case_mask, "fit": case_fit, "listmode": case_listmode,
-         "pair": case_pair, "batch": case_batch}
+         "pair": case_pair, "batch": case_batch, "prep": case_prep}
 
 
 def main():

@@ -46,3 +46,20 @@ def load():
     ):
         mods[name] = importlib.import_module(f"openSSS.{name}")
     return mods
+
+
+def load_utils():
+    """Import the reference's Utils module with the recording skimage stand-in
+    (oracle/skimage_stub) first on sys.path; returns (Utils, stub transform)."""
+    if not available():
+        raise RuntimeError(f"reference package not found at {REFERENCE_PY}")
+    stub = os.path.join(_HERE, "skimage_stub")
+    if stub in sys.path:
+        sys.path.remove(stub)
+    sys.path.insert(0, stub)
+    if REFERENCE_PY not in sys.path:
+        sys.path.insert(1, REFERENCE_PY)
+    import importlib
+
+    transform = importlib.import_module("skimage.transform")
+    return importlib.import_module("openSSS.Utils"), transform

@@ -499,7 +499,78 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit", "span", "listmode"]
+ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit", "span", "listmode", "prep"]
+
+
+# ---------------------------------------------------------------- image preparation
+
+PREP_CASES = [
+    # (image shape, voxel mm, crop mm, output dims): a plain crop, a window
+    # overhanging both ends of one axis (zero pad), Python's negative-start
+    # slice on an odd axis (a one-sample window), and an upscaled axis
+    ((40, 36, 30), (2.0, 2.0, 3.0), (60.0, 50.0, 81.0), (10, 8, 9)),
+    ((20, 24, 16), (4.0, 4.0, 4.0), (100.0, 80.0, 64.0), (9, 7, 16)),
+    ((21, 20, 19), (1.0, 1.0, 1.0), (22.0, 10.0, 7.0), (4, 5, 3)),
+    ((17, 18, 12), (3.0, 2.5, 4.0), (45.0, 40.0, 44.0), (5, 16, 11)),
+]
+
+
+def _interfile(folder, name, image, scale):
+    """Writes an interfile header + float32 data as the reference's LoadImage
+    reads them (image [x][y][z], data stored z-major)."""
+    nx, ny, nz = image.shape
+    with open(os.path.join(folder, name + ".hdr"), "w") as f:
+        f.write("!INTERFILE :=\n")
+        f.write(f"name of data file := {name}.img\n")
+        for i, (n, sc) in enumerate(zip(image.shape, scale)):
+            f.write(f"matrix size [{i + 1}] := {n}\n")
+            f.write(f"scaling factor (mm/pixel) [{i + 1}] := {sc}\n")
+    image.transpose(2, 1, 0).astype(np.float32).tofile(os.path.join(folder, name + ".img"))
+    return os.path.join(folder, name + ".hdr")
+
+
+def gen_prep(_R):
+    """CropAndDownscale and PrepareImages of the reference run with a recording
+    identity resize: the crop windows, the resize options the reference passes,
+    the sizes PrepareImages derives and its attenuation threshold."""
+    Utils, T = refpy.load_utils()
+    rng = np.random.default_rng(11)
+    out = {}
+    for i, (shape, vox, crop, dims) in enumerate(PREP_CASES):
+        img = (rng.random(shape) * 4.0 - 0.5).astype(np.float32)
+        T.CALLS.clear()
+        cropped = Utils.CropAndDownscale(img, np.array(vox), np.array(crop), np.array(dims))
+        (seen, oshape, kw), = T.CALLS
+        assert np.array_equal(seen, cropped)
+        out[f"case{i}_image"] = img
+        out[f"case{i}_args"] = np.array(list(vox) + list(crop) + list(dims), dtype=np.float64)
+        out[f"case{i}_cropped"] = cropped
+        out[f"case{i}_out_shape"] = np.array(oshape)
+        out[f"case{i}_resize_kwargs"] = np.array(sorted(f"{k}={v}" for k, v in kw.items()))
+    # PrepareImages on interfile maps (mm): activity 30x28x20 @ (4, 4, 5),
+    # attenuation with values around its 0.001 threshold
+    act = (rng.random((30, 28, 20)) * 3.0).astype(np.float32)
+    atn = (rng.random((30, 28, 20)) * 0.004).astype(np.float32)
+    with tempfile.TemporaryDirectory() as tmp:
+        fa = _interfile(tmp, "act", act, (4.0, 4.0, 5.0))
+        fm = _interfile(tmp, "atn", atn, (4.0, 4.0, 5.0))
+        loaded, size, scale = Utils.LoadImage(fa)
+        assert np.array_equal(loaded, act)
+        T.CALLS.clear()
+        size_desired = [96.0, 88.0, None]
+        scale_desired = np.array([8.0, 8.0, 10.0])
+        a, m, sd, dd = Utils.PrepareImages(fa, fm, size_desired, scale_desired)
+        out["prep_act"] = act
+        out["prep_atn"] = atn
+        out["prep_scale"] = np.array([4.0, 4.0, 5.0])
+        out["prep_size_desired_in"] = np.array([96.0, 88.0, np.nan])
+        out["prep_scale_desired"] = scale_desired
+        out["prep_act_cropped"] = a
+        out["prep_atn_cropped_thresholded"] = m
+        out["prep_size_desired"] = np.asarray(sd, dtype=np.float64)
+        out["prep_dims_desired"] = np.asarray(dd)
+        out["prep_resize_shapes"] = np.array([c[1] for c in T.CALLS])
+    _save("prep", **out)
 
 
 def main():
@@ -533,6 +604,8 @@ def main():
         gen_span(R)
     if "listmode" in which:
         gen_listmode(R)
+    if "prep" in which:
+        gen_prep(R)
 
 
 if __name__ == "__main__":

@@ -97,3 +97,26 @@ def test_no_cpu_fallback_without_gpu():
     with pytest.raises(_lib.EngineUnavailable):
         RayTracing3DTOF(np.array([4, 4, 4]), np.array([0.0, 0, 0, 1, 1, 1]),
                         np.array([-1.0, 0.5, 0.5, 2, 0.5, 0.5]))
+
+
+def test_crop_downscale_rejects_bad_arguments_without_device_work(lib):
+    from opensss_gb300 import _lib
+
+    dims = np.array([8, 8, 8], np.int32)
+    zero = np.zeros(3, np.int32)
+    sigma = np.zeros(3)
+
+    def p(a):
+        return a.ctypes.data_as(C.c_void_p)
+
+    assert lib.sss_crop_downscale_workspace_size(p(np.array([0, 4, 4], np.int32))) == 0
+    assert lib.sss_crop_downscale_workspace_size(p(dims)) > 0
+    rc = lib.sss_crop_downscale(None, p(dims), p(zero), p(zero), p(dims), p(dims), p(sigma), 1, C.c_float(0),
+                                C.c_void_p(8), C.c_void_p(8), 1 << 30, None)
+    assert rc == 1 and "null" in _lib.last_error()
+    rc = lib.sss_crop_downscale(C.c_void_p(8), p(dims), p(zero), p(zero), p(np.array([8, 0, 8], np.int32)), p(dims),
+                                p(sigma), 1, C.c_float(0), C.c_void_p(8), C.c_void_p(8), 1 << 30, None)
+    assert rc == 1 and "empty" in _lib.last_error()
+    rc = lib.sss_crop_downscale(C.c_void_p(8), p(dims), p(zero), p(zero), p(dims), p(dims), p(sigma), 1,
+                                C.c_float(0), C.c_void_p(8), C.c_void_p(8), 16, None)
+    assert rc == 7  # workspace too small
