@@ -368,8 +368,9 @@ void sss_set_timing(int enable);
 int sss_get_timing(double out[6]);
 
 /* Measured rate of the SFU 2^x instruction on the current device, in 1e9
- * results/s (no reference counterpart: the roofline denominator of the pair
- * stage).  Synchronises `stream`. */
+ * results/s (no reference counterpart: a throughput probe for the pair stage's
+ * non-factored TOF weights, which take one 2^x per voxel and bin).
+ * Synchronises `stream`. */
 int sss_probe_ex2_rate(double *gex2_per_s, void *stream);
 
 /* Measured shared-memory load bandwidth (conflict-free 16-byte loads on every

@@ -117,11 +117,7 @@ extern "C" int sss_raytrace(const int32_t grid[3], const double bounds[6], const
         return sss_set_error(SSS_ERR_CAPACITY, "sss_raytrace: capacity %d < Nx+Ny+Nz = %lld",
                              capacity, (long long)need);
     if (n_rays <= 0) return SSS_OK;
-    Grid g;
-    g.nx = grid[0];
-    g.ny = grid[1];
-    g.nz = grid[2];
-    for (int k = 0; k < 6; ++k) g.b[k] = bounds[k];
+    const Grid g = grid_of(grid[0], grid[1], grid[2], bounds);
     const int threads = 128;
     int64_t blocks = (n_rays + threads - 1) / threads;
     raytrace_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(

@@ -367,10 +367,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
             const sss_tof_problem& p = problems[it.prob];
             const long long nl = (long long)p.nru * p.ndu, cap = (long long)p.nx + p.ny + p.nz;
             LegItem& L = hleg[j];
-            L.p.g.nx = p.nx;
-            L.p.g.ny = p.ny;
-            L.p.g.nz = p.nz;
-            for (int q = 0; q < 6; ++q) L.p.g.b[q] = p.image_size[q];
+            L.p.g = grid_of(p.nx, p.ny, p.nz, p.image_size);
             L.p.act = p.activity;
             L.p.mu = p.attenuation;
             L.p.geom = p.geometry;

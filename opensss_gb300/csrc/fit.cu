@@ -372,15 +372,7 @@ int check_grid(const int32_t* grid, const double* bounds, const char* who)
     return SSS_OK;
 }
 
-Grid make_grid(const int32_t* grid, const double* bounds)
-{
-    Grid g;
-    g.nx = grid[0];
-    g.ny = grid[1];
-    g.nz = grid[2];
-    for (int k = 0; k < 6; ++k) g.b[k] = bounds[k];
-    return g;
-}
+Grid make_grid(const int32_t* grid, const double* bounds) { return grid_of(grid[0], grid[1], grid[2], bounds); }
 
 unsigned blocks_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 

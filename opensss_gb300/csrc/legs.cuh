@@ -63,7 +63,8 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
             // expression decides whether a corner-grazing segment is zero or
             // not (that decides whether a leg carries activity, :483-488)
             const double dt = tb - ta;
-            float len = fabs(dt) < 1e-9 ? (float)ref_length(r, ta, tb) : vlen * (float)fabs(dt);
+            const float adt = (float)fabs(dt);  // the threshold is compared in FP32
+            float len = adt < 1e-9f ? (float)ref_length(r, ta, tb) : vlen * adt;
             float a = __ldg(P.act + v) * len;
             musum = fmaf(__ldg(P.mu + v), len, musum);
             asum += a;

@@ -5,16 +5,16 @@
 //   1. scatter_points_kernel — ordered lattice compaction of mu > 0 points.
 //   2. leg_kernel   — one thread per (scatter point, sampled crystal): FP64
 //      Amanatides-Woo walk (bit-identical voxel sequence), FP32 integrals of
-//      mu and activity, incidence term, and the activity-weighted voxel list
-//      (act*len, TOF sample offset) written voxel-major so that the 32 lanes
-//      of a warp read 32 neighbouring legs in one coalesced access.
-//   3. pair_kernel  — persistent warps pull (slice, leg-1, 32-leg-2 chunk)
-//      tasks; each lane owns one detector pair, loops over the slice's
+//      mu and activity, incidence term, and the list of the leg's non-zero
+//      activity voxels (act*len, TOF sample offset), one list per leg.
+//   3. pair_kernel  — persistent warps pull (slice, walking leg, 32-partner
+//      chunk) tasks; each lane owns one detector pair, loops over the slice's
 //      scatter points, evaluates the Klein-Nishina x efficiency x attenuation
-//      factors once per pair and the Gaussian TOF weights per voxel and bin
-//      with the SFU (2^x), accumulates the slice numerator and count in
-//      registers and adds numerator/count to the output (per-slice
-//      normalisation, :555-557).
+//      factors once per pair, and for each voxel of the walking leg (staged in
+//      shared memory, read as broadcasts) adds the factored TOF weights
+//      [A r^b] G[n][b] of every bin from shared-memory tables; the slice
+//      numerator and count stay in registers and numerator/count is added to
+//      the output (per-slice normalisation, :555-557).
 // Nothing per voxel or per pair reaches HBM except the leg lists themselves.
 #include <algorithm>
 #include <mutex>
@@ -308,10 +308,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
 
 
     LegParams LP;
-    LP.g.nx = p->nx;
-    LP.g.ny = p->ny;
-    LP.g.nz = p->nz;
-    for (int k = 0; k < 6; ++k) LP.g.b[k] = p->image_size[k];
+    LP.g = grid_of(p->nx, p->ny, p->nz, p->image_size);
     LP.act = p->activity;
     LP.mu = p->attenuation;
     LP.geom = p->geometry;

@@ -21,8 +21,23 @@ __device__ __forceinline__ double pymax(double a, double b) { return (b > a) ? b
 
 struct Grid {
     int nx, ny, nz;
-    double b[6];  // xMin yMin zMin xMax yMax zMax
+    double b[6];   // xMin yMin zMin xMax yMax zMax
+    double vs[3];  // voxel sizes (b[3+k] - b[k]) / n_k, set by grid_of (:80-82)
 };
+
+// A grid with its voxel sizes, computed once per launch with the reference's
+// IEEE operations (one subtraction and one division, no fused multiply-add).
+__host__ __device__ inline Grid grid_of(int nx, int ny, int nz, const double* bounds)
+{
+    Grid g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    for (int k = 0; k < 6; ++k) g.b[k] = bounds[k];
+    const double n[3] = {(double)nx, (double)ny, (double)nz};
+    for (int k = 0; k < 3; ++k) g.vs[k] = (bounds[3 + k] - bounds[k]) / n[k];
+    return g;
+}
 
 // Parametric state of one ray after set-up.
 struct Ray {
@@ -119,9 +134,7 @@ __device__ __forceinline__ bool ray_setup(const Grid& g, const double* lc, doubl
     tmin = pymax(tmin, 0.0);
     tmax = pymin(tmax, 1.0);
     const double nx = (double)g.nx, ny = (double)g.ny, nz = (double)g.nz;
-    double vx = div64(sub64(g.b[3], g.b[0]), nx);
-    double vy = div64(sub64(g.b[4], g.b[1]), ny);
-    double vz = div64(sub64(g.b[5], g.b[2]), nz);
+    const double vx = g.vs[0], vy = g.vs[1], vz = g.vs[2];
     r.xv = sub64(lc[3], lc[0]);
     r.yv = sub64(lc[4], lc[1]);
     r.zv = sub64(lc[5], lc[2]);
@@ -157,14 +170,21 @@ __device__ __forceinline__ int ray_walk(const Grid& g, Ray& r, int cap, Visit&& 
     int n = 1;
     while (r.X != r.xe || r.Y != r.ye || r.Z != r.ze) {
         if (n >= cap) return -1;
-        double t;
-        if (r.xt < r.yt) {
-            if (r.xt < r.zt) { r.X += r.xs; t = r.xt; r.xt = add64(r.xt, r.xd); }
-            else { r.Z += r.zs; t = r.zt; r.zt = add64(r.zt, r.zd); }
-        } else {
-            if (r.yt < r.zt) { r.Y += r.ys; t = r.yt; r.yt = add64(r.yt, r.yd); }
-            else { r.Z += r.zs; t = r.zt; r.zt = add64(r.zt, r.zd); }
-        }
+        // The reference's choice (:133-150): x if xt < yt and xt < zt, y if
+        // yt <= xt and yt < zt, else z; made with selects so that the lanes of a
+        // warp stepping along different axes share one FP64 add.
+        const bool xy = r.xt < r.yt;
+        const double a = xy ? r.xt : r.yt;
+        const bool pa = a < r.zt;
+        const bool sx = pa && xy, sy = pa && !xy;
+        const double t = pa ? a : r.zt;
+        const double tn = add64(t, sx ? r.xd : (sy ? r.yd : r.zd));
+        r.xt = sx ? tn : r.xt;
+        r.yt = sy ? tn : r.yt;
+        r.zt = pa ? r.zt : tn;
+        r.X += sx ? r.xs : 0;
+        r.Y += sy ? r.ys : 0;
+        r.Z += pa ? 0 : r.zs;
         visit(n - 1, cur, tprev, t);
         tprev = t;
         cur = sub2ind(g, r.X, r.Y, r.Z);
