@@ -46,7 +46,7 @@ def _pairs(nru, ndu):
 def _workload():
     from opensss_gb300 import workloads as W
 
-    return W.config2(seed=0)
+    return W.tof13_64x64x48(seed=0)
 
 
 def _config(pr, extra=None):
@@ -402,7 +402,7 @@ def run_batch(dev, args, att):
     from opensss_gb300.batch import BatchSSS
     from opensss_gb300.engine import fortran_flat
 
-    inst = W.config3_instances(args.batch_size, seed=0)
+    inst = W.uneven_instances(args.batch_size, seed=0)
     engines, jobs = [], []
     for pr in inst:
         e = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
@@ -470,7 +470,7 @@ def _small_batch(dev, args, att):
     from opensss_gb300.batch import BatchSSS
     from opensss_gb300.engine import fortran_flat
 
-    inst = [W.config1(seed=100 + i) for i in range(64)]
+    inst = [W.nontof_40x40x20(seed=100 + i) for i in range(64)]
     pr0 = inst[0]
     e = TofSSS(pr0.scanner.geometry, pr0.scanner.normals, pr0.scanner.detector_size_mm, att,
                pr0.energy_resolution, pr0.energy_threshold, pr0.nr_rings_used, pr0.nr_detectors_used,
@@ -527,7 +527,7 @@ def run_precision(dev, args, att):
     from opensss_gb300.Interpolation import upsample_device
     from opensss_gb300.TailsMask import tail_mask_device
 
-    pr = W.config4(seed=0)
+    pr = W.tof33_128x128x96(seed=0)
     eng = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att,
                  pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used,
                  pr.sample_step, pr.tof_resolution, pr.tof_range, pr.nr_bins, device=dev)
@@ -796,7 +796,7 @@ def _probe_peaks():
 
 
 def _traffic():
-    path = os.path.join(ROOT, "profiles", "pair_kernel_c2.md")
+    path = os.path.join(ROOT, "profiles", "pair_kernel_tof13_64x64x48.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch:"):

@@ -54,7 +54,7 @@ def case_mask(reps):
     """Tail mask of the 64x64x48 phantom on a 380 x 40 scanner, AF 4."""
     from .TailsMask import tail_mask_device
 
-    pr = W.config2()
+    pr = W.tof13_64x64x48()
     sc = W.ring_scanner(380, 40, radius_cm=41.0, ring_pitch_cm=0.64)
     lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, 40, ID_Shidt=False)
     for _ in range(reps):
@@ -66,7 +66,7 @@ def case_fit(reps):
     a 380 x 40 scanner, AF 4."""
     from .BackProjection import fit_bins_device
 
-    pr = W.config2()
+    pr = W.tof13_64x64x48()
     sc = W.ring_scanner(380, 40, radius_cm=41.0, ring_pitch_cm=0.64)
     lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, 40, ID_Shidt=False)
     shp = (381 * 190, 1600)
@@ -99,7 +99,7 @@ def case_listmode(reps):
 
 def case_pair(reps):
     """The 64x64x48, 16 x 48, 13-bin instance on its first 400 scatter points."""
-    pr = W.config2()
+    pr = W.tof13_64x64x48()
     e = _engine(pr)
     for _ in range(reps):
         e.run(pr.activity, pr.attenuation, pr.image_size, max_points=400)
@@ -109,7 +109,7 @@ def case_batch(reps):
     """Eight instances of the uneven-batch generator as one plan."""
     from .batch import BatchSSS
 
-    inst = W.config3_instances(8, seed=3)
+    inst = W.uneven_instances(8, seed=3)
     b = BatchSSS([(_engine(pr), pr.activity, pr.attenuation, pr.image_size) for pr in inst],
                  workspace_bytes=4 << 30)
     for _ in range(reps):

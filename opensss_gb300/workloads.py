@@ -165,19 +165,19 @@ def make_problem(name: str, shape, voxel_cm, nru: int, ndu: int, nr_bins: int,
                       energy_threshold, tof_resolution_ps, tof_range, nr_bins)
 
 
-def config1(seed: int = 0) -> SSSProblem:
+def nontof_40x40x20(seed: int = 0) -> SSSProblem:
     """Plain non-TOF SSS, small: 40x40x20 @ 10 mm, 8 rings x 32 detectors,
     one TOF bin with a 1e6 ps kernel (unit TOF weights)."""
-    return make_problem("c1-nontof-40x40x20", (40, 40, 20), 1.0, 8, 32, 1, None, 1.0e6, seed)
+    return make_problem("nontof-40x40x20", (40, 40, 20), 1.0, 8, 32, 1, None, 1.0e6, seed)
 
 
-def config2(seed: int = 0) -> SSSProblem:
+def tof13_64x64x48(seed: int = 0) -> SSSProblem:
     """Plain TOF-SSS single instance: 64x64x48 @ 6 mm, 16 rings x 48
     detectors, 13 TOF bins of 39 mm, 214 ps FWHM timing kernel."""
-    return make_problem("c2-tof13-64x64x48", (64, 64, 48), 0.6, 16, 48, 13, 3.9, 214.0, seed)
+    return make_problem("tof13-64x64x48", (64, 64, 48), 0.6, 16, 48, 13, 3.9, 214.0, seed)
 
 
-def config4(seed: int = 0) -> SSSProblem:
+def tof33_128x128x96(seed: int = 0) -> SSSProblem:
     """Precision stress: 128x128x96 @ 4 mm, 32 rings x 96 detectors,
     33 TOF bins of 15 mm, 214 ps FWHM.
 
@@ -185,11 +185,11 @@ def config4(seed: int = 0) -> SSSProblem:
     736 of the 35 million legs of this volume (scatter points on voxel faces
     to that crystal, through exact voxel corners) make the reference's
     traversal run past Nx+Ny+Nz voxels and raise IndexError."""
-    return make_problem("c4-tof33-128x128x96", (128, 128, 96), 0.4, 32, 96, 33, 1.5, 214.0, seed,
+    return make_problem("tof33-128x128x96", (128, 128, 96), 0.4, 32, 96, 33, 1.5, 214.0, seed,
                         scanner=ring_scanner(phase=0.5))
 
 
-def config3_instances(count: int = 64, seed: int = 0):
+def uneven_instances(count: int = 64, seed: int = 0):
     """Uneven batch: volumes from 32x32x24 to 96x96x64 on a 40 cm FOV,
     24-64 detectors x 8-24 rings, TOF bins in {1, 13, 33}, body radius
     8-18 cm, all drawn from ``seed``.
@@ -219,7 +219,7 @@ def config3_instances(count: int = 64, seed: int = 0):
             width, res = 3.9, 214.0
         else:
             width, res = 1.5, 214.0
-        out.append(make_problem(f"c3-{i}", (n, n, nz), vox, nru, ndu, bins, width, res,
+        out.append(make_problem(f"uneven-{i}", (n, n, nz), vox, nru, ndu, bins, width, res,
                                 seed=seed * 1000 + i, radius_cm=min(radius, 19.0), scanner=scanner))
     return out
 
@@ -241,9 +241,9 @@ def served_beds(seed: int = 0):
     the plain non-TOF size (40x40x20 @ 1 cm, 8 rings x 32 crystals, phantoms
     seeded per bed) and four large ones drawn by the uneven-batch generator
     (seed 5).  Returns (small, large)."""
-    small = [dataclasses.replace(config1(seed=seed * 10 + b), name=f"bed{b}-small") for b in range(4)]
+    small = [dataclasses.replace(nontof_40x40x20(seed=seed * 10 + b), name=f"bed{b}-small") for b in range(4)]
     large = [dataclasses.replace(pr, name=f"bed{b}-large")
-             for b, pr in enumerate(config3_instances(4, seed=5))]
+             for b, pr in enumerate(uneven_instances(4, seed=5))]
     return small, large
 
 

@@ -193,7 +193,7 @@ def gen_sss(R, which):
                      ("sss_tiny_b5", W.tiny_problem(5, seed=5, shape=(14, 14, 8), nd=64, nr=8,
                                                     nru=4, ndu=10, voxel_cm=1.7))]
     if "c1" in which:
-        problems.append(("sss_c1", W.config1(seed=0)))
+        problems.append(("sss_nontof_40x40x20", W.nontof_40x40x20(seed=0)))
     for name, pr in problems:
         nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
         LC, SI, _ = _sino(R, nd, nr)
@@ -499,7 +499,7 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_c1", "upsample", "upsample_lut", "mask", "fit", "span", "listmode", "prep"]
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "upsample", "upsample_lut", "mask", "fit", "span", "listmode", "prep"]
 
 
 # ---------------------------------------------------------------- image preparation

@@ -58,7 +58,7 @@ def _valid_mask(nru, ndu):
     return ((d1 < d2) | ((d1 == d2) & (ri1 != ri2))).reshape(nru * nru, ndu, ndu)
 
 
-@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_c1"])
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_nontof_40x40x20"])
 def test_sss_matches_reference(cuda_ok, att_table, name):
     g = golden(name)
     pr = problem_from_golden(g)
@@ -73,7 +73,7 @@ def test_sss_matches_reference(cuda_ok, att_table, name):
 def test_scatter_points_match_oracle(cuda_ok, att_table):
     from opensss_gb300 import workloads as W
 
-    pr = W.config2()
+    pr = W.tof13_64x64x48()
     eng = _engine(pr, att_table)
     from opensss_gb300.engine import fortran_flat
 
@@ -88,8 +88,8 @@ def test_scatter_points_match_oracle(cuda_ok, att_table):
     assert np.array_equal(pts[:, 3].astype(np.int64), sl)
 
 
-@pytest.mark.parametrize("cfg,points", [("config2", 160), ("config4", 6)])
-def test_sss_large_configs_against_fp64_oracle(cuda_ok, att_table, cfg, points):
+@pytest.mark.parametrize("cfg,points", [("tof13_64x64x48", 160), ("tof33_128x128x96", 6)])
+def test_sss_large_problems_against_fp64_oracle(cuda_ok, att_table, cfg, points):
     """Full benchmark geometry, bounded number of scatter points."""
     from opensss_gb300 import workloads as W
 
@@ -146,7 +146,7 @@ def test_tof_bins_sum_to_nontof(cuda_ok, att_table):
     assert rel_l2(tof.sum(axis=0), non[0]) < 1e-4
 
 
-@pytest.mark.parametrize("name", ["sss_tiny_b5", "sss_c1"])
+@pytest.mark.parametrize("name", ["sss_tiny_b5", "sss_nontof_40x40x20"])
 def test_kahan_reduction_matches_reference(cuda_ok, att_table, name):
     """SSS_FLAG_KAHAN (compensated sum over the scatter points) stays within
     the same 1e-4 bar and agrees with the plain reduction to FP32 noise."""
@@ -160,17 +160,17 @@ def test_kahan_reduction_matches_reference(cuda_ok, att_table, name):
     assert rel_l2(kahan, plain) < 1e-5
 
 
-def test_kahan_on_config4_sample(cuda_ok, att_table):
+def test_kahan_on_33bin_sample(cuda_ok, att_table):
     from opensss_gb300 import workloads as W
 
-    pr = W.config4()
+    pr = W.tof33_128x128x96()
     got = _gpu_compact(pr, att_table, max_points=6, kahan=True)
     ref = _oracle_compact(pr, att_table, sp_end=6)
     assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
 
 
-@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_c1"])
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_nontof_40x40x20"])
 def test_unit_tof_fast_path_matches_voxel_walk(cuda_ok, att_table, name):
     """With one bin of unit weights the pairs take the legs' activity
     integrals instead of walking the voxels: same sinogram to FP32 rounding."""

@@ -58,8 +58,8 @@ def test_oracle_sss_matches_reference(name, att_table):
 
 
 @pytest.mark.slow
-def test_oracle_sss_config1_matches_reference(att_table):
-    g = golden("sss_c1")
+def test_oracle_sss_nontof_40x40x20_matches_reference(att_table):
+    g = golden("sss_nontof_40x40x20")
     pr = problem_from_golden(g)
     cmp = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
                         pr.scanner.normals, pr.scanner.detector_size_mm, att_table,

@@ -39,11 +39,11 @@ def _call(fn, p, cap, lz, device):
     return rc, pts.cpu().numpy(), count.value, slices
 
 
-@pytest.mark.parametrize("which", ["tiny", "config2"])
+@pytest.mark.parametrize("which", ["tiny", "tof13_64x64x48"])
 def test_noalloc_matches_allocating_entry_point(cuda_ok, att_table, which):
     from opensss_gb300 import _lib, workloads as W
 
-    pr = W.tiny_problem(3, seed=2) if which == "tiny" else W.config2()
+    pr = W.tiny_problem(3, seed=2) if which == "tiny" else W.tof13_64x64x48()
     eng, act, mu, p = _setup(pr, att_table)
     L = _lib.lib()
     lz = -(-pr.grid[2] // int(pr.sample_step[2]))
