@@ -66,8 +66,9 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
     st.synchronize()
     _lib.check_status(int(status.item()))
     if return_images:
-        im = images.reshape(2, 4, nvox)
-        return float(scale.item()), torch.stack([im[0, 0], im[0, 1], im[0, 2] + im[1, 2], im[0, 3] + im[1, 3]])
+        im = images.reshape(2, 2, nvox, 2)  # [block][(P, S) | (R, sens)][voxel][pair]
+        return float(scale.item()), torch.stack([im[0, 0, :, 0], im[0, 0, :, 1], im[0, 1, :, 0] + im[1, 1, :, 0],
+                                                 im[0, 1, :, 1] + im[1, 1, :, 1]])
     return float(scale.item())
 
 

@@ -225,8 +225,8 @@ struct FitParams {
     const long long* scat_cell; // [cell] offset of the scatter value's cell
     const long long* scat_ring; // [slice] offset of the scatter value's slice
     int scat_clamp;             // clamp the scatter value at 0 (upsampling's fill, :163)
-    float* img;                 // [bin][4][nvox]: P, S, R, sensitivity; block nbins holds the R and
-                                // sensitivity of the LORs that every bin uses
+    float* img;                 // [bin][2][nvox] float2: (P, S) then (R, sensitivity); block nbins
+                                // holds the R and sensitivity of the LORs that every bin uses
     int32_t* status;
 };
 
@@ -290,48 +290,45 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
         }
         const double w = P.length_weighted ? div64(ref_length(r, t0, t1), total) : 0.0;
         const float rw = P.length_weighted ? (float)mul64((double)rv, w) : ar;
+        // (P, S) and (R, sensitivity) go in pairs, one vector atomic each
         for (unsigned long long rest = bins; rest; rest &= rest - 1) {
             const int b = __ffsll((long long)rest) - 1;
-            float* img = P.img + (long long)b * 4 * P.nvox;
+            float2* ps = reinterpret_cast<float2*>(P.img + (long long)b * 4 * P.nvox);
             // one bin: the LOR's values, else re-read per voxel (L1-resident)
             const float s = P.nbins == 1 ? s0 : m * fit_scatter(P, b, cell, slice);
             const float pv = P.nbins == 1 ? p0 : m * P.prompts[b * P.prompt_stride + c];
-            if (P.length_weighted) {
-                atomicAdd(img + v, (float)mul64((double)pv, w));
-                atomicAdd(img + P.nvox + v, (float)mul64((double)s, w));
-            } else {
-                atomicAdd(img + v, pv / fn);
-                atomicAdd(img + P.nvox + v, s / fn);
-            }
-            if (bins != all) {  // randoms and sensitivity of this bin alone
-                atomicAdd(img + 2 * P.nvox + v, rw);
-                atomicAdd(img + 3 * P.nvox + v, 1.0f);
-            }
+            if (P.length_weighted)
+                atomicAdd(ps + v, make_float2((float)mul64((double)pv, w), (float)mul64((double)s, w)));
+            else
+                atomicAdd(ps + v, make_float2(pv / fn, s / fn));
+            if (bins != all)  // randoms and sensitivity of this bin alone
+                atomicAdd(ps + P.nvox + v, make_float2(rw, 1.0f));
         }
         if (bins == all) {  // LORs every bin uses share one randoms / sensitivity image
-            float* img = P.img + (long long)P.nbins * 4 * P.nvox;
-            atomicAdd(img + 2 * P.nvox + v, rw);
-            atomicAdd(img + 3 * P.nvox + v, 1.0f);
+            float2* rs = reinterpret_cast<float2*>(P.img + (long long)P.nbins * 4 * P.nvox) + P.nvox;
+            atomicAdd(rs + v, make_float2(rw, 1.0f));
         }
     });
     if (bad) raise_error(P.status, kErrVoxel);
 }
 
 // per voxel: Sbp, T (BackProjection.py:191-204); sums of x*T and x*x in FP64;
-// blockIdx.y = bin (images [bin][4][nvox], sums [bin][2])
+// blockIdx.y = bin (images [bin][2][nvox] float2, sums [bin][2])
 __global__ void fit_reduce_kernel(const float* __restrict__ img_all, long long nvox, int nbins,
                                   double* sums_all)
 {
-    const float* img = img_all + (long long)blockIdx.y * 4 * nvox;
-    const float* common = img_all + (long long)nbins * 4 * nvox;
+    const float2* ps = reinterpret_cast<const float2*>(img_all + (long long)blockIdx.y * 4 * nvox);
+    const float2* rs = ps + nvox;
+    const float2* common = reinterpret_cast<const float2*>(img_all + (long long)nbins * 4 * nvox) + nvox;
     double* sums = sums_all + 2 * blockIdx.y;
     double sxt = 0.0, sxx = 0.0;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nvox;
          v += (long long)gridDim.x * blockDim.x) {
-        const float sens = img[3 * nvox + v] + common[3 * nvox + v];
-        float sb = img[nvox + v] / sens;
-        float ab = img[v] / sens;
-        float rb = (img[2 * nvox + v] + common[2 * nvox + v]) / sens;
+        const float2 pv = ps[v], rv = rs[v], cv = common[v];
+        const float sens = rv.y + cv.y;
+        float sb = pv.y / sens;
+        float ab = pv.x / sens;
+        float rb = (rv.x + cv.x) / sens;
         if (isnan(sb) || isinf(sb)) sb = 0.f;
         if (isnan(ab) || isinf(ab)) ab = 0.f;
         if (isnan(rb) || isinf(rb)) rb = 0.f;
