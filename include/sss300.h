@@ -239,11 +239,11 @@ int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const flo
  * mask: mask_f32 (multiplied) or, if not NULL, mask_u8 (mask >= 1).  The
  * scatter value is scatters[scat_cell[cell] + scat_ring[slice]] (clamped at
  * 0 when scat_clamp), so an upsampled sinogram can be read straight from
- * the sampled one.  images: device workspace 8 * Nx*Ny*Nz floats: the
- * (P, S) float pairs of every voxel, then its (R, sensitivity) pairs, then the
- * (R, sensitivity) pairs shared by all bins (both halves of that last block);
- * sums: device 2 doubles; scale: device float, the fitted slope (reference:
- * float32 array of shape (1,)). */
+ * the sampled one.  images: device workspace 8 * Nx*Ny*Nz floats, 16-byte
+ * aligned: the (P, S) float pairs of every voxel, then its (R, sensitivity)
+ * pairs, then a block whose second half holds the (R, sensitivity) pairs of
+ * the LORs every bin uses; sums: device 2 doubles; scale: device float, the
+ * fitted slope (reference: float32 array of shape (1,)). */
 int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
                         const double *geometry, const int16_t *lor, const int16_t *sino_order,
                         int32_t af, const float *prompts, const float *randoms, const float *mask_f32,
@@ -273,10 +273,13 @@ int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int
  * prompts[b*prompt_stride + cell*nslices + slice] and the scatter value
  * scatters[b*scat_stride + scat_cell[cell] + scat_ring[slice]]; randoms and
  * the mask are shared.  Either sino_order (all ring pairs) or pairs (span)
- * is given.  images: device float [nbins + 1][2][Nx*Ny*Nz][2]: per bin the
- * (P, S) pairs, then the (R, sensitivity) pairs; block nbins holds the
- * randoms and sensitivity of the LORs every bin uses, so those are added
- * once; sums: device [nbins][2]; scales: device float [nbins];
+ * is given.  images: device float [nbins + 1][4 * Nx*Ny*Nz], 16-byte aligned:
+ * bins 2q and 2q+1 share blocks 2q and 2q+1 as float4 per voxel, (P, S, P, S)
+ * then (R, sensitivity, R, sensitivity); an odd last bin keeps float2 (P, S)
+ * then (R, sensitivity) pairs in its block; the second half of block nbins
+ * holds, as float2, the randoms and sensitivity of the LORs every bin uses,
+ * so those are added once; sums: device [nbins][2]; scales: device float
+ * [nbins];
  * 1 <= nbins <= 64. */
 int sss_backproject_fit_bins(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
                              const double *geometry, const int16_t *lor, const int16_t *sino_order,

@@ -225,8 +225,11 @@ struct FitParams {
     const long long* scat_cell; // [cell] offset of the scatter value's cell
     const long long* scat_ring; // [slice] offset of the scatter value's slice
     int scat_clamp;             // clamp the scatter value at 0 (upsampling's fill, :163)
-    float* img;                 // [bin][2][nvox] float2: (P, S) then (R, sensitivity); block nbins
-                                // holds the R and sensitivity of the LORs that every bin uses
+    float* img;                 // [nbins + 1][4 * nvox]: bins 2q, 2q+1 share blocks 2q, 2q+1 as
+                                // float4 (P, S, P, S) then (R, sens, R, sens); an odd last bin
+                                // has float2 (P, S) then (R, sens); block nbins holds, as float2
+                                // in its second half, the R and sensitivity of the LORs that every
+                                // bin uses
     int32_t* status;
 };
 
@@ -267,22 +270,27 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     lor_line(P.geom, P.nd, L.r1, d1, L.r2, d2, lc);
     Ray r;
     if (!ray_setup(P.g, lc, 1e-20, r)) return;
-    // first pass: voxel count (the reference divides by len(Lengths), :108-110)
-    // and, for the length-weighted back-projection, the summed length (:294-297)
-    Ray r2 = r;
+    // Voxel count (the reference divides by len(Lengths), :108-110).  Every
+    // step of the walk moves one voxel along one axis towards the end voxel,
+    // so a walk that ends crosses 1 + |dX| + |dY| + |dZ| voxels; one that would
+    // overrun is caught by the walk below.  The length-weighted back-projection
+    // needs the summed length first (:294-297), so it walks twice.
     double total = 0.0;
-    int n_vox = ray_walk(P.g, r2, P.cap, [&](int, int64_t, double t0, double t1) {
-        if (P.length_weighted) total = add64(total, ref_length(r2, t0, t1));
-    });
-    if (n_vox < 0) {
+    int n_vox = 1 + abs(r.xe - r.X) + abs(r.ye - r.Y) + abs(r.ze - r.Z);
+    if (P.length_weighted) {
+        Ray r2 = r;
+        n_vox = ray_walk(P.g, r2, P.cap, [&](int, int64_t, double t0, double t1) {
+            total = add64(total, ref_length(r2, t0, t1));
+        });
+    }
+    if (n_vox < 0 || n_vox > P.cap) {
         raise_error(P.status, kErrOverrun);
         return;
     }
-    if (n_vox == 0) return;
     const float fn = (float)n_vox;
     const float ar = rv / fn;
     bool bad = false;
-    ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
+    const int walked = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
         const long long v = lin - 1;
         if (v < 0 || v >= P.nvox) {
             bad = true;
@@ -290,19 +298,36 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
         }
         const double w = P.length_weighted ? div64(ref_length(r, t0, t1), total) : 0.0;
         const float rw = P.length_weighted ? (float)mul64((double)rv, w) : ar;
-        // (P, S) and (R, sensitivity) go in pairs, one vector atomic each
-        for (unsigned long long rest = bins; rest; rest &= rest - 1) {
-            const int b = __ffsll((long long)rest) - 1;
-            float2* ps = reinterpret_cast<float2*>(P.img + (long long)b * 4 * P.nvox);
-            // one bin: the LOR's values, else re-read per voxel (L1-resident)
+        // (P, S) of bin b from this LOR (one bin: the LOR's values, else re-read
+        // per voxel, L1-resident)
+        auto contrib = [&](int b) {
             const float s = P.nbins == 1 ? s0 : m * fit_scatter(P, b, cell, slice);
             const float pv = P.nbins == 1 ? p0 : m * P.prompts[b * P.prompt_stride + c];
-            if (P.length_weighted)
-                atomicAdd(ps + v, make_float2((float)mul64((double)pv, w), (float)mul64((double)s, w)));
-            else
-                atomicAdd(ps + v, make_float2(pv / fn, s / fn));
-            if (bins != all)  // randoms and sensitivity of this bin alone
-                atomicAdd(ps + P.nvox + v, make_float2(rw, 1.0f));
+            return P.length_weighted ? make_float2((float)mul64((double)pv, w), (float)mul64((double)s, w))
+                                     : make_float2(pv / fn, s / fn);
+        };
+        // Bins 2q and 2q+1 share float4 images, (P, S, P, S) then (R, sens, R, sens):
+        // one vector atomic each for the pair; an odd last bin uses float2 pairs.
+        const int paired = P.nbins & ~1;
+        for (unsigned long long rest = bins; rest;) {
+            const int b = __ffsll((long long)rest) - 1;
+            if (b < paired) {
+                const int b0 = b & ~1;
+                const bool in0 = (bins >> b0) & 1ull, in1 = (bins >> (b0 + 1)) & 1ull;
+                rest &= ~(3ull << b0);
+                const float2 c0 = in0 ? contrib(b0) : make_float2(0.f, 0.f);
+                const float2 c1 = in1 ? contrib(b0 + 1) : make_float2(0.f, 0.f);
+                float4* ps4 = reinterpret_cast<float4*>(P.img + (long long)b0 * 4 * P.nvox);
+                atomicAdd(ps4 + v, make_float4(c0.x, c0.y, c1.x, c1.y));
+                if (bins != all)  // randoms and sensitivity of these bins alone
+                    atomicAdd(ps4 + P.nvox + v, make_float4(in0 ? rw : 0.f, in0 ? 1.f : 0.f, in1 ? rw : 0.f,
+                                                            in1 ? 1.f : 0.f));
+            } else {
+                rest &= rest - 1;
+                float2* ps = reinterpret_cast<float2*>(P.img + (long long)b * 4 * P.nvox);
+                atomicAdd(ps + v, contrib(b));
+                if (bins != all) atomicAdd(ps + P.nvox + v, make_float2(rw, 1.0f));
+            }
         }
         if (bins == all) {  // LORs every bin uses share one randoms / sensitivity image
             float2* rs = reinterpret_cast<float2*>(P.img + (long long)P.nbins * 4 * P.nvox) + P.nvox;
@@ -310,21 +335,33 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
         }
     });
     if (bad) raise_error(P.status, kErrVoxel);
+    if (walked != n_vox) raise_error(P.status, kErrOverrun);
 }
 
 // per voxel: Sbp, T (BackProjection.py:191-204); sums of x*T and x*x in FP64;
-// blockIdx.y = bin (images [bin][2][nvox] float2, sums [bin][2])
+// blockIdx.y = bin (images as bp_kernel writes them, sums [bin][2])
 __global__ void fit_reduce_kernel(const float* __restrict__ img_all, long long nvox, int nbins,
                                   double* sums_all)
 {
-    const float2* ps = reinterpret_cast<const float2*>(img_all + (long long)blockIdx.y * 4 * nvox);
-    const float2* rs = ps + nvox;
+    const int b = blockIdx.y;
+    const bool pair = b < (nbins & ~1);  // float4 images shared with the neighbouring bin
+    const float* blk = img_all + (long long)(pair ? (b & ~1) : b) * 4 * nvox;
     const float2* common = reinterpret_cast<const float2*>(img_all + (long long)nbins * 4 * nvox) + nvox;
     double* sums = sums_all + 2 * blockIdx.y;
     double sxt = 0.0, sxx = 0.0;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nvox;
          v += (long long)gridDim.x * blockDim.x) {
-        const float2 pv = ps[v], rv = rs[v], cv = common[v];
+        float2 pv, rv;
+        if (pair) {
+            const float4 p4 = reinterpret_cast<const float4*>(blk)[v];
+            const float4 r4 = reinterpret_cast<const float4*>(blk)[nvox + v];
+            pv = (b & 1) ? make_float2(p4.z, p4.w) : make_float2(p4.x, p4.y);
+            rv = (b & 1) ? make_float2(r4.z, r4.w) : make_float2(r4.x, r4.y);
+        } else {
+            pv = reinterpret_cast<const float2*>(blk)[v];
+            rv = reinterpret_cast<const float2*>(blk)[nvox + v];
+        }
+        const float2 cv = common[v];
         const float sens = rv.y + cv.y;
         float sb = pv.y / sens;
         float ab = pv.x / sens;
@@ -471,6 +508,8 @@ int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, i
     if (!geometry || !lor || !prompts || !randoms || (!mask_f32 && !mask_u8) || !scatters || !scat_cell ||
         !scat_ring || !images || !sums || !scale || nr < 1 || nd < 2 || af < 1 || nbins < 1 || nbins > 64)
         return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: bad argument");
+    if ((uintptr_t)images % 16 != 0)  // vector atomics on float4 / float2 image entries
+        return sss_set_error(SSS_ERR_INVALID, "sss_backproject_fit: images must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     FitParams P;
     P.pairs = pairs;

@@ -130,9 +130,11 @@ def test_fit_reads_upsampled_scatter_without_materialising(cuda_ok):
     assert abs(s - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
 
 
-@pytest.mark.parametrize("case", range(2))
-def test_all_bins_in_one_pass_match_per_bin_fits(cuda_ok, case):
-    """sss_backproject_fit_bins gives every bin the scale of its own fit."""
+@pytest.mark.parametrize("case,nb", [(0, 3), (1, 3), (0, 4)])
+def test_all_bins_in_one_pass_match_per_bin_fits(cuda_ok, case, nb):
+    """sss_backproject_fit_bins gives every bin the scale of its own fit: bins
+    paired into shared vector images, an odd last bin on its own, and bins of
+    a pair that skip different LORs."""
     import torch
 
     from opensss_gb300.BackProjection import fit_bins_device, fit_device
@@ -143,9 +145,12 @@ def test_all_bins_in_one_pass_match_per_bin_fits(cuda_ok, case):
     shp = g[f"case{case}_scatter"].shape
     ncell, nsl = shp[0] * shp[1], shp[2]
     rng = np.random.default_rng(case)
-    scat = np.stack([g[f"case{case}_scatter"] * f for f in (1.0, 0.5, 2.0)])
+    factors = (1.0, 0.5, 2.0, 0.8)[:nb]
+    scat = np.stack([g[f"case{case}_scatter"] * f for f in factors])
     scat[1][rng.uniform(size=shp) < 0.2] = 0  # bins skip different LORs
-    prm = np.stack([rng.poisson(3.0 * f, size=shp).astype(np.float32) for f in (1.0, 0.7, 1.5)])
+    if nb > 3:
+        scat[2][rng.uniform(size=shp) < 0.3] = 0
+    prm = np.stack([rng.poisson(3.0 * f, size=shp).astype(np.float32) for f in (1.0, 0.7, 1.5, 1.2)[:nb]])
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a.reshape(-1, ncell, nsl))).cuda()  # noqa: E731
     cell = np.arange(ncell, dtype=np.int64) * nsl
     ring = np.arange(nsl, dtype=np.int64)
@@ -154,7 +159,7 @@ def test_all_bins_in_one_pass_match_per_bin_fits(cuda_ok, case):
     order = si[:nr, :nr].T
     got = fit_bins_device(dev(prm), rnd, mask, dev(scat).reshape(-1), ncell * nsl, cell, ring,
                           g[f"case{case}_grid"], g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, order, af)
-    for b in range(3):
+    for b in range(nb):
         ref = fit_device(dev(prm)[b], rnd, mask, dev(scat)[b], cell, ring, g[f"case{case}_grid"],
                          g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, order, af)
         assert abs(float(got[b]) - ref) <= 1e-5 * abs(ref)
