@@ -202,6 +202,11 @@ def run_ours(args, rank, world, local_rank):
     nsp = int(counts.sum()) if args.max_points is None else min(int(counts.sum()), args.max_points)
     units = nsp * P * pr.nr_bins
 
+    # launch shapes picked by the tuner on the first 400 scatter points (untimed)
+    from opensss_gb300 import autotune
+
+    tuned = None if args.no_autotune else autotune.tune(eng, act, mu, pr.image_size, sample_points=400,
+                                                        use_cache=False)
     L.sss_set_timing(1)
     out = torch.empty((pr.nr_bins, eng.nl, eng.nl), dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
@@ -310,6 +315,8 @@ def run_ours(args, rank, world, local_rank):
                     "d2h_bytes_per_step": d2h,
                     "path": "TofSSS.run on pinned host volumes, compact result copied back"},
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+            "launch_shape": {"pair_warps": eng.pair_warps, "leg_threads": eng.leg_threads,
+                             "tuned": tuned},
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
             "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
             "batch": batch, "precision": precision, "serving": serving, "listmode": listmode,
@@ -412,7 +419,7 @@ def run_batch(dev, args, att):
         jobs.append((e, fortran_flat(pr.activity, dev), fortran_flat(pr.attenuation, dev), pr.image_size,
                      pr.grid))
     t0 = time.perf_counter()
-    b = BatchSSS(jobs)
+    b = BatchSSS(jobs, autotune=not args.no_autotune)
     torch.cuda.synchronize(dev)
     plan_s = time.perf_counter() - t0
     b.run()  # checked run (status word) before capturing
@@ -448,8 +455,10 @@ def run_batch(dev, args, att):
     mean_ms = statistics.mean(ms)
     res = {"workload": f"{len(inst)} uneven instances (seed 0)", "units_per_step": b.units,
            "scatter_points": b.points, "waves": b.waves, "launches_per_step": b.launches,
-           "graph": True, "steps": steps, "ms_per_step": mean_ms, "value": b.units / (mean_ms / 1e3),
-           "unit": UNIT, "plan_s": plan_s, "plain_sequential_ms": solo_ms,
+           "graph": True, "launch_shapes": b.tuned, "steps": steps, "ms_per_step": mean_ms,
+           "value": b.units / (mean_ms / 1e3),
+           "unit": UNIT, "plan_s": plan_s, "plan_includes_autotune": not args.no_autotune,
+           "plain_sequential_ms": solo_ms,
            "plain_sequential_value": b.units / (solo_ms / 1e3),
            "speedup_vs_plain": solo_ms / mean_ms, "clocks": clk.summary(),
            "plain_note": "scatter points, host sync and leg/pair waves per instance, kernels only"}
@@ -832,6 +841,7 @@ def main():
                     help="served small requests checked against the FP64 oracle")
     ap.add_argument("--no-listmode", action="store_true", help="skip the list-mode histogramming")
     ap.add_argument("--no-prep", action="store_true", help="skip the image preparation (CropAndDownscale)")
+    ap.add_argument("--no-autotune", action="store_true", help="run with the library's default launch shapes")
     ap.add_argument("--listmode-events", type=int, default=50_000_000)
     ap.add_argument("--listmode-cpu-events", type=int, default=200_000)
     ap.add_argument("--max-points", type=int, default=None,

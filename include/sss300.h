@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SSS300_ABI_VERSION 2
+#define SSS300_ABI_VERSION 3
 
 enum {
     SSS_OK = 0,
@@ -92,7 +92,16 @@ typedef struct sss_tof_problem {
                                       FP64 product is 0 (:505-509) */
     const float *atten_ratio;      /* device, [2000]: water mu(E)/mu(511) (:117-120) */
     int32_t flags;                 /* SSS_FLAG_*; 0 = the plain FP32 reduction */
+    int32_t pair_warps;            /* launch shape (no reference counterpart): warps per pair-kernel
+                                      block, 0 = sss_pair_warps_max(nbins, flags), else 1..that */
+    int32_t leg_threads;           /* threads per leg-kernel block, 0 = 128, else a multiple of 32
+                                      up to 256 */
 } sss_tof_problem;
+
+/* Largest (and default) pair-kernel block of a bin count, in warps: the
+ * kernels are compiled for it; a smaller pair_warps launches fewer warps a
+ * block (no reference counterpart: the bound of the launch-shape tuner). */
+int sss_pair_warps_max(int32_t nbins, int32_t flags);
 
 /* sss_tof_problem.flags.  SSS_FLAG_KAHAN: sum each detector pair's per-point
  * terms over a z-slice's scatter points with Kahan's compensated addition
@@ -170,7 +179,9 @@ int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t nd
  * must not) and may be captured in a CUDA graph.  The problems' device
  * arrays, the outputs and the workspace must outlive the plan's last run.
  * sss_batch_info: info[0] waves, info[1] kernel launches per run, info[2]
- * detector-pair x bin evaluations per run, info[3] scatter points. */
+ * detector-pair x bin evaluations per run, info[3] scatter points.  Launch
+ * shapes: the leg launches use problem 0's leg_threads, and each TOF class's
+ * pair launch uses the pair_warps of its first problem. */
 typedef struct sss_batch sss_batch;
 int sss_batch_plan(const sss_tof_problem *problems, int32_t n, float *const *outs, void *workspace,
                    size_t workspace_bytes, int32_t *status, sss_batch **plan, void *stream);

@@ -14,7 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libsss300.so")
 
 SSS_OK = 0
-ABI_VERSION = 2  # SSS300_ABI_VERSION of include/sss300.h
+ABI_VERSION = 3  # SSS300_ABI_VERSION of include/sss300.h
 ERROR_NAMES = {
     1: "SSS_ERR_INVALID", 2: "SSS_ERR_CUDA", 3: "SSS_ERR_OVERRUN", 4: "SSS_ERR_TOF_RANGE",
     5: "SSS_ERR_ENERGY", 6: "SSS_ERR_VOXEL", 7: "SSS_ERR_WORKSPACE", 8: "SSS_ERR_CAPACITY",
@@ -52,6 +52,7 @@ class TofProblem(C.Structure):
         ("tof_bin_width", _D), ("tof_resolution", _D),
         ("tof_log2w", _P), ("efficiency", _P), ("atten_ratio", _P),
         ("flags", _I32),
+        ("pair_warps", _I32), ("leg_threads", _I32),
     ]
 
 
@@ -111,6 +112,7 @@ SIGNATURES = {
                                       _P, _P, _P, C.c_size_t, _P, _P]),
     "sss_crop_downscale_workspace_size": (C.c_size_t, [_P]),
     "sss_crop_downscale": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int, C.c_float, _P, _P, C.c_size_t, _P]),
+    "sss_pair_warps_max": (C.c_int, [_I32, _I32]),
     "sss_set_timing": (None, [C.c_int]),
     "sss_get_timing": (C.c_int, [_P]),
     "sss_probe_ex2_rate": (C.c_int, [C.POINTER(_D), _P]),

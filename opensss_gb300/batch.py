@@ -19,6 +19,37 @@ from . import _lib
 from .engine import WS_BUDGET_BYTES, TofSSS, _ptr, fortran_flat
 
 
+def _tune_classes(jobs) -> dict:
+    """One autotune per TOF class (bins, bin width, resolution) on its
+    largest problem; every engine of the class gets that class's pair shape,
+    all engines the leg shape of the class with the most legs."""
+    from . import autotune
+
+    classes: dict = {}
+    for job in jobs:
+        eng = job[0]
+        shape = tuple(int(s) for s in (job[4] if len(job) > 4 else np.shape(job[1])))
+        key = (eng.nbins, round(eng.tof_range, 6), round(eng.tof_resolution, 6))
+        work = eng.nl * int(np.prod(shape))
+        if key not in classes or work > classes[key][0]:
+            classes[key] = (work, job, shape)
+    results, legs_best = {}, (-1, 0)
+    for key, (work, job, shape) in classes.items():
+        eng, act, mu, size = job[:4]
+        flat = len(job) > 4
+        r = autotune.tune(eng, act, mu, size, shape=shape if flat else None)
+        results[key] = r
+        if work > legs_best[0]:
+            legs_best = (work, int(r["leg_threads"]))
+    for job in jobs:
+        eng = job[0]
+        key = (eng.nbins, round(eng.tof_range, 6), round(eng.tof_resolution, 6))
+        eng.pair_warps = int(results[key]["pair_warps"])
+        eng.leg_threads = legs_best[1]
+    return {f"bins={k[0]}": {"pair_warps": v["pair_warps"], "leg_threads": v["leg_threads"],
+                             "cached": v["cached"]} for k, v in results.items()}
+
+
 class BatchSSS:
     """A planned batch of TOF-SSS problems.
 
@@ -30,15 +61,20 @@ class BatchSSS:
     """
 
     def __init__(self, jobs, workspace_bytes: int | None = None, stream=None, points=None,
-                 workspace: torch.Tensor | None = None, outs=None):
+                 workspace: torch.Tensor | None = None, outs=None, autotune: bool = False):
         """``points``: optional per-job ``(points, slice_counts)`` from
         ``TofSSS.scatter_points`` (they depend on the attenuation map only);
         with them the plan skips the scatter-point pass.  ``workspace`` /
         ``outs``: caller-owned device buffers to plan into (otherwise
-        allocated here)."""
+        allocated here).  ``autotune``: before planning, pick the launch
+        shapes of each TOF class on its largest problem
+        (:func:`opensss_gb300.autotune.tune`, cached per device and size
+        class); the plan's leg launches take the shape of the class with the
+        most legs."""
         if not jobs:
             raise ValueError("empty batch")
         L = _lib.lib()
+        self.tuned = _tune_classes(jobs) if autotune else None
         self.engines: list[TofSSS] = []
         self.shapes = []
         self._keep = []

@@ -38,7 +38,7 @@ struct PairItem {
     long long task_begin;     // prefix over the launch's items of nl * nchunks
 };
 
-__global__ void __launch_bounds__(128) batch_leg_kernel(const LegItem* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(kLegThreadsMax) batch_leg_kernel(const LegItem* __restrict__ items, int nitems,
                                                         long long total)
 {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,7 +116,7 @@ BatchPairFn pick_batch_pairs(int nbins)
 
 // Shared-memory opt-in and persistent grid size of a pair launch, decided at
 // plan time so that a run only enqueues launches (and can be captured).
-int prepare_batch_pairs(BatchPairFn fn, int nbins, long long ntasks, long long* blocks)
+int prepare_batch_pairs(BatchPairFn fn, int nbins, int warps, long long ntasks, long long* blocks)
 {
     const size_t smem = pair_smem_bytes(nbins);
     if (cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -125,7 +125,6 @@ int prepare_batch_pairs(BatchPairFn fn, int nbins, long long ntasks, long long* 
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int warps = pair_block_warps((nbins + 1) / 2, false);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, warps * 32, smem);
     if (per_sm < 1) per_sm = 1;
     *blocks = std::max<long long>(1, std::min<long long>((long long)sms * per_sm, (ntasks + warps - 1) / warps));
@@ -168,6 +167,7 @@ struct sss_batch {
         unsigned int* counter;  // device
         BatchPairFn fn;
         long long blocks;
+        int warps;              // warps per block (the class's first problem's pair_warps)
     };
     struct Wave {
         const LegItem* legs;    // device
@@ -180,6 +180,7 @@ struct sss_batch {
     std::vector<float*> outs;
     std::vector<long long> npoints;
     std::vector<Wave> waves;
+    int leg_threads = 128;      // leg-kernel block (the first problem's leg_threads)
     unsigned int* counters = nullptr;
     int ncounters = 0;
     int32_t* status = nullptr;
@@ -309,6 +310,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
     std::vector<Item> items;
     std::unique_ptr<sss_batch> B(new sss_batch());
     B->problems.assign(problems, problems + n);
+    if (problems[0].leg_threads) B->leg_threads = problems[0].leg_threads;
     B->outs.assign(outs, outs + n);
     B->status = status;
     for (int i = 0; i < n; ++i) {
@@ -410,6 +412,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
             Lc.ntasks = 0;
             Lc.counter = dctr + nctr++;
             Lc.fn = pick_batch_pairs(p0.nbins);
+            Lc.warps = p0.pair_warps ? p0.pair_warps : pair_block_warps((p0.nbins + 1) / 2, false);
             if (!Lc.fn) return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan: nbins out of range");
             for (size_t j : kv.second) {
                 const Item& it = items[j];
@@ -440,7 +443,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
                 P.task_begin = Lc.ntasks;
                 Lc.ntasks += (long long)C.nl * P.nchunks;
             }
-            int rc = prepare_batch_pairs(Lc.fn, Lc.nbins, Lc.ntasks, &Lc.blocks);
+            int rc = prepare_batch_pairs(Lc.fn, Lc.nbins, Lc.warps, Lc.ntasks, &Lc.blocks);
             if (rc) return rc;
             W.launches.push_back(Lc);
         }
@@ -486,11 +489,12 @@ extern "C" int sss_batch_run_waves(const sss_batch* B, int32_t first, int32_t co
             cudaMemsetAsync(B->counters + W.ctr_first, 0, sizeof(unsigned int) * W.launches.size(), st) !=
                 cudaSuccess)
             return sss_set_error(SSS_ERR_CUDA, "sss_batch_run: memset failed");
-        batch_leg_kernel<<<(unsigned)((W.threads + 127) / 128), 128, 0, st>>>(W.legs, W.nlegs, W.threads);
+        const int lt = B->leg_threads;
+        batch_leg_kernel<<<(unsigned)((W.threads + lt - 1) / lt), lt, 0, st>>>(W.legs, W.nlegs, W.threads);
         int rc = sss_check_launch("batch_leg_kernel");
         if (rc) return rc;
         for (const auto& L : W.launches) {
-            L.fn<<<(unsigned)L.blocks, pair_block_warps((L.nbins + 1) / 2, false) * 32, pair_smem_bytes(L.nbins),
+            L.fn<<<(unsigned)L.blocks, L.warps * 32, pair_smem_bytes(L.nbins),
                    st>>>(
                 L.items, L.nitems, L.ntasks, L.T, L.tof, L.counter, B->status);
             rc = sss_check_launch("batch_pair_kernel");

@@ -9,6 +9,9 @@
 
 namespace sss {
 
+constexpr int kLegThreadsDefault = 128;  // leg-kernel block (sss_tof_problem.leg_threads = 0)
+constexpr int kLegThreadsMax = 256;      // the leg kernels are compiled for blocks up to this size
+
 struct LegParams {
     Grid g;
     const float* act;

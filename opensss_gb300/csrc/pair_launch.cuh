@@ -24,6 +24,7 @@ struct PairParams {
     unsigned int* counter;
     unsigned long long* work;  // [0] voxel lists walked per pair, [1] pairs evaluated
     int32_t* status;
+    int warps;                 // warps per block, 0 = pair_block_warps (the compiled bound)
 };
 
 template <int NP, bool SINGLE, bool ODD, bool KAHAN, int MINB>
@@ -61,7 +62,8 @@ template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 int launch_pairs(const PairParams& P, cudaStream_t st)
 {
     constexpr int MINB = KAHAN ? 1 : 2;
-    constexpr int kWarps = pair_block_warps(NP, KAHAN);
+    constexpr int kBound = pair_block_warps(NP, KAHAN);
+    const int kWarps = P.warps > 0 && P.warps < kBound ? P.warps : kBound;
     auto kern = pair_kernel<NP, SINGLE, ODD, KAHAN, MINB>;
     const size_t smem = pair_smem_bytes(P.ctx.nbins, KAHAN ? NP : 0);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(1024) scatter_points_kernel(
 
 // ---------------------------------------------------------------- 2. legs
 
-__global__ void __launch_bounds__(128) leg_kernel(LegParams P)
+__global__ void __launch_bounds__(kLegThreadsMax) leg_kernel(LegParams P)
 {
     long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)P.npts * P.nl) return;
@@ -209,6 +209,12 @@ int validate(const sss_tof_problem* p)
         return sss_set_error(SSS_ERR_INVALID, "image_size must satisfy max > min");
     long long nl = (long long)p->nru * p->ndu;
     if (nl * nl * p->nbins > (1ll << 40)) return sss_set_error(SSS_ERR_INVALID, "output too large");
+    const int wmax = sss_pair_warps_max(p->nbins, p->flags);
+    if (p->pair_warps < 0 || p->pair_warps > wmax)
+        return sss_set_error(SSS_ERR_INVALID, "pair_warps %d outside 0..%d", p->pair_warps, wmax);
+    if (p->leg_threads < 0 || p->leg_threads > kLegThreadsMax || p->leg_threads % 32)
+        return sss_set_error(SSS_ERR_INVALID, "leg_threads %d: 0 or a multiple of 32 up to %d", p->leg_threads,
+                             kLegThreadsMax);
     return SSS_OK;
 }
 
@@ -218,6 +224,12 @@ int validate(const sss_tof_problem* p)
 int sss::dispatch_pairs_plain(const PairParams& P, cudaStream_t st) { return dispatch_pairs<false>(P, st); }
 
 int sss_internal_validate(const sss_tof_problem* p) { return validate(p); }
+
+extern "C" int sss_pair_warps_max(int32_t nbins, int32_t flags)
+{
+    if (nbins < 1 || nbins > 64) return 0;
+    return sss::pair_block_warps((nbins + 1) / 2, (flags & SSS_FLAG_KAHAN) != 0);
+}
 
 int sss_internal_scatter_points(const sss_tof_problem* p, double* points, long long capacity,
                                 unsigned long long* counts, cudaStream_t st)
@@ -353,6 +365,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     PP.work = (unsigned long long*)(ws + w.counter + 8);
     cudaMemsetAsync(ws + w.counter, 0, 256, st);
     PP.status = status;
+    PP.warps = p->pair_warps;
 
     g_timer.clear();
     g_timer.work = PP.work;
@@ -379,7 +392,8 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
             LP.npts = (int)npts;
             long long threads = npts * nl;
             if (g_timer.on) cudaEventRecord(g_timer.get(), st);
-            leg_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(LP);
+            const int lt = p->leg_threads ? p->leg_threads : kLegThreadsDefault;
+            leg_kernel<<<(unsigned)((threads + lt - 1) / lt), lt, 0, st>>>(LP);
             if ((rc = sss_check_launch("leg_kernel"))) return rc;
             if (g_timer.on) cudaEventRecord(g_timer.get(), st);
             PP.ctx.points = LP.points;

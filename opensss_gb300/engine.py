@@ -81,6 +81,10 @@ class TofSSS:
         self.ratio = as_device(tables.attenuation_ratio(att), torch.float32, dev)
         self._ws = None
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        # launch shape of the kernels (0 = the library's default); set by
+        # opensss_gb300.autotune.tune or by hand
+        self.pair_warps = 0
+        self.leg_threads = 0
 
     # ------------------------------------------------------------------
     def problem(self, act_flat, mu_flat, shape, image_size, kahan: bool = False,
@@ -110,6 +114,8 @@ class TofSSS:
         p.tof_log2w = self.tof_log2w.data_ptr()
         p.efficiency = self.eff.data_ptr()
         p.atten_ratio = self.ratio.data_ptr()
+        p.pair_warps = int(self.pair_warps)
+        p.leg_threads = int(self.leg_threads)
         return p
 
     def scatter_points(self, p, stream=None):
