@@ -310,9 +310,9 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
         lane_ok = rp != rw;
         w_first = false;
     }
-    const int ri1 = w_first ? rw : rp, di1 = w_first ? dw : dp;
-    const int ri2 = w_first ? rp : rw, di2 = w_first ? dp : dw;
     const int l1 = w_first ? lw : lp, l2 = w_first ? lp : lw;
+    // sv1 - sv2 = -sigma (sv_w - sv_p); the walked leg's samples enter the TOF
+    // offset with sign sigma (:520 for leg 1, :526 for leg 2)
     const float sigma = w_first ? -1.f : 1.f;
 
     float2 acc[NP];
@@ -333,20 +333,22 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
         const long long lo = (long long)s * C.nl;
         const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw];
         const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp];
-        const float4 A1 = w_first ? Aw : Ap, A2 = w_first ? Ap : Aw;
-        const float4 B1 = w_first ? Bw : Bp, B2 = w_first ? Bp : Bw;
-        bool ok = lane_ok && A1.z != INFINITY && A2.z != INFINITY && !(A1.y == 0.f && A2.y == 0.f);
+        // everything below but the TOF offset's sign is symmetric in the two legs
+        bool ok = lane_ok && Aw.z != INFINITY && Ap.z != INFINITY && !(Aw.y == 0.f && Ap.y == 0.f);
         float c = 0.f;
         if (ok) {
             // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
-            float qc = fmaf(B1.x, B2.x, fmaf(B1.y, B2.y, B1.z * B2.z));
+            float qc = fmaf(Bw.x, Bp.x, fmaf(Bw.y, Bp.y, Bw.z * Bp.z));
             qc = fminf(1.f, fmaxf(-1.f, qc));
-            const float e = 511.0f / (2.0f + qc);
+            // scattered energy: the FP32 estimate is within 3e-4 keV of the FP64
+            // value (unit vectors rounded to FP32, a 2-ulp division), so the FP64
+            // row decides only within 1e-3 keV of a rounding boundary
+            const float e = __fdividef(511.0f, 2.0f + qc);
             const float eh = e + 0.5f;
             const float fr = eh - floorf(eh);
             int row;
             if (fr < 1e-3f || fr > 1.0f - 1e-3f)
-                row = energy_row_fp64(C, s, ri1, di1, ri2, di2);
+                row = energy_row_fp64(C, s, rw, dw, rp, dp);
             else
                 row = 2 * (int)floorf(eh) - 1;
             if (row < 0 || row >= 2000) {
@@ -355,22 +357,23 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                 const float effp = __ldg(C.eff + row);
                 if (effp != 0.f) {  // :508-509 skips before the count is added
                     const float rr = __ldg(C.ratio + row);
-                    // Klein-Nishina with cos(theta) = -qc (:239-258)
-                    const float ratio = 1.0f / (1.0f + C.gamma_kn * (1.0f + qc));
-                    const float sin2 = 1.0f - qc * qc;
-                    const float kn = ratio * ratio * (ratio + 1.0f / ratio - sin2);
+                    // Klein-Nishina with cos(theta) = -qc (:239-258): Ratio = 1/den
+                    const float den = fmaf(C.gamma_kn, 1.0f + qc, 1.0f);
+                    const float ratio = __frcp_rn(den);
+                    const float sin2 = fmaf(-qc, qc, 1.0f);
+                    const float kn = ratio * ratio * (ratio + den - sin2);
                     // geometry (:533-536): (ds)^2 |cos a1||cos a2| / (4 pi sv1^2 sv2^2)
-                    const float f = C.geo_c * A1.w * A2.w * effp * kn;
+                    const float f = C.geo_c * (Aw.w * Ap.w) * (effp * kn);
                     // this task's part: M1 * M2^r * AB1 or M2 * M1^r * AB2 (:540)
                     const float mw = ex2(-Aw.z), mpr = ex2(-rr * Ap.z);
                     if (Aw.y != 0.f) c = f * mw * mpr;
-                    cnt += (A1.y != 0.f && A2.y != 0.f) ? 2.f : 1.f;  // :485-488
+                    cnt += (Aw.y != 0.f && Ap.y != 0.f) ? 2.f : 1.f;  // :485-488
                     npairs += 1;
                 }
             }
         }
         // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
-        const float u = fmaf(A1.x - A2.x, inv_c, 4000.5f);
+        const float u = fmaf(-sigma * (Aw.x - Ap.x), inv_c, 4000.5f);
         if (SINGLE && C.unit_tof) {
             // weights of exactly 1: sum(a_v * 1) is the walking leg's activity integral
             acc[0].x = fmaf(c, Aw.y, acc[0].x);
