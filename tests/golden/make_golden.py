@@ -192,8 +192,18 @@ def gen_sss(R, which):
                      ("sss_tiny_b3", W.tiny_problem(3, seed=4)),
                      ("sss_tiny_b5", W.tiny_problem(5, seed=5, shape=(14, 14, 8), nd=64, nr=8,
                                                     nru=4, ndu=10, voxel_cm=1.7))]
-    if "c1" in which:
+    if "nontof_40x40x20" in which:
         problems.append(("sss_nontof_40x40x20", W.nontof_40x40x20(seed=0)))
+    if "nxgt" in which:
+        # Nx > Ny: the reference's sub2ind strides x by Ny, so it reads shifted
+        # voxels without leaving the volume, and its scatter-point grid spaces y
+        # with the x extent (:377-394)
+        # (the ring is turned by half a crystal so that no leg runs exactly
+        # through voxel corners, where the reference's traversal overruns)
+        problems.append(("sss_tiny_nx14_ny10",
+                         W.make_problem("tiny-nx14-ny10", (14, 10, 6), 2.0, 3, 8, 3, 3.0, 214.0, seed=6,
+                                        scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0,
+                                                               phase=0.5), radius_cm=8.0)))
     for name, pr in problems:
         nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
         LC, SI, _ = _sino(R, nd, nr)
@@ -499,7 +509,8 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "upsample", "upsample_lut", "mask", "fit", "span", "listmode", "prep"]
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "upsample", "upsample_lut", "mask", "fit", "span",
+       "listmode", "prep"]
 
 
 # ---------------------------------------------------------------- image preparation

@@ -58,7 +58,8 @@ def _valid_mask(nru, ndu):
     return ((d1 < d2) | ((d1 == d2) & (ri1 != ri2))).reshape(nru * nru, ndu, ndu)
 
 
-@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_nontof_40x40x20"])
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_nontof_40x40x20",
+                                  "sss_tiny_nx14_ny10"])
 def test_sss_matches_reference(cuda_ok, att_table, name):
     g = golden(name)
     pr = problem_from_golden(g)
