@@ -148,3 +148,19 @@ def test_unsupported_options_raise_before_device_work():
         Utils.CropAndDownscale(img, (1, 1, 1), (4, 4, 4), (2, 2, 2), mode="constant")
     with pytest.raises(NotImplementedError):
         Utils.CropAndDownscale(img, (1, 1, 1), (4, 4, 4), (2, 2, 2), order=1)
+
+
+def test_crop_window_matches_oracle_on_random_windows():
+    """The host window rule against the oracle's literal numpy slicing/padding
+    for windows that crop, pad, overhang one end or start at a negative index."""
+    rng = np.random.default_rng(21)
+    for _ in range(200):
+        shape = tuple(int(v) for v in rng.integers(1, 23, size=3))
+        vox = rng.uniform(0.5, 4.0, size=3).round(2)
+        crop = rng.uniform(0.0, 2.5, size=3) * np.array(shape) * vox
+        img = rng.random(shape).astype(np.float32)
+        win = Utils.crop_window(shape, vox, crop)
+        ref = P.crop(img, vox, crop)
+        assert tuple(w[2] for w in win) == ref.shape
+        if ref.size:
+            assert np.array_equal(_apply_window(img, win), ref)
