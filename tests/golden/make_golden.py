@@ -204,6 +204,22 @@ def gen_sss(R, which):
                          W.make_problem("tiny-nx14-ny10", (14, 10, 6), 2.0, 3, 8, 3, 3.0, 214.0, seed=6,
                                         scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0,
                                                                phase=0.5), radius_cm=8.0)))
+    if "tofrange" in which:
+        # a 2 m wide body in a scanner of 1.5 m radius: TOF offsets of pairs
+        # pass the 8001-entry table (+-4000 ps, 120 cm), where the reference
+        # indexes past the table and raises IndexError (:521, :527)
+        pr = W.make_problem("tiny-tofrange", (80, 80, 6), 2.5, 3, 8, 3, 3.0, 214.0, seed=7,
+                            scanner=W.ring_scanner(48, 6, radius_cm=150.0, ring_pitch_cm=1.0, phase=0.5),
+                            radius_cm=99.0)
+        nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
+        LC, _, _ = _sino(R, nd, nr)
+        try:
+            _run_sss(R, pr, LC)
+            err = ""
+        except IndexError as e:
+            err = f"IndexError: {e}"
+        print(f"sss_tofrange: reference {err or 'ran'}")
+        _save("sss_tofrange", **_problem_arrays(pr), reference_error=np.array(err))
     for name, pr in problems:
         nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
         LC, SI, _ = _sino(R, nd, nr)
@@ -509,8 +525,8 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "upsample", "upsample_lut", "mask", "fit", "span",
-       "listmode", "prep"]
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "upsample", "upsample_lut",
+       "mask", "fit", "span", "listmode", "prep"]
 
 
 # ---------------------------------------------------------------- image preparation

@@ -223,3 +223,16 @@ def test_widest_bin_counts_launch_and_match_oracle(cuda_ok, att_table, bins):
     for name, got in runs.items():
         assert_same_support(got, ref)
         assert rel_l2(got, ref) < TOL, name
+
+
+def test_tof_offsets_past_the_table_are_an_error(cuda_ok, att_table):
+    """A 2 m wide body in a 1.5 m ring: the reference raises IndexError on its
+    TOF table (recorded in the fixture); the engine reports SSS_ERR_TOF_RANGE."""
+    from opensss_gb300._lib import SSSError
+
+    g = golden("sss_tofrange")
+    assert str(g["reference_error"]).startswith("IndexError")
+    pr = problem_from_golden(g)
+    with pytest.raises(SSSError) as e:
+        _gpu_compact(pr, att_table)
+    assert e.value.code == 4

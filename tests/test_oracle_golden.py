@@ -112,3 +112,19 @@ def test_oracle_upsample_matches_reference(case):
         bins.append(O.upsample_bin(cmp[b], nru, ndu, nr, nd, lut, rmap, si))
     assert np.array_equal(np.stack(bins), g[f"case{case}_bins"])
     assert np.allclose(np.sum(bins, axis=0), g[f"case{case}_sum"], rtol=1e-6, atol=0)
+
+
+def test_oracle_rejects_tof_offsets_past_the_table_as_the_reference_does(att_table):
+    """A 2 m wide body in a 1.5 m ring: the reference indexes its 8001-entry
+    TOF table past the end and raises IndexError (recorded in the fixture);
+    the oracle reports status -2 for the same problem (the engine:
+    SSS_ERR_TOF_RANGE)."""
+    g = golden("sss_tofrange")
+    assert str(g["reference_error"]).startswith("IndexError")
+    pr = problem_from_golden(g)
+    with pytest.raises(RuntimeError, match="status -2"):
+        O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                      pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                      pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                      pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                      pr.nr_bins)
