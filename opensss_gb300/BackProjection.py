@@ -29,6 +29,7 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
     With ``span``, ``Geometry`` is the expanded geometry, ``SinogramOrder`` the
     mashed SinogramIndex (float [n, 2]) and the back-projection is
     length-weighted (BackProjection.py:217-393)."""
+    _lib.require_cuda(prompts=prompts, randoms=randoms, mask=mask, scatters=scatters)
     geom = np.asarray(Geometry, dtype=np.float64)
     nr, nd = geom.shape[:2]
     grid = np.ascontiguousarray(np.asarray(GridSize).reshape(-1)[:3], dtype=np.int32)
@@ -79,6 +80,7 @@ def fit_bins_device(prompts, randoms, mask, scatters, scat_stride: int, scat_cel
     prompts: CUDA float32 [bins, cell, slice]; scatters: CUDA float32 with
     bin b's values from ``b * scat_stride`` (through the gather tables);
     randoms / mask as in ``fit_device``.  Returns float32 [bins]."""
+    _lib.require_cuda(prompts=prompts, randoms=randoms, mask=mask, scatters=scatters)
     geom = np.asarray(Geometry, dtype=np.float64)
     nr, nd = geom.shape[:2]
     nbins = int(prompts.shape[0])

@@ -63,6 +63,7 @@ def histogram_device(events: torch.Tensor, header: dict, LORCoordinates, Sinogra
                      TOF_range: float, mash: int = 1, Shift: int = 0, device="cuda"):
     """(prompts uint16, randoms float32 or None, norm float32 or None) as
     device tensors of the reference's shapes."""
+    _lib.require_cuda(events=events)
     lor = np.asarray(LORCoordinates)
     table = np.asarray(SinogramIndex)
     nrad = int(lor[:, :, 1].max()) + 1
@@ -114,6 +115,7 @@ def inject_device(events: torch.Tensor, header: dict, LORCoordinates, slice_tabl
                   device="cuda"):
     """(out records uint8 device tensor, kept events): the injection on
     device-resident events and scatter sinograms [bins, rad, ang, slice]."""
+    _lib.require_cuda(events=events, scatters=scatters)
     lor = np.asarray(LORCoordinates)
     nrad = int(lor[:, :, 1].max()) + 1
     nang = int(lor[:, :, 0].max()) + 1

@@ -28,6 +28,7 @@ def upsample_device(sampled: torch.Tensor, tables, nbins: int, ncell: int, nslic
                     bin_index: int | None = None, out: torch.Tensor | None = None) -> torch.Tensor:
     """Gather on the device.  ``tables``: geometry.upsample_tables(...).
     bin_index None sums all bins (in bin order)."""
+    _lib.require_cuda(sampled=sampled, out=out)
     if not isinstance(tables, geometry.UpsampleTables):
         tables = geometry.UpsampleTables(*(t.cpu().numpy() if isinstance(t, torch.Tensor) else t
                                            for t in tables[:2]), int(tables[2]))

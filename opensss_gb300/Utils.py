@@ -57,6 +57,8 @@ def crop_downscale_device(image: torch.Tensor, window, out_dims, anti_aliasing: 
                           clip: bool = True, zero_below: float = -np.inf) -> torch.Tensor:
     """The GPU call: image float32 [n0][n1][n2] on the device, window from
     ``crop_window``; returns float32 ``out_dims`` on the same device."""
+    if not image.is_cuda:
+        raise ValueError("crop_downscale_device needs a CUDA tensor")
     dev = image.device
     img = image.to(torch.float32).contiguous()
     dims = np.array(img.shape, dtype=np.int32)
@@ -92,6 +94,8 @@ def CropAndDownscale(image, voxel_size, crop_size, downscaled_dimensions, clip: 
     if mode != "edge" or order != 3 or not preserve_range:
         raise NotImplementedError("only resize(order=3, mode='edge', preserve_range=True) is built on the GPU")
     as_numpy = not isinstance(image, torch.Tensor)
+    if not as_numpy and not image.is_cuda:
+        raise ValueError("CropAndDownscale takes a numpy array or a CUDA tensor")
     t = torch.from_numpy(np.ascontiguousarray(image, dtype=np.float32)).cuda() if as_numpy else image
     if t.dim() != 3:
         raise ValueError("CropAndDownscale expects a 3-D volume")

@@ -151,6 +151,15 @@ def lib():
     return _lib
 
 
+def require_cuda(**tensors) -> None:
+    """Raise ValueError unless every given tensor (None skipped) lives on a
+    CUDA device: the kernels take raw device pointers, and a host pointer would
+    reach the GPU unchecked."""
+    for name, t in tensors.items():
+        if t is not None and not (hasattr(t, "is_cuda") and t.is_cuda):
+            raise ValueError(f"{name} must be a CUDA tensor")
+
+
 def last_error() -> str:
     return lib().sss_last_error().decode(errors="replace")
 

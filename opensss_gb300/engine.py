@@ -22,7 +22,10 @@ WS_BUDGET_BYTES = 24 << 30  # default cap on the leg-list workspace per run
 def _require_cuda(device):
     if not torch.cuda.is_available():
         raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
-    return torch.device(device)
+    dev = torch.device(device)
+    if dev.type != "cuda":
+        raise ValueError(f"device {dev} is not a CUDA device: the engine has no CPU path")
+    return dev
 
 
 def as_device(a, dtype, device):

@@ -120,3 +120,23 @@ def test_crop_downscale_rejects_bad_arguments_without_device_work(lib):
     rc = lib.sss_crop_downscale(C.c_void_p(8), p(dims), p(zero), p(zero), p(dims), p(dims), p(sigma), 1,
                                 C.c_float(0), C.c_void_p(8), C.c_void_p(8), 16, None)
     assert rc == 7  # workspace too small
+
+
+def test_device_wrappers_reject_host_tensors():
+    import torch
+
+    from opensss_gb300.BackProjection import fit_bins_device, fit_device
+    from opensss_gb300.Datafile import histogram_device
+    from opensss_gb300.Interpolation import upsample_device
+
+    host = torch.zeros(4)
+    with pytest.raises(ValueError):
+        upsample_device(host, (np.zeros(1, np.int64), np.zeros(1, np.int64), 1), 1, 1, 1)
+    with pytest.raises(ValueError):
+        fit_device(host, host, host, host, None, None, [1, 1, 1], [0, 0, 0, 1, 1, 1], np.zeros((1, 2, 3)),
+                   None, None, 1)
+    with pytest.raises(ValueError):
+        fit_bins_device(host, host, host, host, 1, None, None, [1, 1, 1], [0, 0, 0, 1, 1, 1],
+                        np.zeros((1, 2, 3)), None, None, 1)
+    with pytest.raises(ValueError):
+        histogram_device(host, {}, np.zeros((2, 2, 2)), np.zeros((1, 1)), 1, 1000.0)

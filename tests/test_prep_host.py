@@ -164,3 +164,13 @@ def test_crop_window_matches_oracle_on_random_windows():
         assert tuple(w[2] for w in win) == ref.shape
         if ref.size:
             assert np.array_equal(_apply_window(img, win), ref)
+
+
+def test_host_tensors_are_rejected_before_device_work():
+    import torch
+
+    with pytest.raises(ValueError):
+        Utils.CropAndDownscale(torch.zeros((4, 4, 4)), (1, 1, 1), (4, 4, 4), (2, 2, 2))
+    with pytest.raises(ValueError):
+        Utils.crop_downscale_device(torch.zeros((4, 4, 4)), Utils.crop_window((4, 4, 4), (1, 1, 1), (4, 4, 4)),
+                                    (2, 2, 2))
