@@ -206,10 +206,16 @@ def scatter_points(act, mu, image_size, step):
 
 def sss_compact(act, mu, image_size, geometry, normals, det_size, att_table, energy_resolution,
                 energy_threshold, nru, ndu, step, tof_resolution, tof_range, nbins,
-                sp_begin=0, sp_end=-1, nthreads=0):
-    """FP64 SSS; returns compact [B, NRU*NRU, NDU, NDU] (pairs di1<=di2 filled)."""
+                sp_begin=0, sp_end=-1, nthreads=0, tof=None):
+    """FP64 SSS; returns compact [B, NRU*NRU, NDU, NDU] (pairs di1<=di2 filled).
+    ``tof`` replaces the TOF table ([B, 8001], e.g. an emulation of another
+    evaluation of the weights)."""
     tables = problem_tables(att_table, energy_threshold, energy_resolution, nbins, tof_range,
                             tof_resolution)
+    if tof is not None:
+        if np.shape(tof) != (nbins, TOF_ENTRIES):
+            raise ValueError(f"tof table must be [{nbins}, {TOF_ENTRIES}], got {np.shape(tof)}")
+        tables["tof"] = np.ascontiguousarray(tof, dtype=np.float64)
     s, keep = _sss_struct(act, mu, image_size, geometry, normals, det_size, nru, ndu, step,
                           tables, sp_begin, sp_end)
     out = np.zeros((nbins, nru * nru, ndu, ndu))

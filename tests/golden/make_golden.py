@@ -204,6 +204,20 @@ def gen_sss(R, which):
                          W.make_problem("tiny-nx14-ny10", (14, 10, 6), 2.0, 3, 8, 3, 3.0, 214.0, seed=6,
                                         scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0,
                                                                phase=0.5), radius_cm=8.0)))
+    if "bins" in which:
+        # bins wider than 1.33 x the timing FWHM: the pair kernel evaluates
+        # every bin's weight with its own 2^x instead of the factored product
+        problems.append(("sss_tiny_wide",
+                         W.make_problem("tiny-wide", (12, 12, 6), 2.0, 3, 8, 3, 5.0, 214.0, seed=10,
+                                        scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0),
+                                        radius_cm=8.0)))
+        # a 60 ps timing kernel with 5 bins of 1 cm: TOF offsets run up to
+        # ~575 ps, far past the last bin centre (133 ps), where the normalised
+        # column's weight sits almost entirely on the last bin
+        problems.append(("sss_tiny_far",
+                         W.make_problem("tiny-far", (12, 12, 6), 2.0, 3, 8, 5, 1.0, 60.0, seed=8,
+                                        scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0,
+                                                               phase=0.5), radius_cm=8.0)))
     if "tofrange" in which:
         # a 2 m wide body in a scanner of 1.5 m radius: TOF offsets of pairs
         # pass the 8001-entry table (+-4000 ps, 120 cm), where the reference
@@ -525,7 +539,7 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "upsample", "upsample_lut",
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "upsample", "upsample_lut",
        "mask", "fit", "span", "listmode", "prep"]
 
 

@@ -145,11 +145,13 @@ def _pack_bin(a, n, mask):
     return np.int32(p).view(np.float32)
 
 
-def _factored_weights(nb, rng, res):
-    """The pair kernel's weights for ca = 1, operation for operation in float32:
-    the table set-up of load_pair_tables (A with the bin in its low bits, r,
-    G rows) and the FFMA2 / FMUL2 chain of accumulate_loaded."""
+def _factored_weights(nb, rng, res, ca=1.0):
+    """The pair kernel's terms ca * w_b, operation for operation in float32,
+    divided by ca: the table set-up of load_pair_tables (A with the bin in its
+    low bits, r, G rows) and the FFMA2 / FMUL2 chain of accumulate_loaded,
+    which starts from ca * A."""
     f32 = np.float32
+    ca = f32(ca)
     w = 2 * rng / nb
     kappa = 4.0 / (res * res)
     s0, W, k2w, gam = f32((1.0 - (nb + 1) / 2.0) * w), f32(w), f32(2 * kappa * w), f32(kappa * w * w)
@@ -173,32 +175,37 @@ def _factored_weights(nb, rng, res):
             A = _pack_bin(a, n, mask)
             row = int(A.view(np.int32)) & mask
             r = np.exp2(beta)
-            px, py, r2 = f32(A), f32(f32(A) * r), f32(r * r)
+            px = f32(ca * A)
+            py, r2 = f32(px * r), f32(r * r)
             for kk in range((nb + 1) // 2):
                 out[2 * kk, i] = f32(px * G[row, 2 * kk])
                 if 2 * kk + 1 < nb:
                     out[2 * kk + 1, i] = f32(py * G[row, 2 * kk + 1])
                 px, py = f32(px * r2), f32(py * r2)
-    return out
+    return out / np.float64(ca)
 
 
-def _valid_limit(nb, rng, res):
-    """Largest offset (ps) up to which A = 2^(Y - n beta) stays a normal float
-    on the high side (n = B-1): (B-1) beta <= 126."""
+def _valid_limit(nb, rng, res, ca=1.0):
+    """Largest offset (ps) up to which the chain's first term ca * A, A =
+    2^(Y - n beta), stays a normal float on the high side (n = B-1, Y ~ 0):
+    (B-1) beta <= 126 + log2(ca)."""
     w = 2 * rng / nb
-    return (nb - 1) / 2.0 * w + 126.0 / ((nb - 1) * 2 * (4.0 / res ** 2) * w)
+    return (nb - 1) / 2.0 * w + (126.0 + np.log2(ca)) / ((nb - 1) * 2 * (4.0 / res ** 2) * w)
 
 
 _C = 0.0299792458
 _FACTORED = [(13, 13 * 3.9 / _C, 214.0), (33, 33 * 1.5 / _C, 214.0), (64, 64 * 1.5 / _C, 214.0)]
 
 
+# ca = (pair factor) x (activity x length) of one voxel term; 2^-27 is about the
+# largest in a 41 cm ring with 3.2 mm crystals (geometry factor ~8e-4 / d1^2 d2^2)
+@pytest.mark.parametrize("ca", [1.0, 2.0 ** -27])
 @pytest.mark.parametrize("nb,rng,res", _FACTORED)
-def test_factored_weights_match_table_within_their_range(nb, rng, res):
+def test_factored_weights_match_table_within_their_range(nb, rng, res, ca):
     ref = T.tof_table(nb, rng, res)
-    got = _factored_weights(nb, rng, res)
+    got = _factored_weights(nb, rng, res, ca)
     t = np.arange(-4000, 4001)
-    ok = t <= _valid_limit(nb, rng, res)
+    ok = t <= _valid_limit(nb, rng, res, ca)
     # rounding of the FP32 power chain (up to B-1 products) and of the packed A:
     # measured 1.9e-6 / 4.6e-6 / 6.5e-6 absolute and 3.8e-6 / 7.9e-6 / 1.4e-5
     # relative on weights above 1e-3 for 13 / 33 / 64 bins
@@ -214,3 +221,64 @@ def test_factored_weights_match_table_everywhere(nb, rng, res):
     ref = T.tof_table(nb, rng, res)
     got = _factored_weights(nb, rng, res)
     assert np.isfinite(got).all() and np.abs(got - ref).max() < 1e-5
+
+
+def _largest_tof_offset(pr):
+    """Largest positive TOF offset (ps) any (scatter point, pair, voxel) term
+    of a problem reaches, from the oracle tracer.  A pair (l1, l2) with l1 on
+    the smaller crystal (or the same crystal on another ring, both orders)
+    puts leg-1 voxels at (d1 - d2 - 2s)/c and leg-2 voxels at (d1 - d2 + 2s)/c,
+    s the voxel's distance from the point; only voxels with activity count."""
+    from oracle import oracle as O
+
+    xyz, _ = O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)
+    g = pr.scanner.geometry
+    rings = O.sampled_rings(g.shape[0], pr.nr_rings_used)
+    dets = O.sampled_detectors(g.shape[1], pr.nr_detectors_used)
+    crys = np.array([[g[r, d, 0], g[r, d, 1], g[r, 0, 2]] for d in dets for r in rings])
+    cid = np.repeat(np.arange(len(dets)), len(rings))
+    nl = len(crys)
+    lines = np.concatenate([np.repeat(xyz, nl, 0), np.tile(crys, (len(xyz), 1))], 1)
+    cnt, _, ix, sm = O.trace_batch(np.array(pr.activity.shape), np.asarray(pr.image_size).reshape(-1)[:6], lines,
+                                   allow_overrun=True)
+    act = np.asarray(pr.activity, np.float32).flatten("F")
+    hot = (np.arange(sm.shape[1])[None, :] < cnt[:, None]) & (act[np.maximum(ix - 1, 0)] > 0)
+    s_hi = np.where(hot, sm, -np.inf).max(1).reshape(len(xyz), nl)
+    s_lo = np.where(hot, sm, np.inf).min(1).reshape(len(xyz), nl)
+    d = np.linalg.norm(lines[:, 3:] - lines[:, :3], axis=1).reshape(len(xyz), nl)
+    first = (cid[:, None] < cid[None, :]) | ((cid[:, None] == cid[None, :]) & ~np.eye(nl, dtype=bool))
+    base = d[:, :, None] - d[:, None, :]                                   # [point, l1, l2]
+    walk1 = np.where(first[None] & np.isfinite(s_lo)[:, :, None], base - 2 * s_lo[:, :, None], -np.inf)
+    walk2 = np.where(first[None] & np.isfinite(s_hi)[:, None, :], base + 2 * s_hi[:, None, :], -np.inf)
+    return max(walk1.max(), walk2.max()) / _C
+
+
+def test_far_golden_reaches_past_the_factored_range(att_table):
+    """The far-offset fixture exercises the known issue: its offsets pass the
+    factored weights' range and the NaN region (beta >= 64) but stay inside
+    the reference's +-4000 ps table.  The FP64 oracle run with the kernel's
+    emulated factored weights instead of the exact table gives NaN cells,
+    and still differs with those terms dropped; with the exact table it
+    matches the reference."""
+    from conftest import golden, problem_from_golden, rel_l2
+    from oracle import oracle as O
+
+    g = golden("sss_tiny_far")
+    pr = problem_from_golden(g)
+    top = _largest_tof_offset(pr)
+    limit = _valid_limit(pr.nr_bins, pr.tof_range, pr.tof_resolution)
+    w = 2 * pr.tof_range / pr.nr_bins
+    nan_from = (pr.nr_bins - 1) / 2 * w + 64 / (2 * (4 / pr.tof_resolution ** 2) * w)
+    assert limit < nan_from < top < 4000, (limit, nan_from, top)
+
+    def run(tof=None):
+        return O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry, pr.scanner.normals,
+                             pr.scanner.detector_size_mm, att_table, pr.energy_resolution, pr.energy_threshold,
+                             pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step, pr.tof_resolution,
+                             pr.tof_range, pr.nr_bins, tof=tof)
+
+    assert rel_l2(run(), g["compact"]) < 1e-6
+    weights = _factored_weights(pr.nr_bins, pr.tof_range, pr.tof_resolution)
+    assert np.isnan(run(weights)).any()
+    # without the NaN terms, the zero weights past the range still show: 5e-2
+    assert rel_l2(run(np.nan_to_num(weights, nan=0.0)), g["compact"]) > 1e-2

@@ -42,7 +42,8 @@ def test_rays_fixture_has_edge_cases():
     assert (allc > 0).sum() > 1000
 
 
-@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_tiny_nx14_ny10"])
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_tiny_nx14_ny10",
+                                  "sss_tiny_wide", "sss_tiny_far"])
 def test_oracle_sss_matches_reference(name, att_table):
     g = golden(name)
     pr = problem_from_golden(g)
