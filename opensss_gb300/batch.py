@@ -139,7 +139,8 @@ class BatchSSS:
             raise RuntimeError("batch plan was freed")
         st = stream if stream is not None else torch.cuda.current_stream(self.device)
         if check:
-            self.status.zero_()
+            with torch.cuda.stream(st):  # ordered before the batch's launches
+                self.status.zero_()
         _lib.check(_lib.lib().sss_batch_run(self._plan, C.c_void_p(st.cuda_stream)))
         if check:
             st.synchronize()

@@ -147,10 +147,12 @@ class TofSSS:
         per-point terms with Kahan's compensated addition."""
         dev = self.device
         shape = tuple(int(s) for s in ActivityMap.shape)
-        act = fortran_flat(ActivityMap, dev)
-        mu = fortran_flat(AttenuationMap, dev)
-        return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, stream, check,
-                             kahan, unit_tof, slice_range)
+        st = stream if stream is not None else torch.cuda.current_stream(dev)
+        with torch.cuda.stream(st):  # the maps' copies are ordered before the launches on st
+            act = fortran_flat(ActivityMap, dev)
+            mu = fortran_flat(AttenuationMap, dev)
+            return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, st, check,
+                                 kahan, unit_tof, slice_range)
 
     def run_flat(self, act, mu, shape, ImageSize, max_points: int | None = None,
                  wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
@@ -160,8 +162,15 @@ class TofSSS:
         (float32, Nx*Ny*Nz).  ``slice_range`` = (a, b) keeps the sampled
         z-slices a..b-1 only (a shard: the slice terms add up, :201)."""
         dev = self.device
-        p = self.problem(act, mu, shape, ImageSize, kahan, unit_tof)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
+        with torch.cuda.stream(st):  # buffers and the status reset belong to the launch stream
+            return self._run_on(st, act, mu, shape, ImageSize, max_points, wave_points, out, check, kahan,
+                                unit_tof, slice_range)
+
+    def _run_on(self, st, act, mu, shape, ImageSize, max_points, wave_points, out, check, kahan, unit_tof,
+                slice_range) -> torch.Tensor:
+        dev = self.device
+        p = self.problem(act, mu, shape, ImageSize, kahan, unit_tof)
         pts, counts = self.scatter_points(p, st)
         if slice_range is not None:
             # whole sampled z-slices [a, b): the points of the other slices are dropped

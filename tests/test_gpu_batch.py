@@ -147,3 +147,22 @@ def test_batch_graph_replay_matches_run(cuda_ok, att_table):
     assert rel_l2(got2[1], 2.0 * ref[1]) < TOL  # SSS is linear in the activity
     assert rel_l2(got2[0], ref[0]) < TOL
     b.close()
+
+
+def test_batch_run_on_a_side_stream(cuda_ok, att_table):
+    """run(stream=s) with s not the current stream resets the status word on s
+    and gives the default-stream outputs."""
+    import torch
+
+    from opensss_gb300.batch import BatchSSS
+
+    probs = _uneven_problems()[:2]
+    engines = [_engine(pr, att_table) for pr in probs]
+    b = BatchSSS([(e, pr.activity, pr.attenuation, pr.image_size) for e, pr in zip(engines, probs)])
+    ref = [o.cpu().numpy() for o in b.run()]
+    side = torch.cuda.Stream(b.device)
+    side.wait_stream(torch.cuda.current_stream(b.device))
+    got = [o.cpu().numpy() for o in b.run(stream=side)]  # synchronises side
+    for a, r in zip(got, ref):
+        assert rel_l2(a, r) < TOL
+    b.close()
