@@ -279,9 +279,12 @@ extern "C" int sss_batch_plan_points(const sss_tof_problem* problems, int32_t n,
         if (!slice_counts[i] || (!points[i] && lat.capacity > 0))
             return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan_points: null points of problem %d", i);
         counts[i].resize((size_t)lat.lz);
+        const long long per_slice = lat.lz > 0 ? lat.capacity / lat.lz : 0;  // lattice points of one slice
         for (long long z = 0; z < lat.lz; ++z) {
-            if (slice_counts[i][z] < 0)
-                return sss_set_error(SSS_ERR_INVALID, "sss_batch_plan_points: negative count");
+            if (slice_counts[i][z] < 0 || slice_counts[i][z] > per_slice)
+                return sss_set_error(SSS_ERR_INVALID,
+                                     "sss_batch_plan_points: problem %d slice %lld has %lld points (0..%lld)", i, z,
+                                     (long long)slice_counts[i][z], per_slice);
             counts[i][(size_t)z] = (unsigned long long)slice_counts[i][z];
         }
         pts[i] = points[i];

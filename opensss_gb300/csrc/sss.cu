@@ -295,13 +295,15 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
 {
     int rc = validate(p);
     if (rc) return rc;
-    if (!out || (n_points > 0 && (!points || !slice_counts)))
+    if (!out || (n_points > 0 && (!points || !slice_counts)) || n_slices < 0 || (n_slices > 0 && !slice_counts))
         return sss_set_error(SSS_ERR_INVALID, "sss_tof_run: null argument");
     cudaStream_t st = (cudaStream_t)stream;
     const long long nl = (long long)p->nru * p->ndu;
     const long long cap = (long long)p->nx + p->ny + p->nz;
     long long maxslice = 0, tot = 0;
     for (int64_t i = 0; i < n_slices; ++i) {
+        if (slice_counts[i] < 0)
+            return sss_set_error(SSS_ERR_INVALID, "sss_tof_run: slice_counts[%lld] is negative", (long long)i);
         maxslice = std::max<long long>(maxslice, slice_counts[i]);
         tot += slice_counts[i];
     }

@@ -87,6 +87,45 @@ def test_problem_validation(lib):
     assert rc == 1
 
 
+def _fake_problem(nx=8, ny=8, nz=4):
+    """A problem that passes validation; its pointers are never dereferenced
+    by the argument checks under test."""
+    from opensss_gb300 import _lib
+
+    p = _lib.TofProblem()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    for f in ("activity", "attenuation", "geometry", "normals", "rings", "detectors", "tof_log2w", "efficiency",
+              "atten_ratio"):
+        setattr(p, f, 8)
+    p.image_size[:] = [-1, -1, -1, 1, 1, 1]
+    p.nr, p.nd, p.nru, p.ndu = 4, 16, 2, 4
+    p.sample_step[:] = [2, 2, 2]
+    p.nbins = 1
+    return p
+
+
+def test_slice_counts_are_checked_before_any_device_work(lib):
+    from opensss_gb300 import _lib
+
+    p = _fake_problem()
+    fake = C.c_void_p(8)
+    neg = np.array([5, -2], np.int64)
+    rc = lib.sss_tof_run(C.byref(p), fake, 3, neg.ctypes.data_as(C.c_void_p), 2, 8, None, 0, fake, fake, None)
+    assert rc == 1 and "negative" in _lib.last_error()
+    # no point and no count array, but slices announced
+    rc = lib.sss_tof_run(C.byref(p), None, 0, None, 2, 8, None, 0, fake, fake, None)
+    assert rc == 1
+    # a lattice slice of this problem holds 4 x 4 points
+    too_many = np.array([17, 0], np.int64)
+    pts = (C.c_void_p * 1)(8)
+    cts = (C.c_void_p * 1)(too_many.ctypes.data)
+    outs = (C.c_void_p * 1)(8)
+    plan = C.c_void_p(0)
+    rc = lib.sss_batch_plan_points(C.byref(p), 1, C.cast(outs, C.c_void_p), C.cast(pts, C.c_void_p),
+                                   C.cast(cts, C.c_void_p), fake, 1 << 20, fake, C.byref(plan), None)
+    assert rc == 1 and "slice 0 has 17 points" in _lib.last_error() and not plan.value
+
+
 def test_no_cpu_fallback_without_gpu():
     import torch
 
