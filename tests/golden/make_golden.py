@@ -218,6 +218,22 @@ def gen_sss(R, which):
                          W.make_problem("tiny-far", (12, 12, 6), 2.0, 3, 8, 5, 1.0, 60.0, seed=8,
                                         scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0,
                                                                phase=0.5), radius_cm=8.0)))
+    if "edge" in which:
+        # degenerate inputs: no scatter point (empty attenuation map, or a
+        # sampling step past the volume), no activity, one sampled ring, and
+        # one sampled crystal per ring (only same-crystal pairs, all backscatter,
+        # whose FP64 energy efficiency is exactly 0)
+        pr = W.tiny_problem(3, seed=11)
+        pr.attenuation = np.zeros_like(pr.attenuation)
+        problems.append(("sss_edge_empty_mu", pr))
+        pr = W.tiny_problem(3, seed=12)
+        pr.activity = np.zeros_like(pr.activity)
+        problems.append(("sss_edge_empty_act", pr))
+        problems.append(("sss_edge_one_ring", W.tiny_problem(3, seed=13, nru=1, ndu=8)))
+        problems.append(("sss_edge_one_crystal", W.tiny_problem(3, seed=14, nru=3, ndu=1)))
+        pr = W.tiny_problem(3, seed=15)
+        pr.sample_step = np.array([13, 13, 7])
+        problems.append(("sss_edge_step_past_volume", pr))
     if "tofrange" in which:
         # a 2 m wide body in a scanner of 1.5 m radius: TOF offsets of pairs
         # pass the 8001-entry table (+-4000 ps, 120 cm), where the reference
@@ -539,7 +555,7 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "upsample", "upsample_lut",
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_edge", "upsample", "upsample_lut",
        "mask", "fit", "span", "listmode", "prep"]
 
 

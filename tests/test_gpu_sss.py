@@ -73,6 +73,26 @@ def test_sss_matches_reference(cuda_ok, att_table, name):
     assert not got[:, ~_valid_mask(pr.nr_rings_used, pr.nr_detectors_used)].any()
 
 
+@pytest.mark.parametrize("name", ["sss_edge_empty_mu", "sss_edge_empty_act", "sss_edge_one_ring",
+                                  "sss_edge_one_crystal", "sss_edge_step_past_volume"])
+def test_degenerate_inputs_match_reference(cuda_ok, att_table, name):
+    """No scatter point (empty attenuation map, sampling step past the
+    volume), no activity, one sampled ring, one sampled crystal per ring
+    (backscatter pairs only, efficiency 0): the reference's sinogram, which
+    is all zero in every case but the single ring."""
+    g = golden(name)
+    pr = problem_from_golden(g)
+    got = _gpu_compact(pr, att_table)
+    ref = g["compact"]
+    assert got.shape == ref.shape
+    assert np.isfinite(got).all()
+    if not ref.any():
+        assert not got.any()
+    else:
+        assert_same_support(got, ref)
+        assert rel_l2(got, ref) < TOL
+
+
 def test_scatter_points_match_oracle(cuda_ok, att_table):
     from opensss_gb300 import workloads as W
 

@@ -42,8 +42,12 @@ def test_rays_fixture_has_edge_cases():
     assert (allc > 0).sum() > 1000
 
 
+EDGE = ["sss_edge_empty_mu", "sss_edge_empty_act", "sss_edge_one_ring", "sss_edge_one_crystal",
+        "sss_edge_step_past_volume"]
+
+
 @pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_tiny_nx14_ny10",
-                                  "sss_tiny_wide", "sss_tiny_far"])
+                                  "sss_tiny_wide", "sss_tiny_far"] + EDGE)
 def test_oracle_sss_matches_reference(name, att_table):
     g = golden(name)
     pr = problem_from_golden(g)
