@@ -86,6 +86,11 @@ def ray_cases(seed=7):
         # lines along a face plane (touching only)
         lines[360:380, 0] = gb[0]
         lines[360:380, 3] = gb[0]
+        # zero-length segments (appended; no draw from rng): inside a voxel, on
+        # a voxel corner, on each corner of the grid, on a face, outside
+        pts = np.array([(gb[:3] + gb[3:]) / 2 + 0.3 * vox, gb[:3] + 2 * vox, gb[:3], gb[3:],
+                        np.array([gb[0], (gb[1] + gb[4]) / 2, (gb[2] + gb[5]) / 2]), gb[3:] + vox])
+        lines = np.concatenate([lines, np.concatenate([pts, pts], axis=1)])
         cases.append((grid, gb, lines))
     return cases
 
