@@ -409,6 +409,16 @@ def gen_fit(R):
         out[f"case{ci}_prompts"] = prm
         out[f"case{ci}_scale"] = np.asarray(scale, np.float32)
         print(f"fit case {ci}: scale {scale}")
+        if ci == 0:
+            # degenerate inputs on case 0: no masked LOR, no scatter, and prompts
+            # below the randoms everywhere (T = 0): the reference's lstsq gives 0
+            zero = {"mask": (prm, scat, np.zeros_like(maskf)), "scatter": (prm, np.zeros_like(scat), maskf),
+                    "trues": (np.zeros_like(prm), scat, maskf)}
+            for name, (p_, s_, m_) in zero.items():
+                sc0 = B.BackProjectionScatterRandFit(p_, s_, rnd, m_, np.array(fgrid), fit_bounds, sc.geometry, lc,
+                                                     order, af)
+                out[f"edge_no_{name}_scale"] = np.asarray(sc0, np.float32)
+                print(f"fit case 0 without {name}: scale {sc0}")
     _save("fit", **out)
 
 

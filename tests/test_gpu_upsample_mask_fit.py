@@ -96,6 +96,24 @@ def test_backprojection_fit_matches_reference(cuda_ok, case):
     assert abs(float(s[0]) - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
 
 
+@pytest.mark.parametrize("name", ["mask", "scatter", "trues"])
+def test_backprojection_fit_degenerate_inputs(cuda_ok, name):
+    """No masked LOR, no scatter, or prompts below the randoms everywhere:
+    a scale of 0, as the reference's lstsq gives."""
+    from opensss_gb300.BackProjection import BackProjectionScatterRandFit
+
+    g = golden("fit")
+    nd, nr, af = (int(v) for v in g["case0_dims"])
+    lor, si, _ = _sino(nd, nr)
+    prm, scat, mask = g["case0_prompts"], g["case0_scatter"], g["case0_mask"]
+    prm, scat, mask = {"mask": (prm, scat, 0 * mask), "scatter": (prm, 0 * scat, mask),
+                       "trues": (0 * prm, scat, mask)}[name]
+    s = BackProjectionScatterRandFit(prm, scat, g["case0_randoms"], mask, g["case0_grid"], g["case0_bounds"],
+                                     g["case0_geometry"], lor, si[:nr, :nr].T, af)
+    assert float(g[f"edge_no_{name}_scale"][0]) == 0.0
+    assert s.dtype == np.float32 and s.shape == (1,) and float(s[0]) == 0.0
+
+
 def test_fit_reads_upsampled_scatter_without_materialising(cuda_ok):
     """Fused path: the fit reads the sampled (leg-pair) sinogram through the
     upsampling tables; same scale as fitting the materialised upsampled

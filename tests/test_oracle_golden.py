@@ -101,6 +101,24 @@ def test_oracle_fit_matches_reference(case):
     assert abs(float(s[0]) - float(ref[0])) <= 1e-5 * abs(float(ref[0]))
 
 
+@pytest.mark.parametrize("name", ["mask", "scatter", "trues"])
+def test_oracle_fit_degenerate_inputs(name):
+    """No masked LOR, no scatter, or prompts below the randoms everywhere:
+    the reference's lstsq gives a scale of 0."""
+    from opensss_gb300.geometry import SinogramCoordinates
+
+    g = golden("fit")
+    nd, nr, af = (int(v) for v in g["case0_dims"])
+    lor, si, _ = SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    prm, scat, mask = g["case0_prompts"], g["case0_scatter"], g["case0_mask"]
+    prm, scat, mask = {"mask": (prm, scat, 0 * mask), "scatter": (prm, 0 * scat, mask),
+                       "trues": (0 * prm, scat, mask)}[name]
+    s = O.fit(prm, scat, g["case0_randoms"], mask, g["case0_grid"], g["case0_bounds"], g["case0_geometry"], lor,
+              si, af)
+    assert float(g[f"edge_no_{name}_scale"][0]) == 0.0
+    assert float(s[0]) == 0.0
+
+
 @pytest.mark.parametrize("case", range(2))
 def test_oracle_upsample_matches_reference(case):
     from opensss_gb300 import geometry as G
