@@ -363,9 +363,12 @@ def gen_mask(R):
     out = {}
     for ci, (nd, nr, shape, vox, af) in enumerate(((48, 6, (12, 12, 6), 2.0, 1),
                                                     (64, 8, (16, 16, 8), 1.5, 3),
-                                                    (48, 6, (12, 12, 6), 2.0, 5))):
+                                                    (48, 6, (12, 12, 6), 2.0, 5),
+                                                    (48, 6, (12, 12, 6), 2.0, 2))):
         sc = _small_scan(nd, nr)
         act, mu, bounds = W.cylinder_phantom(shape, vox, seed=ci, radius_cm=6.0)
+        if ci == 3:  # empty attenuation map: every LOR of the lattice is a tail
+            mu = np.zeros_like(mu)
         lc, si, _ = _sino(R, nd, nr)
         m = T.MaskGenerator(act, mu, bounds, sc.geometry, lc, si, True, af)
         out[f"case{ci}_dims"] = np.array([nd, nr, af])

@@ -49,7 +49,7 @@ def test_upsample_from_engine_layout(cuda_ok):
     assert np.array_equal(out.cpu().numpy().reshape(nd + 1, nd // 2, nr * nr), g["case0_sum"])
 
 
-@pytest.mark.parametrize("case", range(3))
+@pytest.mark.parametrize("case", range(4))
 def test_tail_mask_matches_reference_bit_exact(cuda_ok, case):
     from opensss_gb300.TailsMask import MaskGenerator
 

@@ -76,7 +76,7 @@ def test_oracle_sss_nontof_40x40x20_matches_reference(att_table):
     assert rel_l2(cmp, ref) < 1e-6
 
 
-@pytest.mark.parametrize("case", range(3))
+@pytest.mark.parametrize("case", range(4))
 def test_oracle_mask_matches_reference(case):
     from opensss_gb300.geometry import SinogramCoordinates
 
