@@ -526,15 +526,16 @@ def gen_span(R):
 def gen_listmode(R):
     """ExportPrompts and InjectScatters (the reference's Timber package) on
     seeded synthetic list-mode files: plain, with mash 2 and a crystal
-    shift, and with span (LookUpTable slices)."""
+    shift, with span (LookUpTable slices), and an empty file."""
     sys.path.insert(0, refpy.REFERENCE_PY)
     from Timber import Datafile as TD
 
     out = {}
-    cases = (("plain", 48, 6, 1, 0, None), ("mash_shift", 48, 6, 2, 3, None), ("span", 48, 10, 1, 0, (3, 9)))
-    for ci, (tag, ncr, nr, mash, shift, span) in enumerate(cases):
+    cases = (("plain", 48, 6, 1, 0, None, 20000), ("mash_shift", 48, 6, 2, 3, None, 20000),
+             ("span", 48, 10, 1, 0, (3, 9), 20000), ("empty", 48, 6, 1, 0, None, 0))
+    for ci, (tag, ncr, nr, mash, shift, span, nev) in enumerate(cases):
         with tempfile.TemporaryDirectory() as d:
-            hdr = W.synthetic_listmode(d, f"case{ci}_df", 20000, ncr, nr, seed=30 + ci, tof_range=1000.0)
+            hdr = W.synthetic_listmode(d, f"case{ci}_df", nev, ncr, nr, seed=30 + ci, tof_range=1000.0)
             lor, si, _ = R["Sinogram"].SinogramCoordinates(1, 1, 1, 1, ncr // mash, nr, ID_Shidt=False)
             if span:
                 msi, _, lut, _ = R["DataReduction"].SinogramLUT(nr, span[0], span[1])

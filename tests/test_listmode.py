@@ -33,7 +33,7 @@ def _write_case(g, ci, d):
     return f"{name}.Cdh"
 
 
-@pytest.mark.parametrize("ci", range(3))
+@pytest.mark.parametrize("ci", range(4))
 def test_host_decoding_reproduces_reference_histogram(ci, tmp_path):
     """Python restatement of the event layout and ParseCASToRIDs, looped over
     the events: the oracle for this row."""
@@ -76,7 +76,7 @@ def test_header_round_trip(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ci", range(3))
+@pytest.mark.parametrize("ci", range(4))
 def test_gpu_export_prompts_matches_reference(cuda_ok, ci, tmp_path):
     from opensss_gb300.Datafile import ExportPrompts
 
@@ -91,7 +91,7 @@ def test_gpu_export_prompts_matches_reference(cuda_ok, ci, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ci", range(3))
+@pytest.mark.parametrize("ci", range(4))
 def test_gpu_inject_scatters_matches_reference(cuda_ok, ci, tmp_path):
     from opensss_gb300.Datafile import InjectScatters
 
