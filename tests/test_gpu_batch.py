@@ -166,3 +166,23 @@ def test_batch_run_on_a_side_stream(cuda_ok, att_table):
     for a, r in zip(got, ref):
         assert rel_l2(a, r) < TOL
     b.close()
+
+
+def test_batch_with_degenerate_problems(cuda_ok, att_table):
+    """A batch mixing ordinary problems with one that has no scatter point
+    (empty attenuation map) and one with no activity: the degenerate ones
+    plan no item and come out all zero; the others match their solo runs."""
+    from opensss_gb300.batch import BatchSSS
+
+    probs = _uneven_problems()[:2]
+    empty_mu, empty_act = _uneven_problems()[2], _uneven_problems()[3]
+    empty_mu.attenuation = np.zeros_like(empty_mu.attenuation)
+    empty_act.activity = np.zeros_like(empty_act.activity)
+    probs += [empty_mu, empty_act]
+    engines = [_engine(pr, att_table) for pr in probs]
+    b = BatchSSS([(e, pr.activity, pr.attenuation, pr.image_size) for e, pr in zip(engines, probs)])
+    outs = [o.cpu().numpy() for o in b.run()]
+    for e, pr, got in zip(engines[:2], probs[:2], outs[:2]):
+        assert rel_l2(got, _solo(e, pr)) < TOL, pr.name
+    assert not outs[2].any() and not outs[3].any()
+    b.close()
