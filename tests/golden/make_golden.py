@@ -574,8 +574,54 @@ def gen_listmode(R):
     _save("listmode", **out)
 
 
+# parameter-file lines covering every typing rule of ReadParameters (one file
+# per entry of SUPPORT_BAD: lines the reference rejects)
+SUPPORT_LINES = [
+    "# comment line", "", "   ", "Path2Data = 'Data'", 'Name = "scan_df.Cdh"', "Plain = some text",
+    "Flag = True", "Off = False", "QuotedFlag = 'True'", "Int = 42", "Neg = -7", "Float = 0.108", "Sci = 1e-3",
+    "Inf = inf", "Tuple = (1, 2, 3)", "TupleF = (1.5, 2, 3)", "Tuple4 = (1, 2, 3, 4)", "TupleS = (a, b, c)",
+    "TupleNoSpace = (1,2,3)", "List = [1, 2, 3]", "ListF = [0.5, 2]", "ListS = [x, y]", "ListEmpty = []",
+    "Nested = ([1, 2])", "Empty =", "Quote = '", "Spaces   =   8   ", "Mixed = '(4, 5, 6)'", "Under = 1_000",
+]
+SUPPORT_BAD = ["Two = a = b", "NoEquals", "Short = (1, 2)"]
+NORMALIZE_CASES = [
+    (np.linspace(-3.0, 5.0, 24).reshape(2, 3, 4), 0, 255),
+    (np.full((2, 2, 2), 7.0), 0, 255),
+    (np.arange(8, dtype=np.float32).reshape(2, 2, 2), -1.0, 1.0),
+    (np.arange(12).reshape(3, 2, 2), 0, 100),
+]
+
+
+def gen_support(R):
+    S = R["Support"]
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "params.txt")
+        with open(path, "w") as f:
+            f.write("\n".join(SUPPORT_LINES) + "\n")
+        out["params_repr"] = np.array(repr(S.ReadParameters(path)))
+        errors = []
+        for line in SUPPORT_BAD:
+            with open(path, "w") as f:
+                f.write(line + "\n")
+            try:
+                S.ReadParameters(path)
+                errors.append("")
+            except Exception as e:  # the reference's exception type is the fixture
+                errors.append(type(e).__name__)
+        out["bad_errors"] = np.array(errors)
+    out["lines"] = np.array(SUPPORT_LINES)
+    out["bad_lines"] = np.array(SUPPORT_BAD)
+    for i, (a, lo, hi) in enumerate(NORMALIZE_CASES):
+        out[f"normalize{i}_in"] = a
+        out[f"normalize{i}_range"] = np.array([lo, hi], dtype=np.float64)
+        out[f"normalize{i}"] = S.NormalizeArray(a, lo, hi)
+    print(f"support: {out['params_repr']}; errors {errors}")
+    _save("support", **out)
+
+
 ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_edge", "upsample", "upsample_lut",
-       "mask", "fit", "span", "listmode", "prep"]
+       "mask", "fit", "span", "listmode", "prep", "support"]
 
 
 # ---------------------------------------------------------------- image preparation
@@ -682,6 +728,8 @@ def main():
         gen_listmode(R)
     if "prep" in which:
         gen_prep(R)
+    if "support" in which:
+        gen_support(R)
 
 
 if __name__ == "__main__":
