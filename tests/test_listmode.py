@@ -108,3 +108,55 @@ def test_gpu_inject_scatters_matches_reference(cuda_ok, ci, tmp_path):
     assert np.array_equal(got, g[f"case{ci}_injected"])
     text = (tmp_path / (hdr[:-6] + "scatter_" + hdr[-6:])).read_text()
     assert text == g[f"case{ci}_injected_header"].tobytes().decode()
+
+
+def test_generate_prompts_cache_rule(tmp_path, monkeypatch):
+    """GeneratePrompts histograms once per SavePath and span setting (the
+    reference's file names); a later call finds the prompts file and skips
+    the histogram.  The histogram itself is replaced by a recording fake."""
+    from opensss_gb300 import IO
+
+    calls = []
+
+    def fake_export(DataPath, DataHeader, lor, table, bins, rng, mash=1, Shift=0, device="cuda"):
+        calls.append((table, mash, Shift))
+        return np.zeros((2, 2, 2, bins), np.uint16), np.zeros((2, 2, 2), np.float32), np.ones((2, 2, 2), np.float32)
+
+    monkeypatch.setattr(IO.Datafile, "ExportPrompts", fake_export)
+    si, lut = np.zeros((2, 2)), np.ones((2, 2))
+    assert IO.GeneratePrompts(str(tmp_path), "d", "h", None, si, lut, 3, 1000.0, 1, 2, 5)
+    assert calls[-1][0] is si and calls[-1][1:] == (2, 5)
+    assert not IO.GeneratePrompts(str(tmp_path), "d", "h", None, si, lut, 3, 1000.0, 1, 2, 5)
+    assert IO.GeneratePrompts(str(tmp_path), "d", "h", None, si, lut, 3, 1000.0, 3, 1)  # span: its own file
+    assert calls[-1][0] is lut and len(calls) == 2
+    assert not IO.GeneratePrompts(str(tmp_path), "d", "h", None, si, lut, 3, 1000.0, 3, 1)
+    assert not IO.GeneratePrompts(str(tmp_path / "x"), "d", "h", None, si, lut, 3, 1000.0, 0, 1)
+    names = sorted(os.listdir(tmp_path))
+    assert names == ["NormSinogram.npz", "PromptsSinogram.npz", "PromptsSinogramMashed.npz", "RandomsSinogram.npz"]
+    assert np.load(tmp_path / "PromptsSinogram.npz")["arr_0"].shape == (2, 2, 2, 3)
+
+
+def test_create_directories(tmp_path, capsys):
+    from opensss_gb300 import IO
+
+    params = tmp_path / "p.txt"
+    params.write_text("TOFbins = 6\n")
+    IO.CreateDirectories(str(tmp_path / "out"), "Images", "Scatters", str(params))
+    assert (tmp_path / "out" / "Images").is_dir() and (tmp_path / "out" / "Scatters").is_dir()
+    assert (tmp_path / "out" / "parameters_backup.txt").read_text() == "TOFbins = 6\n"
+    IO.CreateDirectories(str(tmp_path / "out"), "Images", "Scatters", str(tmp_path / "missing.txt"))
+    assert "Unable to copy file" in capsys.readouterr().out
+
+
+@pytest.mark.gpu
+def test_gpu_generate_prompts_writes_the_reference_histogram(cuda_ok, tmp_path):
+    from opensss_gb300 import IO
+
+    g = golden("listmode")
+    ncr, nr, mash, shift, span, mrd = (int(v) for v in g["case1_args"])
+    lor, si, msi, lut, table = _tables(ncr, nr, mash, span, mrd)
+    hdr = _write_case(g, 1, str(tmp_path))
+    assert IO.GeneratePrompts(str(tmp_path), str(tmp_path), hdr, lor, si, lut, 5, 1000.0, 1, mash, shift)
+    assert np.array_equal(np.load(tmp_path / "PromptsSinogram.npz")["arr_0"], g["case1_prompts"])
+    assert np.array_equal(np.load(tmp_path / "RandomsSinogram.npz")["arr_0"], g["case1_randoms"])
+    assert np.array_equal(np.load(tmp_path / "NormSinogram.npz")["arr_0"], g["case1_norm"])
