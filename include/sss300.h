@@ -79,8 +79,10 @@ typedef struct sss_tof_problem {
     const double *normals;         /* device, [nr][nd][3] face normals */
     double detector_size[2];       /* crystal face, mm */
     int32_t nru, ndu;              /* sampled rings, sampled crystals per ring */
-    const int32_t *rings;          /* device, [nru] ring numbers (:153) */
-    const int32_t *detectors;      /* device, [ndu] crystal numbers (:159-167) */
+    const int32_t *rings;          /* device, [nru] ring numbers (:153), each in 0..nr-1 */
+    const int32_t *detectors;      /* device, [ndu] crystal numbers (:159-167), each in 0..nd-1;
+                                      the library reads both arrays on the device only and does
+                                      not check their values */
     int32_t sample_step[3];        /* scatter-point lattice step, voxels */
     int32_t nbins;                 /* TOF bins, 1..64 */
     double tof_bin_width;          /* ps, 2*TOFRange/NrBins */
