@@ -282,3 +282,42 @@ def test_far_golden_reaches_past_the_factored_range(att_table):
     assert np.isnan(run(weights)).any()
     # without the NaN terms, the zero weights past the range still show: 5e-2
     assert rel_l2(run(np.nan_to_num(weights, nan=0.0)), g["compact"]) > 1e-2
+
+
+def _t_safe(nb, rng, res):
+    """Planned split point of the fix: past it, ca * A falls below 2^-126 for
+    ca < 2^-64 ((B-1) beta > 62), so those offsets take the per-bin path."""
+    w = 2 * rng / nb
+    return (nb - 1) / 2.0 * w + 62.0 / ((nb - 1) * 2 * (4.0 / res ** 2) * w)
+
+
+def _per_bin_weights(nb, rng, res):
+    """The per-bin evaluation 2^(Y - d (beta + gamma d)), d = n - b, in float32
+    (the non-factored path of the pair kernel, with exp2 for its ex2)."""
+    f32 = np.float32
+    w = 2 * rng / nb
+    kappa = 4.0 / (res * res)
+    l2 = T.tof_log2_table(nb, rng, res).astype(np.float32)
+    Y, n = l2[:, 0], l2[:, 1]
+    k2w, gam = f32(2 * kappa * w), f32(kappa * w * w)
+    s0, W = f32((1.0 - (nb + 1) / 2.0) * w), f32(w)
+    beta = (k2w * (np.arange(-4000, 4001).astype(np.float32) - (n * W + s0))).astype(np.float32)
+    d = (n[None, :] - np.arange(nb, dtype=np.float32)[:, None]).astype(np.float32)
+    with np.errstate(all="ignore"):
+        out = np.exp2((Y[None, :] - d * (beta[None, :] + gam * d)).astype(np.float32)).astype(np.float64)
+    out[:, ~np.isfinite(Y)] = 0
+    return out
+
+
+@pytest.mark.parametrize("nb,rng,res", _FACTORED + [(5, 5 * 1.0 / _C, 60.0), (2, 2 * 4.0 / _C, 214.0)])
+def test_planned_split_keeps_every_offset_exact(nb, rng, res):
+    """The fix planned for the far-offset issue: factored weights up to
+    t_safe, per-bin weights past it.  In float32 emulation that matches the
+    FP64 table at every offset, for voxel terms ca down to 2^-64."""
+    ref = T.tof_table(nb, rng, res)
+    t = np.arange(-4000, 4001)
+    exact = _per_bin_weights(nb, rng, res)
+    for ca in (1.0, 2.0 ** -27, 2.0 ** -64):
+        got = np.where((t <= _t_safe(nb, rng, res))[None, :], _factored_weights(nb, rng, res, ca), exact)
+        assert np.isfinite(got).all()
+        assert np.abs(got - ref).max() < 1e-5, ca
