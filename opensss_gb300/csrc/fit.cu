@@ -424,7 +424,12 @@ extern "C" int sss_upsample(const float* sampled, int64_t bin_stride, int32_t nb
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long cap = (long long)sms * 8;
     const unsigned blocks = (unsigned)(ncell < cap ? ncell : cap);
-    upsample_kernel<<<blocks, 256, sizeof(float) * nring, (cudaStream_t)stream>>>(
+    const size_t smem = sizeof(float) * (size_t)nring;
+    // more than 12288 ring pairs (over 110 sampled rings) need the opt-in past 48 KB
+    if (smem > 48 * 1024 && cudaFuncSetAttribute((const void*)upsample_kernel,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return sss_set_error(SSS_ERR_CUDA, "sss_upsample: %zu bytes of shared memory refused", smem);
+    upsample_kernel<<<blocks, 256, smem, (cudaStream_t)stream>>>(
         sampled, bin_stride, nbins, (const long long*)cell_src, ncell, (const long long*)ring_off, nring,
         ring_idx, nslices, out);
     return sss_check_launch("upsample_kernel");
