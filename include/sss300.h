@@ -160,7 +160,8 @@ int sss_tof_run(const sss_tof_problem *p, const double *points, int64_t n_points
 
 /* Expand the leg-pair output to the reference's dense layout
  * [nbins][nd+1][nd/2][nru*nru] (SingleScatterSimulationTOF.py:171).  lor
- * (device) is LORCoordinates int16 [nd][nd][2] (Python/openSSS/Sinogram.py:121-122).
+ * (device) is LORCoordinates int16 [nd][nd][2] (Python/openSSS/Sinogram.py:121-122), every
+ * entry in range (angular < nd/2, radial <= nd; not checked on the device).
  * dense must be zeroed by the caller. */
 int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
                     const int16_t *lor, const int32_t *detectors, float *dense, void *stream);
