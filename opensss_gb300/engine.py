@@ -222,6 +222,7 @@ class TofSSS:
     def densify(self, compact: torch.Tensor, lor) -> torch.Tensor:
         """Leg-pair layout -> reference layout [B, ND+1, ND//2, NRU^2] (CUDA)."""
         dev = self.device
+        lor = geometry.check_dense_lor(lor, self.dets_np, self.nd)
         lor_t = as_device(np.asarray(lor, dtype=np.int16), torch.int16, dev)
         dense = torch.zeros((self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru),
                             dtype=torch.float32, device=dev)

@@ -58,6 +58,25 @@ def SinogramCoordinates(NrSectorsTrans: int, NrSectorsAxial: int, NrModulesAxial
     return lor.astype(np.int16), sino.astype(np.int16), int(shift)
 
 
+def check_dense_lor(lor, detectors, nd: int) -> np.ndarray:
+    """The LORCoordinates table ``sss_tof_densify`` reads, checked on the
+    host: shape [nd, nd, 2], and for every pair of sampled crystals (di1 <=
+    di2) an angle in 0..nd/2-1 and a radius in 0..nd, the bounds of the
+    dense [B, nd+1, nd/2, NRU^2] output.  Raises IndexError otherwise (the
+    reference's numpy indexing raises for entries past the array)."""
+    lor = np.asarray(lor)
+    if lor.shape != (nd, nd, 2):
+        raise ValueError(f"SinogramCoordinates must be [{nd}, {nd}, 2], got {lor.shape}")
+    d = np.asarray(detectors, dtype=np.int64)
+    i1, i2 = np.triu_indices(len(d))
+    pairs = lor[d[i1], d[i2]]
+    ang, rad = pairs[:, 0], pairs[:, 1]
+    if len(pairs) and (ang.min() < 0 or ang.max() >= nd // 2 or rad.min() < 0 or rad.max() > nd):
+        raise IndexError(f"SinogramCoordinates of a sampled crystal pair lie outside the "
+                         f"{nd + 1} x {nd // 2} sinogram")
+    return lor
+
+
 def sampled_rings(nr_rings: int, nr_rings_used: int) -> np.ndarray:
     """Rings the SSS simulates (``SingleScatterSimulationTOF.py:153``)."""
     return np.floor(np.linspace(0, nr_rings - 1, nr_rings_used) + 0.5).astype(np.int64)

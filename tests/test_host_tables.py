@@ -321,3 +321,27 @@ def test_planned_split_keeps_every_offset_exact(nb, rng, res):
         got = np.where((t <= _t_safe(nb, rng, res))[None, :], _factored_weights(nb, rng, res, ca), exact)
         assert np.isfinite(got).all()
         assert np.abs(got - ref).max() < 1e-5, ca
+
+
+def test_dense_lor_check_accepts_reference_tables_and_rejects_bad_ones():
+    from opensss_gb300 import geometry as G
+
+    for args in ((1, 1, 1, 1, 48, 6), (38, 8, 1, 1, 20, 10), (1, 1, 1, 1, 64, 8)):
+        for shift in (False, True):
+            lor, _, _ = G.SinogramCoordinates(*args, ID_Shidt=shift)
+            nd = lor.shape[0]
+            for ndu in (1, 8, nd // 2, nd):
+                G.check_dense_lor(lor, G.sampled_detectors(nd, ndu), nd)
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, 48, 6, ID_Shidt=False)
+    dets = G.sampled_detectors(48, 8)
+    with pytest.raises(ValueError):
+        G.check_dense_lor(lor[:40, :40], dets, 48)
+    for bad in ((dets[1], dets[3], 0, 24), (dets[0], dets[5], 1, 49), (dets[2], dets[2], 1, -1)):
+        d1, d2, k, v = bad
+        t = lor.copy()
+        t[d1, d2, k] = v
+        with pytest.raises(IndexError):
+            G.check_dense_lor(t, dets, 48)
+    t = lor.copy()
+    t[dets[3], dets[1], 0] = 99  # di1 > di2: never read
+    G.check_dense_lor(t, dets, 48)
