@@ -52,7 +52,7 @@ def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramI
             int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(pairs), nslices, nslices,
             int(AccelerationFactor or 1), _ptr(out), _ptr(status), C.c_void_p(st.cuda_stream)))
     else:
-        si = as_device(np.asarray(SinogramIndex, dtype=np.int16)[:nr, :nr], torch.int16, device)
+        si = as_device(geometry.check_slice_table(SinogramIndex, nr).astype(np.int16), torch.int16, device)
         out = torch.zeros(((nd + 1) * (nd // 2), nr * nr), dtype=torch.uint8, device=device)
         _lib.check(_lib.lib().sss_tail_mask(grid.ctypes.data_as(C.c_void_p),
                                             bounds.ctypes.data_as(C.c_void_p), _ptr(vol),

@@ -77,6 +77,18 @@ def check_dense_lor(lor, detectors, nd: int) -> np.ndarray:
     return lor
 
 
+def check_slice_table(SinogramIndex, nr: int) -> np.ndarray:
+    """SinogramIndex[:nr, :nr] as the tail mask reads it on the device: every
+    ring pair's slice in 0..nr^2-1, the mask's slice axis.  Raises IndexError
+    otherwise (the reference's numpy indexing raises past the axis)."""
+    si = np.asarray(SinogramIndex)[:nr, :nr]
+    if si.shape != (nr, nr):
+        raise ValueError(f"SinogramIndex must cover {nr} x {nr} ring pairs, got {si.shape}")
+    if si.size and (si.min() < 0 or si.max() >= nr * nr):
+        raise IndexError(f"SinogramIndex holds slices outside 0..{nr * nr - 1}")
+    return si
+
+
 def sampled_rings(nr_rings: int, nr_rings_used: int) -> np.ndarray:
     """Rings the SSS simulates (``SingleScatterSimulationTOF.py:153``)."""
     return np.floor(np.linspace(0, nr_rings - 1, nr_rings_used) + 0.5).astype(np.int64)

@@ -345,3 +345,20 @@ def test_dense_lor_check_accepts_reference_tables_and_rejects_bad_ones():
     t = lor.copy()
     t[dets[3], dets[1], 0] = 99  # di1 > di2: never read
     G.check_dense_lor(t, dets, 48)
+
+
+def test_slice_table_check_accepts_reference_tables_and_rejects_bad_ones():
+    from opensss_gb300 import geometry as G
+
+    for args in ((1, 1, 1, 1, 48, 6), (38, 8, 1, 1, 20, 10), (1, 1, 1, 1, 64, 8)):
+        _, si, _ = G.SinogramCoordinates(*args, ID_Shidt=False)
+        nr = si.shape[0]
+        assert np.array_equal(G.check_slice_table(si, nr), si)
+    _, si, _ = G.SinogramCoordinates(1, 1, 1, 1, 48, 6, ID_Shidt=False)
+    with pytest.raises(ValueError):
+        G.check_slice_table(si[:4, :4], 6)
+    for v in (-1, 36):
+        t = si.copy()
+        t[2, 3] = v
+        with pytest.raises(IndexError):
+            G.check_slice_table(t, 6)
