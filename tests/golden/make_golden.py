@@ -265,6 +265,50 @@ def gen_sss(R, which):
               ref_cores=np.array(os.cpu_count()))
 
 
+class _OneSlice:
+    """Stand-in for joblib.Parallel inside the reference's driver: runs the
+    delayed bodySSS call of one z-slice only (argument 0 is zIndex) and
+    returns its dense slice term, so that one slice of a full-size problem
+    fits in host memory (each term is a dense [B, ND+1, ND/2, NRU^2] array)."""
+
+    def __init__(self, z):
+        self.z = z
+
+    def __call__(self, *args, **kwargs):
+        def run(calls):
+            out = [f(*a, **kw) for f, a, kw in calls if a[0] == self.z]
+            assert len(out) == 1, "the chosen z-slice is not on the sampling lattice"
+            return out
+        return run
+
+
+def gen_sss_slice(R, z=24, ncells=50000, seed=17):
+    """One sampled z-slice (zIndex 24 of the 48) of the 13-bin, 64x64x48 @ 6 mm
+    workload on the 760 x 80 scanner, 16 x 48 sampled: the reference's own
+    driver with its parallel loop restricted to that slice.  The fixture keeps
+    a seeded subset of the compact cells and every bin's total."""
+    S = R["SingleScatterSimulationTOF"]
+    pr = W.tof13_64x64x48(seed=0)
+    nd, nr = pr.scanner.nr_detectors, pr.scanner.nr_rings
+    LC, _, _ = _sino(R, nd, nr)
+    saved = S.Parallel
+    S.Parallel = _OneSlice(z)
+    try:
+        dense, dt = _run_sss(R, pr, LC)
+    finally:
+        S.Parallel = saved
+    cmp = _compact_from_dense(dense, LC, nd, pr.nr_rings_used, pr.nr_detectors_used)
+    del dense
+    flat = cmp.reshape(cmp.shape[0], -1)
+    rng = np.random.default_rng(seed)
+    nz = np.flatnonzero(flat.any(axis=0))
+    cells = np.sort(rng.choice(nz, size=min(ncells, len(nz)), replace=False))
+    print(f"sss_tof13_slice: zIndex {z}, reference {dt:.0f} s, {len(nz)} contributing cells, kept {len(cells)}")
+    _save("sss_tof13_slice", z_index=np.array(z), lattice_slice=np.array(z // int(pr.sample_step[2])),
+          cells=cells.astype(np.int64), values=flat[:, cells], bin_totals=flat.astype(np.float64).sum(axis=1),
+          contributing=np.array(len(nz)), shape=np.array(cmp.shape), ref_seconds=np.array(dt))
+
+
 # ---------------------------------------------------------------- tables / LUTs
 
 
@@ -620,7 +664,8 @@ def gen_support(R):
     _save("support", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_edge", "upsample", "upsample_lut",
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_edge",
+       "sss_tof13_slice", "upsample", "upsample_lut",
        "mask", "fit", "span", "listmode", "prep", "support"]
 
 
@@ -711,7 +756,9 @@ def main():
         gen_rays(R)
     if "tables" in which:
         gen_tables(R)
-    sss = [w.split("_", 1)[1] for w in which if w.startswith("sss_")]
+    if "sss_tof13_slice" in which:
+        gen_sss_slice(R)
+    sss = [w.split("_", 1)[1] for w in which if w.startswith("sss_") and w != "sss_tof13_slice"]
     if sss:
         gen_sss(R, sss)
     if "upsample" in which:

@@ -291,3 +291,23 @@ def test_far_tof_offsets_match_reference(cuda_ok, att_table):
     assert np.isfinite(got).all()
     assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
+
+
+def test_tof13_slice_matches_reference(cuda_ok, att_table):
+    """One sampled z-slice of the 13-bin benchmark workload on the 760 x 80
+    scanner (the reference's own driver restricted to that slice): a seeded
+    subset of 50,000 cells and every bin's total."""
+    from opensss_gb300 import workloads as W
+    from opensss_gb300.engine import leg_pair_to_compact
+
+    g = golden("sss_tof13_slice")
+    pr = W.tof13_64x64x48(seed=0)
+    k = int(g["lattice_slice"])
+    lp = _engine(pr, att_table).run(pr.activity, pr.attenuation, pr.image_size, slice_range=(k, k + 1))
+    cmp = leg_pair_to_compact(lp.cpu().numpy(), pr.nr_rings_used, pr.nr_detectors_used)
+    assert tuple(cmp.shape) == tuple(g["shape"])
+    flat = cmp.reshape(cmp.shape[0], -1)
+    got, ref = flat[:, g["cells"]], g["values"]
+    assert_same_support(got, ref)
+    assert rel_l2(got, ref) < TOL
+    np.testing.assert_allclose(flat.astype(np.float64).sum(axis=1), g["bin_totals"], rtol=TOL)
