@@ -1,7 +1,7 @@
 """Python face of the oracle (test infrastructure only).
 
 ORACLE — only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
-baseline import this module, and only as the checker or the timed CPU
+baseline import this module, and only as the test oracle or the timed CPU
 reference arm.  It loads ``oracle/_build/libsssoracle.so`` (the FP64 C
 restatement) and, where it was built, the reference's own MEX ray tracers from
 ``oracle/_ref``.  The per-problem tables are rebuilt here independently of the

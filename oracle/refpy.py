@@ -1,11 +1,11 @@
 """Loader for the reference openSSS Python package (test infrastructure only).
 
-ORACLE — this module is part of the checker, never of the product.  It imports
+ORACLE — this module is test infrastructure, never part of the product.  It imports
 the unmodified reference modules from the reference checkout (default
 ``/root/reference/Python``, override with ``OPENSSS_REFERENCE``) with a
 pass-through ``numba`` stub first on ``sys.path``.  It is used only by
-``tests/golden/make_golden.py`` in the build container to produce the golden
-fixtures committed under ``tests/golden``; nothing on a GPU machine imports it.
+``tests/golden/make_golden.py`` where the reference checkout exists, to produce
+the golden fixtures committed under ``tests/golden``; nothing at run time imports it.
 """
 
 import os

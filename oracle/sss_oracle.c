@@ -2,7 +2,7 @@
  * ORACLE — test infrastructure, not product code.
  *
  * A plain-C, FP64 restatement of the openSSS (v1.0, Python) algorithms on the
- * TOF-SSS path.  It is the checker for the CUDA engine and the CPU baseline
+ * TOF-SSS path.  It is the test oracle for the CUDA engine and the CPU baseline
  * timed by bench.py; the engine never links or calls it.  Every function
  * follows the reference's arithmetic step by step (IEEE FP64, no FMA
  * contraction: build with -ffp-contract=off) and cites the reference lines it
