@@ -1,6 +1,6 @@
 """Pass-through stand-in for ``numba`` (test infrastructure only).
 
-numba is not installed in the build container.  The reference package
+numba need not be installed.  The reference package
 decorates its kernels with ``@jit(nopython=True)``; numba without fast-math
 compiles them to IEEE FP64 without FMA contraction, which is exactly what the
 plain CPython interpreter computes.  This stub makes ``jit`` the identity so

@@ -5,7 +5,7 @@ pass-through numba stub in ``oracle/numba_stub``) and the reference's MEX ray
 tracers compiled from source (``oracle/_ref``), on seeded synthetic inputs,
 and stores inputs + outputs as compressed ``.npz`` fixtures.  It needs the
 reference checkout (``OPENSSS_REFERENCE``, default ``/root/reference/Python``)
-and is run by hand in the build container:
+and is run by hand where that checkout exists:
 
     python tests/golden/make_golden.py [--only name,...]
 
