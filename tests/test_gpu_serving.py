@@ -71,3 +71,36 @@ def test_served_results_match_solo_runs(cuda_ok, att_table, budget_mb, large_ws_
     plain = PlainServer(beds).serve(poisson_stream(2000.0, 0.015, beds, 0.7, seed=1))
     for a, b in zip(served, plain):
         assert rel_l2(a.out.cpu().numpy(), b.out.cpu().numpy()) < TOL
+
+
+@pytest.mark.gpu
+def test_request_over_the_hbm_budget_is_refused(cuda_ok, att_table):
+    """Admission: with nothing in flight, a batch that cannot fit the HBM
+    budget raises MemoryError before any of its work is enqueued."""
+    from opensss_gb300.serving import Request, ScatterServer
+
+    beds = _beds(att_table)[:1]
+    srv = ScatterServer(beds, hbm_budget=1 << 20)
+    with pytest.raises(MemoryError, match="HBM budget"):
+        srv.serve([Request(0, 0.0, 0, seed=1)])
+
+
+@pytest.mark.gpu
+def test_device_error_of_a_served_request_is_raised(cuda_ok, att_table):
+    """A served problem whose TOF offsets pass the 8001-entry table (the
+    reference raises IndexError there): the batch's status word reports it
+    and serve() raises SSS_ERR_TOF_RANGE once the stream has drained."""
+    from conftest import golden, problem_from_golden
+    from opensss_gb300 import TofSSS
+    from opensss_gb300._lib import SSSError
+    from opensss_gb300.serving import Request, ScatterServer, make_bed
+
+    pr = problem_from_golden(golden("sss_tofrange"))
+    e = TofSSS(pr.scanner.geometry, pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+               pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used,
+               pr.sample_step, pr.tof_resolution, pr.tof_range, pr.nr_bins)
+    bed = make_bed(e, pr.activity, pr.attenuation, pr.image_size)
+    srv = ScatterServer([bed], hbm_budget=8 << 30)
+    with pytest.raises(SSSError) as err:
+        srv.serve([Request(0, 0.0, 0, seed=1)])
+    assert err.value.code == 4
