@@ -37,8 +37,11 @@ enum {
     SSS_ERR_VOXEL = 6,      /* linear voxel index outside the volume (only if Nx != Ny) */
     SSS_ERR_WORKSPACE = 7,  /* workspace too small */
     SSS_ERR_CAPACITY = 8,   /* an output capacity was too small */
-    SSS_ERR_EVENT = 9       /* a list-mode event addresses a crystal or ring outside the sinogram
+    SSS_ERR_EVENT = 9,      /* a list-mode event addresses a crystal or ring outside the sinogram
                                tables; the reference raises IndexError (Timber/Datafile.py:90-92) */
+    SSS_ERR_NONFINITE = 10  /* a scatter term came out infinite or NaN; no reference counterpart
+                               (the reference's nan_to_num, SingleScatterSimulationTOF.py:557, only
+                               hides 0/0 of empty slices): the result must not be used */
 };
 
 /* Thread-local text of the last error. */

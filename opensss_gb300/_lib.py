@@ -18,7 +18,7 @@ ABI_VERSION = 3  # SSS300_ABI_VERSION of include/sss300.h
 ERROR_NAMES = {
     1: "SSS_ERR_INVALID", 2: "SSS_ERR_CUDA", 3: "SSS_ERR_OVERRUN", 4: "SSS_ERR_TOF_RANGE",
     5: "SSS_ERR_ENERGY", 6: "SSS_ERR_VOXEL", 7: "SSS_ERR_WORKSPACE", 8: "SSS_ERR_CAPACITY",
-    9: "SSS_ERR_EVENT",
+    9: "SSS_ERR_EVENT", 10: "SSS_ERR_NONFINITE",
 }
 
 # every symbol the header declares, with (restype, argtypes)

@@ -47,6 +47,10 @@ extern "C" int sss_status_code(int32_t s)
         return sss_set_error(SSS_ERR_ENERGY, "a scattered energy row fell outside the tables");
     if (s & kErrCapacity)
         return sss_set_error(SSS_ERR_CAPACITY, "an internal capacity was exceeded");
+    if (s & kErrNonFinite)
+        return sss_set_error(SSS_ERR_NONFINITE,
+                             "a detector pair's scatter term came out infinite or NaN (the result is not "
+                             "usable)");
     if (s & kErrEvent)
         return sss_set_error(SSS_ERR_EVENT,
                              "a list-mode event addresses a crystal or ring outside the sinogram tables "

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(pair_block_warps(NP, false) * 32, MINB)
     load_pair_tables(tof_log2w, T, sAR, sN, sG);
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    bool tof_bad = false, energy_bad = false;
+    bool tof_bad = false, energy_bad = false, nonfinite = false;
     unsigned long long walked = 0, npairs = 0;
     for (;;) {
         long long task = 0;
@@ -83,9 +83,9 @@ __global__ void __launch_bounds__(pair_block_warps(NP, false) * 32, MINB)
         const PairItem& it = items[lo];
         const int rem = (int)(task - it.task_begin);
         walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sAR,
-                                          sN, sG, vbuf, nullptr, tof_bad, energy_bad, walked, npairs);
+                                          sN, sG, vbuf, nullptr, tof_bad, energy_bad, nonfinite, walked, npairs);
     }
-    finish_pairs(lane, tof_bad, energy_bad, walked, npairs, status, nullptr);
+    finish_pairs(lane, tof_bad, energy_bad, nonfinite, walked, npairs, status, nullptr);
 }
 
 using BatchPairFn = void (*)(const PairItem*, int, long long, TofConst, const float*, unsigned int*,

@@ -17,6 +17,7 @@ enum DeviceError : int32_t {
     kErrVoxel = 1 << 3,      // linear voxel index outside the volume (Nx != Ny case)
     kErrCapacity = 1 << 4,   // an internal list capacity was exceeded
     kErrEvent = 1 << 5,      // a list-mode event outside the sinogram tables (reference: IndexError)
+    kErrNonFinite = 1 << 6,  // a detector pair's slice term came out infinite or NaN
     // not an error: set by the tail mask's pre-pass when the map has a negative
     // or NaN value (its line integrals can then shrink); sss_status_code ignores it
     kNoteMapSigned = 1 << 30,

@@ -53,6 +53,9 @@ struct TofConst {
     float s0, w;           // first bin centre offset and bin width (ps)
     float kappa2w, gamma;  // 2 kappa w and kappa w^2, kappa = 4/FWHM^2 (log2 units)
     int factored;          // weights as 2^(Y - n beta) r^b G[n][b] (see accumulate_voxel)
+    int tsafe;             // table entries below this index use the factored weights; entries
+                           // from it on (offsets far past the last bin) hold (Y, 0) and take
+                           // the per-bin 2^x evaluation (see far_voxel)
     int nbins;
     int nmask;             // low mantissa bits of the tabled A that carry the nearest bin n
 };
@@ -90,6 +93,19 @@ inline TofConst tof_const(const sss_tof_problem& p)
     // w / FWHM < 1.33 (offsets whose column is still above 2^-126 have
     // beta < 45 w / FWHM, so r^2 = 2^(2 beta) < 2^120).
     T.factored = p.nbins > 1 && (kappa * w * w) * (p.nbins - 1) < 100.0 && w / p.tof_resolution < 1.33;
+    // Past the last bin centre s_{B-1} the nearest bin is B-1 and the chain
+    // starts at ca 2^(Y - (B-1) beta), beta = 2 kappa w (t - s_{B-1}).  Up to
+    // (B-1) beta = 62 that start stays a normal float for voxel terms ca down
+    // to 2^-64 and r^2 = 2^(2 beta) stays below 2^124; offsets beyond take the
+    // per-bin path.  Offsets below -4000 ps wrap into the table's top (numpy's
+    // negative index), so the far entries are one suffix of the table.
+    T.tsafe = kTofEntries;
+    if (T.factored) {
+        const double s_last = (1.0 - (p.nbins + 1) / 2.0) * w + (p.nbins - 1) * w;
+        const double t_safe = s_last + 62.0 / ((p.nbins - 1) * 2.0 * kappa * w);
+        const double idx = floor(t_safe) + kTimeRange + 1;  // first entry whose offset passes t_safe
+        T.tsafe = idx >= kTofEntries ? kTofEntries : (int)idx;
+    }
     T.nbins = p.nbins;
     int bits = 1;
     while ((1 << bits) < p.nbins) ++bits;
@@ -121,11 +137,11 @@ __device__ __forceinline__ float pack_bin(float a, int n, int mask)
 }
 
 // Block-wide set-up of the shared tables.  From the (log2 largest weight Y,
-// bin n) table: for the factored weights, per TOF offset t, beta(t) = 2 kappa
-// w (t - 4000 - s_n) rounded to float once, r = 2^beta and A = 2^(Y - n beta)
-// with the same beta (so that A r^n = 2^Y up to rounding), A rounded to the
-// nearest value whose low bits hold n (relative change below 2^-(24 - bits),
-// bits = ceil(log2 nbins)); otherwise (Y, 0).
+// bin n) table: for the factored weights, per TOF offset t below T.tsafe,
+// beta(t) = 2 kappa w (t - 4000 - s_n) rounded to float once, r = 2^beta and
+// A = 2^(Y - n beta) with the same beta (so that A r^n = 2^Y up to rounding),
+// A rounded to the nearest value whose low bits hold n (relative change below
+// 2^-(24 - bits), bits = ceil(log2 nbins)); otherwise (Y, 0).
 // G[n][b] = 2^(-gamma (n - b)^2), 0 past the last bin and in the padding.
 __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst& T, float2* sAR,
                                                  unsigned char* sN, float* sG)
@@ -134,7 +150,7 @@ __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst&
         const float Y = g[2 * i];
         const float n = g[2 * i + 1];
         sN[i] = (unsigned char)n;
-        if (T.factored) {
+        if (T.factored && i < T.tsafe) {
             const float off = (float)(i - kTimeRange);
             const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));  // as the per-voxel form rounds it
             const double e = (double)Y - (double)n * (double)beta;     // -inf stays -inf
@@ -212,25 +228,64 @@ __device__ __forceinline__ void accumulate_loaded(float2 (&acc)[NP], float ca, f
     }
 }
 
-// Table offset of x: floor(x), numpy's wrap of negative indices; an offset
-// past either end is flagged and replaced by 0 (its voxel then adds nothing).
-__device__ __forceinline__ int lookup_offset(float x, bool& ok, bool& tof_bad)
+// Table offset of x: floor(x) for |x| < 2^22 (a round-down add of 1.5 * 2^23
+// leaves it in the mantissa), with numpy's wrap of negative indices (:521,
+// :527).  The result may still lie outside 0..8000 (the reference's
+// IndexError); the caller compares it with its bound.
+__device__ __forceinline__ int table_offset(float x)
 {
-    int t = __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
-    t = t < 0 ? t + kTofEntries : t;
-    ok = (unsigned)t < (unsigned)kTofEntries;
-    tof_bad |= !ok;
-    return ok ? t : 0;
+    const int t = __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
+    return t < 0 ? t + kTofEntries : t;
+}
+
+// Per-bin weights w_b = 2^(Y - d (beta + gamma d)), d = n - b, each on the
+// SFU; ca * w_b is added to every bin.  Bins go two at a time through packed
+// FP32x2 instructions; with an odd bin count the last pair's second bin does
+// not exist.
+template <int NP, bool ODD>
+__device__ __forceinline__ void accumulate_per_bin(float2 (&acc)[NP], float ca, float Y, float n, float beta,
+                                                   const TofConst& T)
+{
+    const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
+    const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-T.gamma, -T.gamma);
+    const float2 two = make_float2(2.f, 2.f);
+    float2 nd = make_float2(-n, 1.f - n);  // b - n for the pair (b, b+1)
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
+        const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
+        const float wy = (ODD && k + 1 == NP) ? 0.f : ex2(e2.y);
+        acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), wy), acc[k]);
+        if (k + 1 < NP) nd = __fadd2_rn(nd, two);
+    }
+}
+
+// A voxel of the factored path whose table offset t is not below T.tsafe:
+// an offset far past the last bin takes the per-bin weights from its (Y, 0)
+// entry and its bin n; an offset outside the table is flagged and adds
+// nothing.  Runs only for such voxels.
+template <int NP, bool ODD>
+__device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, int t, const float2* sAR,
+                                          const unsigned char* sN, const TofConst& T, bool& tof_bad)
+{
+    if ((unsigned)t >= (unsigned)kTofEntries) {
+        tof_bad = true;
+        return;
+    }
+    const float n = (float)sN[t];
+    const float beta = T.kappa2w * ((float)(t - kTimeRange) - fmaf(n, T.w, T.s0));
+    accumulate_per_bin<NP, ODD>(acc, ca, sAR[t].x, n, beta, T);
 }
 
 // Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
-// reference's 8001-entry TOF table, :520-528).  w_b is rebuilt from the
+// reference's 8001-entry TOF table, :520-528), where the factored weights are
+// not used (one bin, or bins too wide for them).  w_b is rebuilt from the
 // largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
-// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b.  Bins go two
-// at a time through packed FP32x2 instructions; NP = number of bin pairs.
+// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b; NP = number of
+// bin pairs.
 template <int NP, bool SINGLE, bool ODD>
 __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
-                                                 const float2* sAR, const unsigned char* sN, const float* sG,
+                                                 const float2* sAR, const unsigned char* sN,
                                                  const TofConst& T, bool& tof_bad)
 {
     // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
@@ -246,10 +301,6 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
             return;
         }
     }
-    if (!SINGLE && T.factored) {
-        accumulate_loaded<NP>(acc, ca, sAR[t], __float_as_int(sAR[t].x) & T.nmask, sG);
-        return;
-    }
     const float Y = sAR[t].x;
     const float n = (float)sN[t];
     // beta = 2 kappa w (off - s_n), s_n = s0 + n w
@@ -257,19 +308,7 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
     if constexpr (SINGLE) {
         acc[0].x = fmaf(ca, ex2(fmaf(-n, fmaf(T.gamma, n, beta), Y)), acc[0].x);
     } else {
-        const float2 Y2 = make_float2(Y, Y), b2 = make_float2(beta, beta);
-        const float2 ca2 = make_float2(ca, ca), mg2 = make_float2(-T.gamma, -T.gamma);
-        const float2 two = make_float2(2.f, 2.f);
-        float2 nd = make_float2(-n, 1.f - n);  // b - n for the pair (b, b+1)
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-            const float2 t2 = __ffma2_rn(mg2, nd, b2);  // beta + gamma d
-            const float2 e2 = __ffma2_rn(nd, t2, Y2);   // Y - d (beta + gamma d)
-            // with an odd bin count the last pair's second bin does not exist
-            const float wy = (ODD && k + 1 == NP) ? 0.f : ex2(e2.y);
-            acc[k] = __ffma2_rn(ca2, make_float2(ex2(e2.x), wy), acc[k]);
-            if (k + 1 < NP) nd = __fadd2_rn(nd, two);
-        }
+        accumulate_per_bin<NP, ODD>(acc, ca, Y, n, beta, T);
     }
 }
 
@@ -285,7 +324,7 @@ template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int s_first, int s_count,
                                           int lw, int chunk, int lane, const float2* sAR,
                                           const unsigned char* sN, const float* sG, float2* vbuf, float2* kahan,
-                                          bool& tof_bad, bool& energy_bad,
+                                          bool& tof_bad, bool& energy_bad, bool& nonfinite,
                                           unsigned long long& walked, unsigned long long& npairs)
 {
     const float inv_c = (float)(1.0 / kLightCmPerPs);
@@ -389,20 +428,25 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                 if (c != 0.f) {
                     if (!SINGLE && T.factored) {
                         // the table lookup of voxel j+1 overlaps the accumulation of voxel j
-                        float2 v = vbuf[0];
-                        bool ok;
-                        int t = lookup_offset(fmaf(sigma, v.y, u), ok, tof_bad);
-                        float2 ar = sAR[t];
+                        // (offsets at or past T.tsafe, far past the last bin or outside the
+                        // table, go to far_voxel once, when they are looked up)
+                        const float2 v = vbuf[0];
+                        const int t = table_offset(fmaf(sigma, v.y, u));
+                        const bool ok = (unsigned)t < (unsigned)T.tsafe;
+                        if (!ok) far_voxel<NP, ODD>(acc, c * v.x, t, sAR, sN, T, tof_bad);
+                        float2 ar = sAR[ok ? t : 0];
                         int nb = __float_as_int(ar.x) & T.nmask;
                         float ca = ok ? c * v.x : 0.f;
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
-                            const float2 v1 = vbuf[j + 1 < jn ? j + 1 : j];
-                            bool ok1;
-                            const int t1 = lookup_offset(fmaf(sigma, v1.y, u), ok1, tof_bad);
-                            const float2 ar1 = sAR[t1];
+                            const bool more = j + 1 < jn;
+                            const float2 v1 = vbuf[more ? j + 1 : j];
+                            const int t1 = table_offset(fmaf(sigma, v1.y, u));
+                            const bool ok1 = (unsigned)t1 < (unsigned)T.tsafe;
+                            const float2 ar1 = sAR[ok1 ? t1 : 0];
                             const int nb1 = __float_as_int(ar1.x) & T.nmask;
                             accumulate_loaded<NP>(acc, ca, ar, nb, sG);
+                            if (!ok1 && more) far_voxel<NP, ODD>(acc, c * v1.x, t1, sAR, sN, T, tof_bad);
                             ar = ar1;
                             nb = nb1;
                             ca = ok1 ? c * v1.x : 0.f;
@@ -411,8 +455,8 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
                             const float2 v = vbuf[j];
-                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sAR, sN, sG,
-                                                              T, tof_bad);
+                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sAR, sN, T,
+                                                              tof_bad);
                         }
                     }
                 }
@@ -444,19 +488,27 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
         const float inv = 1.0f / cnt;
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
-            if (2 * k < C.nbins) atomicAdd(o + (2 * k) * plane, acc[k].x * inv);
-            if (2 * k + 1 < C.nbins) atomicAdd(o + (2 * k + 1) * plane, acc[k].y * inv);
+            const float vx = acc[k].x * inv, vy = acc[k].y * inv;
+            if (2 * k < C.nbins) {
+                nonfinite |= !isfinite(vx);
+                atomicAdd(o + (2 * k) * plane, vx);
+            }
+            if (2 * k + 1 < C.nbins) {
+                nonfinite |= !isfinite(vy);
+                atomicAdd(o + (2 * k + 1) * plane, vy);
+            }
         }
     }
 }
 
 // Block-end bookkeeping: error bits and the walked / evaluated counters.
-__device__ __forceinline__ void finish_pairs(int lane, bool tof_bad, bool energy_bad,
+__device__ __forceinline__ void finish_pairs(int lane, bool tof_bad, bool energy_bad, bool nonfinite,
                                              unsigned long long walked, unsigned long long npairs,
                                              int32_t* status, unsigned long long* work)
 {
     if (tof_bad) raise_error(status, kErrTofRange);
     if (energy_bad) raise_error(status, kErrEnergy);
+    if (nonfinite) raise_error(status, kErrNonFinite);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         walked += __shfl_xor_sync(0xffffffffu, walked, o);

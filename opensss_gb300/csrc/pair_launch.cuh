@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(pair_block_warps(NP, KAHAN) * 32, MINB) pair_k
     const int lane = threadIdx.x & 31;
     const long long per_slice = (long long)P.ctx.nl * P.nchunks;
     const long long ntasks = (long long)P.nslices * per_slice;
-    bool tof_bad = false, energy_bad = false;
+    bool tof_bad = false, energy_bad = false, nonfinite = false;
     unsigned long long walked = 0, npairs = 0;
     for (;;) {
         long long task = 0;
@@ -53,9 +53,9 @@ __global__ void __launch_bounds__(pair_block_warps(NP, KAHAN) * 32, MINB) pair_k
         const int rem = (int)(task % per_slice);
         walk_task<NP, SINGLE, ODD, KAHAN>(P.ctx, P.T, P.slice_first[slice], P.slice_count[slice],
                                           rem / P.nchunks, rem % P.nchunks, lane, sAR, sN, sG, vbuf, kahan,
-                                          tof_bad, energy_bad, walked, npairs);
+                                          tof_bad, energy_bad, nonfinite, walked, npairs);
     }
-    finish_pairs(lane, tof_bad, energy_bad, walked, npairs, P.status, P.work);
+    finish_pairs(lane, tof_bad, energy_bad, nonfinite, walked, npairs, P.status, P.work);
 }
 
 template <int NP, bool SINGLE, bool ODD, bool KAHAN>

@@ -223,6 +223,17 @@ def gen_sss(R, which):
                          W.make_problem("tiny-far", (12, 12, 6), 2.0, 3, 8, 5, 1.0, 60.0, seed=8,
                                         scanner=W.ring_scanner(48, 6, radius_cm=20.0, ring_pitch_cm=1.0,
                                                                phase=0.5), radius_cm=8.0)))
+    if "widebody" in which:
+        # a 50 cm wide body (radius 25 cm, 17 x 17 x 4 voxels of 3.1 cm) in the
+        # 41 cm ring at the benchmark's 13 bins of 3.9 cm and 214 ps: offsets
+        # reach ~1770 ps, past the last bin centre (1561 ps) by more than the
+        # factored weights take, but stay inside the +-4000 ps table (an odd
+        # grid keeps scatter points off the centre, where opposite crystals
+        # would make the reference's acos argument leave [-1, 1])
+        problems.append(("sss_wide_body_tof13",
+                         W.make_problem("wide-body-tof13", (17, 17, 4), 3.1, 2, 12, 13, 3.9, 214.0, seed=21,
+                                        scanner=W.ring_scanner(48, 4, radius_cm=41.0, ring_pitch_cm=1.0,
+                                                               phase=0.5), radius_cm=25.0)))
     if "edge" in which:
         # degenerate inputs: no scatter point (empty attenuation map, or a
         # sampling step past the volume), no activity, one sampled ring, and
@@ -664,7 +675,8 @@ def gen_support(R):
     _save("support", **out)
 
 
-ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_edge",
+ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_widebody",
+       "sss_edge",
        "sss_tof13_slice", "upsample", "upsample_lut",
        "mask", "fit", "span", "listmode", "prep", "support"]
 

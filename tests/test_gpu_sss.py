@@ -278,13 +278,15 @@ def test_tof_offsets_past_the_table_are_an_error(cuda_ok, att_table):
     assert e.value.code == 4
 
 
-@pytest.mark.xfail(strict=False, reason="known issue: factored TOF weights past s_last + (126 + log2 ca) / "
-                                        "((B-1) 2 kappa w) underflow (zero) or give NaN where r^2 overflows")
-def test_far_tof_offsets_match_reference(cuda_ok, att_table):
-    """5 bins of 1 cm with a 60 ps kernel: offsets run to ~575 ps, past the
-    factored weights' range (~346 ps); the reference's weights there sit on
-    the last bin."""
-    g = golden("sss_tiny_far")
+@pytest.mark.parametrize("name", ["sss_tiny_far", "sss_wide_body_tof13"])
+def test_far_tof_offsets_match_reference(cuda_ok, att_table, name):
+    """TOF offsets far past the last bin centre, where the pair kernel takes
+    per-bin weights instead of the factored chain: 5 bins of 1 cm with a
+    60 ps kernel (offsets to ~575 ps, factored range ~346 ps), and a 50 cm
+    wide body at 13 bins of 3.9 cm and 214 ps (offsets to ~1770 ps, split at
+    1675 ps).  The reference's weights there sit on the last bin.  The
+    engine's result is finite, its status clean, and it matches."""
+    g = golden(name)
     pr = problem_from_golden(g)
     got = _gpu_compact(pr, att_table)
     ref = g["compact"]

@@ -214,13 +214,14 @@ def test_factored_weights_match_table_within_their_range(nb, rng, res, ca):
     assert (np.abs(got - ref)[big] / ref[big]).max() < 3e-5
 
 
-@pytest.mark.xfail(strict=True, reason="known issue: past the last bin by more than 126 / ((B-1) 2 kappa w) ps "
-                                        "the table's A underflows in FP32 (weights 0, NaN where r^2 overflows)")
 @pytest.mark.parametrize("nb,rng,res", _FACTORED[:1])
-def test_factored_weights_match_table_everywhere(nb, rng, res):
+def test_factored_chain_alone_fails_far_past_the_last_bin(nb, rng, res):
+    """Why the kernel splits the table: run at every offset, the factored
+    chain's start ca * A underflows past its range (weights of about 1 become
+    0) and r^2 overflows further out (NaN)."""
     ref = T.tof_table(nb, rng, res)
     got = _factored_weights(nb, rng, res)
-    assert np.isfinite(got).all() and np.abs(got - ref).max() < 1e-5
+    assert not (np.isfinite(got).all() and np.abs(got - ref).max() < 1e-5)
 
 
 def _largest_tof_offset(pr):
@@ -253,23 +254,23 @@ def _largest_tof_offset(pr):
     return max(walk1.max(), walk2.max()) / _C
 
 
-def test_far_golden_reaches_past_the_factored_range(att_table):
-    """The far-offset fixture exercises the known issue: its offsets pass the
-    factored weights' range and the NaN region (beta >= 64) but stay inside
+@pytest.mark.parametrize("name", ["sss_tiny_far", "sss_wide_body_tof13"])
+def test_far_goldens_need_the_per_bin_split(att_table, name):
+    """The far-offset fixtures reach past the kernel's split offset: 5 bins
+    of 1 cm at 60 ps (into the factored chain's NaN region, beta >= 64) and a
+    50 cm wide body at the benchmark's 13 bins of 3.9 cm.  Both stay inside
     the reference's +-4000 ps table.  The FP64 oracle run with the kernel's
-    emulated factored weights instead of the exact table gives NaN cells,
-    and still differs with those terms dropped; with the exact table it
-    matches the reference."""
+    emulated weights (factored below the split, per-bin from it on) matches
+    the reference; on the 5-bin case the factored chain at every offset gives
+    NaN."""
     from conftest import golden, problem_from_golden, rel_l2
     from oracle import oracle as O
 
-    g = golden("sss_tiny_far")
+    g = golden(name)
     pr = problem_from_golden(g)
     top = _largest_tof_offset(pr)
-    limit = _valid_limit(pr.nr_bins, pr.tof_range, pr.tof_resolution)
-    w = 2 * pr.tof_range / pr.nr_bins
-    nan_from = (pr.nr_bins - 1) / 2 * w + 64 / (2 * (4 / pr.tof_resolution ** 2) * w)
-    assert limit < nan_from < top < 4000, (limit, nan_from, top)
+    nb, rng, res = pr.nr_bins, pr.tof_range, pr.tof_resolution
+    assert _kernel_split_offset(nb, rng, res) < _valid_limit(nb, rng, res, 2.0 ** -27) < top < 4000, top
 
     def run(tof=None):
         return O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry, pr.scanner.normals,
@@ -278,17 +279,20 @@ def test_far_golden_reaches_past_the_factored_range(att_table):
                              pr.tof_range, pr.nr_bins, tof=tof)
 
     assert rel_l2(run(), g["compact"]) < 1e-6
-    weights = _factored_weights(pr.nr_bins, pr.tof_range, pr.tof_resolution)
-    assert np.isnan(run(weights)).any()
-    # without the NaN terms, the zero weights past the range still show: 5e-2
-    assert rel_l2(run(np.nan_to_num(weights, nan=0.0)), g["compact"]) > 1e-2
+    kernel = run(_kernel_weights(nb, rng, res))
+    assert np.isfinite(kernel).all() and rel_l2(kernel, g["compact"]) < 1e-5
+    if name == "sss_tiny_far":
+        assert np.isnan(run(_factored_weights(nb, rng, res))).any()
 
 
-def _t_safe(nb, rng, res):
-    """Planned split point of the fix: past it, ca * A falls below 2^-126 for
-    ca < 2^-64 ((B-1) beta > 62), so those offsets take the per-bin path."""
+def _kernel_split_offset(nb, rng, res):
+    """First TOF offset (ps) whose weights the pair kernel takes per bin
+    instead of from the factored chain (tof_const's tsafe, less 4000): past
+    t_safe = s_{B-1} + 62 / ((B-1) 2 kappa w) the chain's start ca * A falls
+    below 2^-126 for voxel terms ca < 2^-64."""
     w = 2 * rng / nb
-    return (nb - 1) / 2.0 * w + 62.0 / ((nb - 1) * 2 * (4.0 / res ** 2) * w)
+    t_safe = (nb - 1) / 2.0 * w + 62.0 / ((nb - 1) * 2 * (4.0 / res ** 2) * w)
+    return min(np.floor(t_safe) + 1, 4001)
 
 
 def _per_bin_weights(nb, rng, res):
@@ -309,16 +313,23 @@ def _per_bin_weights(nb, rng, res):
     return out
 
 
-@pytest.mark.parametrize("nb,rng,res", _FACTORED + [(5, 5 * 1.0 / _C, 60.0), (2, 2 * 4.0 / _C, 214.0)])
-def test_planned_split_keeps_every_offset_exact(nb, rng, res):
-    """The fix planned for the far-offset issue: factored weights up to
-    t_safe, per-bin weights past it.  In float32 emulation that matches the
-    FP64 table at every offset, for voxel terms ca down to 2^-64."""
-    ref = T.tof_table(nb, rng, res)
+def _kernel_weights(nb, rng, res, ca=1.0):
+    """The pair kernel's weights in float32 emulation: the factored chain
+    below the split offset, per-bin 2^x from it on."""
     t = np.arange(-4000, 4001)
-    exact = _per_bin_weights(nb, rng, res)
+    far = (t >= _kernel_split_offset(nb, rng, res))[None, :]
+    return np.where(far, _per_bin_weights(nb, rng, res), _factored_weights(nb, rng, res, ca))
+
+
+@pytest.mark.parametrize("nb,rng,res", _FACTORED + [(5, 5 * 1.0 / _C, 60.0), (2, 2 * 4.0 / _C, 214.0),
+                                                    (7, 7 * 1.4 / _C, 100.0)])
+def test_kernel_weights_match_table_at_every_offset(nb, rng, res):
+    """Factored weights below the split, per-bin weights from it on: in
+    float32 emulation that matches the FP64 table at all 8001 offsets, with
+    no NaN, for voxel terms ca down to 2^-64."""
+    ref = T.tof_table(nb, rng, res)
     for ca in (1.0, 2.0 ** -27, 2.0 ** -64):
-        got = np.where((t <= _t_safe(nb, rng, res))[None, :], _factored_weights(nb, rng, res, ca), exact)
+        got = _kernel_weights(nb, rng, res, ca)
         assert np.isfinite(got).all()
         assert np.abs(got - ref).max() < 1e-5, ca
 
