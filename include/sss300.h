@@ -133,15 +133,18 @@ int sss_scatter_points(const sss_tof_problem *p, double *points, int64_t capacit
 
 /* No counterpart in the reference.  sss_scatter_points without any device
  * allocation, for callers that must not allocate: code running inside a
- * fixed memory arena or pool it does not own, under a runtime that forbids
- * allocation calls while it records or replays work, or in a process whose
- * device memory is capped.  Same arguments, results and errors as
- * sss_scatter_points; its scratch is a 32 KiB array inside the library that
- * every GPU loading the library holds until exit.  Limit: at most 4096
- * sampled z-slices (ceil(nz / sample_step[2])); larger problems get
- * SSS_ERR_INVALID.  The first call on each device looks up that array's
- * device address, so make it before any stream capture.  All calls share the
- * array: calls whose work overlaps on the GPU race, so serialise them. */
+ * fixed memory arena or pool it does not own, or in a process whose device
+ * memory is capped, where a late allocation could fail in mid-pipeline.
+ * Same arguments, results and errors as sss_scatter_points; like it, the call
+ * copies its counts to the host and synchronises `stream` before it returns.
+ * Its scratch is a 32 KiB array inside the library that every GPU loading
+ * the library holds until exit.  Limit: at most 4096 sampled z-slices
+ * (ceil(nz / sample_step[2])); larger problems get SSS_ERR_INVALID.  The
+ * first call on each device looks up that array's device address and keeps
+ * it, so make that first call before any stream capture on the device; a
+ * device reset (cudaDeviceReset) is not supported afterwards.  All calls
+ * share the array: calls whose work overlaps on the GPU race, so serialise
+ * them. */
 int sss_scatter_points_noalloc(const sss_tof_problem *p, double *points, int64_t capacity,
                                int64_t *count, int64_t *slice_counts, void *stream);
 
@@ -388,19 +391,6 @@ int sss_crop_downscale(const float *image, const int image_dims[3], const int cr
  * The workspace of that run must still be alive. */
 void sss_set_timing(int enable);
 int sss_get_timing(double out[6]);
-
-/* Measured rate of the SFU 2^x instruction on the current device, in 1e9
- * results/s (no reference counterpart: a throughput probe for the pair stage's
- * non-factored TOF weights, which take one 2^x per voxel and bin).
- * Synchronises `stream`. */
-int sss_probe_ex2_rate(double *gex2_per_s, void *stream);
-
-/* Measured shared-memory load bandwidth (conflict-free 16-byte loads on every
- * multiprocessor) and L2 load bandwidth (a 32 MB L2-resident buffer read with
- * L2-only loads) of the current device, in GB/s (no reference counterpart:
- * roofline denominators of the pair stage).  Synchronise `stream`. */
-int sss_probe_smem_rate(double *gb_per_s, void *stream);
-int sss_probe_l2_rate(double *gb_per_s, void *stream);
 
 #ifdef __cplusplus
 }

@@ -2,6 +2,8 @@
 
 Each translation unit is compiled in parallel with nvcc (one -gencode,
 ``compute_103a``/``sm_103a``), then linked into one shared library in-tree.
+The benchmark's throughput probes (``csrc/probe/probe.cu``) go into a library
+of their own, ``libsss300_probe.so``, which only ``bench.py`` loads.
 A rebuild happens only when a source or header is newer than the library.
 """
 
@@ -18,6 +20,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(PKG, "libsss300.so")
+PROBE_LIB = os.path.join(PKG, "libsss300_probe.so")
+PROBE_SRC = os.path.join(CSRC, "probe", "probe.cu")
 OBJ_DIR = os.path.join(PKG, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -42,10 +46,13 @@ def _deps():
 
 
 def needs_build() -> bool:
-    if not os.path.exists(LIB):
-        return True
-    t = os.path.getmtime(LIB)
-    return any(os.path.getmtime(f) > t for f in _deps())
+    for lib, deps in ((LIB, _deps()), (PROBE_LIB, _deps() + [PROBE_SRC])):
+        if not os.path.exists(lib):
+            return True
+        t = os.path.getmtime(lib)
+        if any(os.path.getmtime(f) > t for f in deps):
+            return True
+    return False
 
 
 def _compile(src: str, extra) -> str:
@@ -62,15 +69,16 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     if not force and not needs_build():
         return LIB
     os.makedirs(OBJ_DIR, exist_ok=True)
-    srcs = sources()
+    srcs = sources() + [PROBE_SRC]
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", *objs, "-o", tmp, "-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    for lib, lib_objs in ((LIB, objs[:-1]), (PROBE_LIB, objs[-1:])):
+        tmp = lib + ".tmp"
+        cmd = [nvcc(), *ARCH, "-shared", *lib_objs, "-o", tmp, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, lib)
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -115,9 +115,6 @@ SIGNATURES = {
     "sss_pair_warps_max": (C.c_int, [_I32, _I32]),
     "sss_set_timing": (None, [C.c_int]),
     "sss_get_timing": (C.c_int, [_P]),
-    "sss_probe_ex2_rate": (C.c_int, [C.POINTER(_D), _P]),
-    "sss_probe_smem_rate": (C.c_int, [C.POINTER(_D), _P]),
-    "sss_probe_l2_rate": (C.c_int, [C.POINTER(_D), _P]),
 }
 
 _lib = None

@@ -238,6 +238,16 @@ __device__ __forceinline__ int table_offset(float x)
     return t < 0 ? t + kTofEntries : t;
 }
 
+// table_offset for the factored path: an offset at or past tsafe (far past
+// the last bin, or outside the table) is noted in far and replaced by 0.
+__device__ __forceinline__ int lookup_offset(float x, int tsafe, bool& ok, bool& far)
+{
+    const int t = table_offset(x);
+    ok = (unsigned)t < (unsigned)tsafe;
+    far |= !ok;
+    return ok ? t : 0;
+}
+
 // Per-bin weights w_b = 2^(Y - d (beta + gamma d)), d = n - b, each on the
 // SFU; ca * w_b is added to every bin.  Bins go two at a time through packed
 // FP32x2 instructions; with an odd bin count the last pair's second bin does
@@ -429,27 +439,33 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                     if (!SINGLE && T.factored) {
                         // the table lookup of voxel j+1 overlaps the accumulation of voxel j
                         // (offsets at or past T.tsafe, far past the last bin or outside the
-                        // table, go to far_voxel once, when they are looked up)
-                        const float2 v = vbuf[0];
-                        const int t = table_offset(fmaf(sigma, v.y, u));
-                        const bool ok = (unsigned)t < (unsigned)T.tsafe;
-                        if (!ok) far_voxel<NP, ODD>(acc, c * v.x, t, sAR, sN, T, tof_bad);
-                        float2 ar = sAR[ok ? t : 0];
+                        // table, add nothing here; they are noted and taken afterwards)
+                        bool anyfar = false;
+                        float2 v = vbuf[0];
+                        bool ok;
+                        int t = lookup_offset(fmaf(sigma, v.y, u), T.tsafe, ok, anyfar);
+                        float2 ar = sAR[t];
                         int nb = __float_as_int(ar.x) & T.nmask;
                         float ca = ok ? c * v.x : 0.f;
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
-                            const bool more = j + 1 < jn;
-                            const float2 v1 = vbuf[more ? j + 1 : j];
-                            const int t1 = table_offset(fmaf(sigma, v1.y, u));
-                            const bool ok1 = (unsigned)t1 < (unsigned)T.tsafe;
-                            const float2 ar1 = sAR[ok1 ? t1 : 0];
+                            const float2 v1 = vbuf[j + 1 < jn ? j + 1 : j];
+                            bool ok1;
+                            const int t1 = lookup_offset(fmaf(sigma, v1.y, u), T.tsafe, ok1, anyfar);
+                            const float2 ar1 = sAR[t1];
                             const int nb1 = __float_as_int(ar1.x) & T.nmask;
                             accumulate_loaded<NP>(acc, ca, ar, nb, sG);
-                            if (!ok1 && more) far_voxel<NP, ODD>(acc, c * v1.x, t1, sAR, sN, T, tof_bad);
                             ar = ar1;
                             nb = nb1;
                             ca = ok1 ? c * v1.x : 0.f;
+                        }
+                        if (anyfar) {  // rare: per-bin weights for this batch's far voxels
+                            for (int j = 0; j < jn; ++j) {
+                                const float2 vf = vbuf[j];
+                                const int tf = table_offset(fmaf(sigma, vf.y, u));
+                                if ((unsigned)tf >= (unsigned)T.tsafe)
+                                    far_voxel<NP, ODD>(acc, c * vf.x, tf, sAR, sN, T, tof_bad);
+                            }
                         }
                     } else {
 #pragma unroll 2

@@ -3,6 +3,13 @@
 // (ex2.approx.ftz.f32), the shared-memory load bandwidth (the pair kernel
 // reads its TOF factors from shared memory) and the L2 load bandwidth (where
 // a TOF-table gather, as the reference does it, would read them from).
+//
+// Measurement only: built into its own library (libsss300_probe.so), which
+// the benchmark loads; the engine library does not contain these kernels.
+// Each entry point returns 0 or the failing cudaError_t, synchronises
+// `stream` and writes its rate (GB/s, or 1e9 results/s for 2^x).
+#include <cuda_runtime.h>
+
 #include "common.cuh"
 
 namespace {
@@ -72,54 +79,55 @@ __global__ void __launch_bounds__(256) l2_probe_kernel(const float4* __restrict_
 }
 
 // Times one launch of a probe between two events on st (after one warm-up
-// launch); returns 0 and the milliseconds, or an SSS error code.
+// launch); returns 0 and the milliseconds, or the failing cudaError_t.
 template <typename Launch>
-int time_probe(const char* what, cudaStream_t st, Launch launch, float* ms)
+int time_probe(cudaStream_t st, Launch launch, float* ms)
 {
     cudaEvent_t a, b;
-    if (cudaEventCreate(&a) != cudaSuccess) return sss_set_error(SSS_ERR_CUDA, "%s: event", what);
-    if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaError_t e = cudaEventCreate(&a);
+    if (e != cudaSuccess) return (int)e;
+    if ((e = cudaEventCreate(&b)) != cudaSuccess) {
         cudaEventDestroy(a);
-        return sss_set_error(SSS_ERR_CUDA, "%s: event", what);
+        return (int)e;
     }
     launch(true);
     cudaEventRecord(a, st);
     launch(false);
     cudaEventRecord(b, st);
-    int rc = sss_check_launch(what);
-    if (!rc && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(ms, a, b) != cudaSuccess))
-        rc = sss_set_error(SSS_ERR_CUDA, "%s: timing failed", what);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    return rc;
+    return (int)e;
 }
 
 }  // namespace
 
 extern "C" int sss_probe_smem_rate(double* gb_per_s, void* stream)
 {
-    if (!gb_per_s) return sss_set_error(SSS_ERR_INVALID, "sss_probe_smem_rate: null output");
+    if (!gb_per_s) return (int)cudaErrorInvalidValue;
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = sms * 4, threads = 256, iters = 4096;
     unsigned* sink = nullptr;
-    if (cudaMallocAsync(&sink, sizeof(unsigned), st) != cudaSuccess)
-        return sss_set_error(SSS_ERR_CUDA, "sss_probe_smem_rate: allocation failed");
+    cudaError_t e = cudaMallocAsync(&sink, sizeof(unsigned), st);
+    if (e != cudaSuccess) return (int)e;
     float ms = 0.f;
-    int rc = time_probe("smem_probe_kernel", st, [&](bool warm) {
+    int rc = time_probe(st, [&](bool warm) {
         smem_probe_kernel<<<blocks, threads, 0, st>>>(warm ? iters / 8 : iters, sink);
     }, &ms);
     cudaFreeAsync(sink, st);
     if (rc) return rc;
     *gb_per_s = (double)blocks * threads * iters * 8 * 16 / (ms * 1e-3) / 1e9;
-    return SSS_OK;
+    return 0;
 }
 
 extern "C" int sss_probe_l2_rate(double* gb_per_s, void* stream)
 {
-    if (!gb_per_s) return sss_set_error(SSS_ERR_INVALID, "sss_probe_l2_rate: null output");
+    if (!gb_per_s) return (int)cudaErrorInvalidValue;
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -128,47 +136,37 @@ extern "C" int sss_probe_l2_rate(double* gb_per_s, void* stream)
     const int blocks = sms * 8, threads = 256, reps = 256;
     float4* buf = nullptr;
     unsigned* sink = nullptr;
-    if (cudaMallocAsync(&buf, n4 * 16 + 256, st) != cudaSuccess)
-        return sss_set_error(SSS_ERR_CUDA, "sss_probe_l2_rate: allocation failed");
+    cudaError_t e = cudaMallocAsync(&buf, n4 * 16 + 256, st);
+    if (e != cudaSuccess) return (int)e;
     sink = reinterpret_cast<unsigned*>(buf + n4);
     cudaMemsetAsync(buf, 0, n4 * 16, st);
     float ms = 0.f;
-    int rc = time_probe("l2_probe_kernel", st, [&](bool warm) {
+    int rc = time_probe(st, [&](bool warm) {
         l2_probe_kernel<<<blocks, threads, 0, st>>>(buf, n4, warm ? 2 : reps, sink);
     }, &ms);
     cudaFreeAsync(buf, st);
     if (rc) return rc;
     *gb_per_s = (double)n4 * 16 * reps / (ms * 1e-3) / 1e9;
-    return SSS_OK;
+    return 0;
 }
 
 extern "C" int sss_probe_ex2_rate(double* gex2_per_s, void* stream)
 {
-    if (!gex2_per_s) return sss_set_error(SSS_ERR_INVALID, "sss_probe_ex2_rate: null output");
+    if (!gex2_per_s) return (int)cudaErrorInvalidValue;
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = sms * 8, threads = 256, iters = 4096;
     float* sink = nullptr;
-    if (cudaMallocAsync(&sink, sizeof(float), st) != cudaSuccess)
-        return sss_set_error(SSS_ERR_CUDA, "sss_probe_ex2_rate: allocation failed");
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    ex2_probe_kernel<<<blocks, threads, 0, st>>>(iters / 8, sink);  // warm-up
-    cudaEventRecord(a, st);
-    ex2_probe_kernel<<<blocks, threads, 0, st>>>(iters, sink);
-    cudaEventRecord(b, st);
-    int rc = sss_check_launch("ex2_probe_kernel");
+    cudaError_t e = cudaMallocAsync(&sink, sizeof(float), st);
+    if (e != cudaSuccess) return (int)e;
     float ms = 0.f;
-    if (!rc && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
-        rc = sss_set_error(SSS_ERR_CUDA, "sss_probe_ex2_rate: timing failed");
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    int rc = time_probe(st, [&](bool warm) {
+        ex2_probe_kernel<<<blocks, threads, 0, st>>>(warm ? iters / 8 : iters, sink);
+    }, &ms);
     cudaFreeAsync(sink, st);
     if (rc) return rc;
-    double n = (double)blocks * threads * iters * kChains;
-    *gex2_per_s = n / (ms * 1e-3) / 1e9;
-    return SSS_OK;
+    *gex2_per_s = (double)blocks * threads * iters * kChains / (ms * 1e-3) / 1e9;
+    return 0;
 }

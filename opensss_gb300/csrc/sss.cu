@@ -463,12 +463,12 @@ extern "C" int sss_tof_densify(const float* compact, int32_t nbins, int32_t nru,
 //
 // sss_scatter_points_noalloc: the same scatter-point enumeration as
 // sss_scatter_points for callers that must not allocate device memory —
-// code that runs inside a fixed memory arena or pool it does not own, under
-// a runtime that forbids allocation calls while it records or replays work,
-// or in a process whose memory is capped so that a late allocation could
-// fail mid-pipeline.  Its scratch (the running total and one counter per
-// sampled z-slice) lives in the file-scope array below instead of a
-// temporary buffer.
+// code that runs inside a fixed memory arena or pool it does not own, or in
+// a process whose memory is capped so that a late allocation could fail
+// mid-pipeline.  Its scratch (the running total and one counter per sampled
+// z-slice) lives in the file-scope array below instead of a temporary
+// buffer.  Like sss_scatter_points it copies the counts to the host and
+// synchronises the stream.
 namespace {
 
 // At most this many sampled z-slices (ceil(nz / sample_step_z)).
@@ -485,7 +485,9 @@ std::mutex g_noalloc_lock;
 unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
 // Device address of the scratch on the current device, looked up once per
-// device (host code cannot use the symbol's name as an address).
+// device (host code cannot use the symbol's name as an address) and kept: a
+// device reset after the first call would leave it stale, which the header
+// rules out.
 int noalloc_scratch(unsigned long long** out)
 {
     int dev = 0;

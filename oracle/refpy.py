@@ -1,8 +1,8 @@
 """Loader for the reference openSSS Python package (test infrastructure only).
 
 ORACLE — this module is test infrastructure, never part of the product.  It imports
-the unmodified reference modules from the reference checkout (default
-``/root/reference/Python``, override with ``OPENSSS_REFERENCE``) with a
+the unmodified reference modules from the reference checkout named by the
+``OPENSSS_REFERENCE`` environment variable (its ``Python`` folder) with a
 pass-through ``numba`` stub first on ``sys.path``.  It is used only by
 ``tests/golden/make_golden.py`` where the reference checkout exists, to produce
 the golden fixtures committed under ``tests/golden``; nothing at run time imports it.
@@ -12,17 +12,18 @@ import os
 import sys
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_PY = os.environ.get("OPENSSS_REFERENCE", "/root/reference/Python")
+REFERENCE_PY = os.environ.get("OPENSSS_REFERENCE", "")
 
 
 def available() -> bool:
-    return os.path.isdir(os.path.join(REFERENCE_PY, "openSSS"))
+    return bool(REFERENCE_PY) and os.path.isdir(os.path.join(REFERENCE_PY, "openSSS"))
 
 
 def load():
     """Import and return the reference modules as a namespace dict."""
     if not available():
-        raise RuntimeError(f"reference package not found at {REFERENCE_PY}")
+        raise RuntimeError("set OPENSSS_REFERENCE to the reference checkout's Python folder "
+                           f"(found: {REFERENCE_PY!r})")
     stub = os.path.join(_HERE, "numba_stub")
     for p in (stub, REFERENCE_PY):
         if p not in sys.path:
@@ -52,7 +53,8 @@ def load_utils():
     """Import the reference's Utils module with the recording skimage stand-in
     (oracle/skimage_stub) first on sys.path; returns (Utils, stub transform)."""
     if not available():
-        raise RuntimeError(f"reference package not found at {REFERENCE_PY}")
+        raise RuntimeError("set OPENSSS_REFERENCE to the reference checkout's Python folder "
+                           f"(found: {REFERENCE_PY!r})")
     stub = os.path.join(_HERE, "skimage_stub")
     if stub in sys.path:
         sys.path.remove(stub)

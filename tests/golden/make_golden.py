@@ -4,10 +4,10 @@ Runs the unmodified openSSS v1.0 Python modules (interpreted, through the
 pass-through numba stub in ``oracle/numba_stub``) and the reference's MEX ray
 tracers compiled from source (``oracle/_ref``), on seeded synthetic inputs,
 and stores inputs + outputs as compressed ``.npz`` fixtures.  It needs the
-reference checkout (``OPENSSS_REFERENCE``, default ``/root/reference/Python``)
+reference checkout, named by ``OPENSSS_REFERENCE`` (its ``Python`` folder),
 and is run by hand where that checkout exists:
 
-    python tests/golden/make_golden.py [--only name,...]
+    OPENSSS_REFERENCE=<checkout>/Python python tests/golden/make_golden.py [--only name,...]
 
 The fixtures are then used by the CPU tests (oracle pinning) and the GPU
 parity tests, which never need the reference checkout.

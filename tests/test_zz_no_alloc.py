@@ -1,11 +1,14 @@
 """sss_scatter_points_noalloc: the scatter-point step for callers that must
-not allocate device memory (a fixed arena they do not own, a runtime that
-forbids allocation while it records or replays work, a capped process).
+not allocate device memory (code inside a fixed arena it does not own, or a
+process whose device memory is capped).
 
 Checked through the C ABI against sss_scatter_points on two calls in a row:
 the second call must not see the first call's counts, because every call
-shares the library's scratch array and clears it first.  Kept in the last
-collected file so a run that stops at the first failure has run all else."""
+shares the library's scratch array and clears it first.  Around each call
+the device's free memory and the default stream-ordered pool's use (current
+and high-water mark) must not move: the call allocates nothing, not even
+briefly.  Kept in the last collected file so a run that stops at the first
+failure has run all else."""
 
 import ctypes as C
 
@@ -27,15 +30,53 @@ def _setup(pr, att):
     return eng, act, mu, eng.problem(act, mu, pr.grid, pr.image_size)
 
 
-def _call(fn, p, cap, lz, device):
+# cudaMemPoolAttr values of the CUDA runtime's public header (driver_types.h)
+_RESERVED_CURRENT, _USED_CURRENT, _USED_HIGH = 0x5, 0x7, 0x8
+
+
+class _DeviceMemory:
+    """Free device memory (cudaMemGetInfo) and the default pool's reserved,
+    used and peak-used bytes, read through the CUDA runtime the engine
+    library links (libcudart.so.13, already loaded with it)."""
+
+    def __init__(self, device_index):
+        self.rt = C.CDLL("libcudart.so.13")
+        self.pool = C.c_void_p()
+        assert self.rt.cudaDeviceGetDefaultMemPool(C.byref(self.pool), int(device_index)) == 0
+
+    def _attr(self, which):
+        v = C.c_uint64(0)
+        assert self.rt.cudaMemPoolGetAttribute(self.pool, which, C.byref(v)) == 0
+        return v.value
+
+    def reset_peak(self):
+        zero = C.c_uint64(0)
+        assert self.rt.cudaMemPoolSetAttribute(self.pool, _USED_HIGH, C.byref(zero)) == 0
+
+    def snapshot(self):
+        free, total = C.c_size_t(0), C.c_size_t(0)
+        assert self.rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+        return {"free": free.value, "reserved": self._attr(_RESERVED_CURRENT), "used": self._attr(_USED_CURRENT),
+                "peak": self._attr(_USED_HIGH)}
+
+
+def _call(fn, p, cap, lz, device, memory=None):
     import torch
 
     pts = torch.full((cap, 4), -7.0, dtype=torch.float64, device=device)
     count = C.c_int64(-1)
     slices = np.full(lz, -1, dtype=np.int64)
     st = torch.cuda.current_stream(device)
+    torch.cuda.synchronize(device)
+    if memory is not None:
+        memory.reset_peak()
+        before = memory.snapshot()
     rc = fn(C.byref(p), C.c_void_p(pts.data_ptr()), cap, C.byref(count),
             slices.ctypes.data_as(C.c_void_p), C.c_void_p(st.cuda_stream))
+    if memory is not None:
+        after = memory.snapshot()
+        assert after == before, (before, after)
+        assert after["peak"] == after["used"]
     return rc, pts.cpu().numpy(), count.value, slices
 
 
@@ -50,8 +91,9 @@ def test_noalloc_matches_allocating_entry_point(cuda_ok, att_table, which):
     cap = (-(-pr.grid[0] // int(pr.sample_step[0]))) * (-(-pr.grid[1] // int(pr.sample_step[1]))) * lz
     rc, ref_pts, ref_n, ref_sl = _call(L.sss_scatter_points, p, cap, lz, eng.device)
     assert rc == 0, _lib.last_error()
+    memory = _DeviceMemory(eng.device.index or 0)
     for _ in range(2):  # two calls in a row share the scratch array
-        rc, pts, n, sl = _call(L.sss_scatter_points_noalloc, p, cap, lz, eng.device)
+        rc, pts, n, sl = _call(L.sss_scatter_points_noalloc, p, cap, lz, eng.device, memory)
         assert rc == 0, _lib.last_error()
         assert n == ref_n
         assert np.array_equal(sl, ref_sl)
