@@ -138,13 +138,16 @@ class TofSSS:
     def run(self, ActivityMap, AttenuationMap, ImageSize, max_points: int | None = None,
             wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
             check: bool = True, kahan: bool = False, unit_tof: bool | None = None,
-            slice_range=None) -> torch.Tensor:
+            slice_range=None, points=None) -> torch.Tensor:
         """Sampled scatter sinogram, leg-pair layout [B, NL, NL] float32 (CUDA).
 
         ``max_points`` restricts the run to the first scatter points in
         lattice order (a partial last slice is normalised over its points,
-        like the oracle's bounded samples).  ``kahan`` sums each pair's
-        per-point terms with Kahan's compensated addition."""
+        like the oracle's bounded samples).  ``points`` (ascending scatter-point
+        numbers in lattice order) restricts it to those points, each z-slice
+        normalised over its kept points (the oracle's ``points`` sample).
+        ``kahan`` sums each pair's per-point terms with Kahan's compensated
+        addition."""
         dev = self.device
         shape = tuple(int(s) for s in ActivityMap.shape)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
@@ -152,12 +155,12 @@ class TofSSS:
             act = fortran_flat(ActivityMap, dev)
             mu = fortran_flat(AttenuationMap, dev)
             return self.run_flat(act, mu, shape, ImageSize, max_points, wave_points, out, st, check,
-                                 kahan, unit_tof, slice_range)
+                                 kahan, unit_tof, slice_range, points)
 
     def run_flat(self, act, mu, shape, ImageSize, max_points: int | None = None,
                  wave_points: int | None = None, out: torch.Tensor | None = None, stream=None,
                  check: bool = True, kahan: bool = False, unit_tof: bool | None = None,
-                 slice_range=None) -> torch.Tensor:
+                 slice_range=None, points=None) -> torch.Tensor:
         """``run`` on device-resident maps already flattened in Fortran order
         (float32, Nx*Ny*Nz).  ``slice_range`` = (a, b) keeps the sampled
         z-slices a..b-1 only (a shard: the slice terms add up, :201)."""
@@ -165,10 +168,10 @@ class TofSSS:
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         with torch.cuda.stream(st):  # buffers and the status reset belong to the launch stream
             return self._run_on(st, act, mu, shape, ImageSize, max_points, wave_points, out, check, kahan,
-                                unit_tof, slice_range)
+                                unit_tof, slice_range, points)
 
     def _run_on(self, st, act, mu, shape, ImageSize, max_points, wave_points, out, check, kahan, unit_tof,
-                slice_range) -> torch.Tensor:
+                slice_range, points=None) -> torch.Tensor:
         dev = self.device
         p = self.problem(act, mu, shape, ImageSize, kahan, unit_tof)
         pts, counts = self.scatter_points(p, st)
@@ -184,6 +187,8 @@ class TofSSS:
             keep = np.minimum(counts, np.maximum(0, max_points - np.concatenate([[0], np.cumsum(counts)[:-1]])))
             counts = keep
             pts = pts[: int(counts.sum())]
+        if points is not None:
+            pts, counts = select_points(pts, counts, points)
         n = int(counts.sum())
         if out is None:
             out = torch.empty((self.nbins, self.nl, self.nl), dtype=torch.float32, device=dev)
@@ -231,6 +236,18 @@ class TofSSS:
                                               _ptr(lor_t), _ptr(self.dets), _ptr(dense),
                                               C.c_void_p(st.cuda_stream)))
         return dense
+
+
+def select_points(pts: torch.Tensor, counts: np.ndarray, points):
+    """The scatter points numbered ``points`` (ascending, lattice order) out
+    of ``(pts, counts)`` from ``TofSSS.scatter_points``: their rows and the
+    per-slice counts of the kept points."""
+    idx = np.asarray(points, dtype=np.int64).reshape(-1)
+    if len(idx) and (idx[0] < 0 or idx[-1] >= len(pts) or np.any(np.diff(idx) <= 0)):
+        raise IndexError("points must be ascending scatter-point numbers below the point count")
+    slice_of = np.repeat(np.arange(len(counts)), counts)
+    kept = np.bincount(slice_of[idx], minlength=len(counts)).astype(np.int64)
+    return pts[torch.from_numpy(idx).to(pts.device)], kept
 
 
 def leg_pair_to_compact(lp: np.ndarray, nru: int, ndu: int) -> np.ndarray:

@@ -224,6 +224,15 @@ def uneven_instances(count: int = 64, seed: int = 0):
     return out
 
 
+def stratified_points(n_points: int, count: int) -> np.ndarray:
+    """``count`` scatter-point numbers spread evenly over ``0..n_points-1``
+    (lattice order, so every sampled z-slice contributes): a sample for
+    checks that a first-N cut would take from the lowest slices only."""
+    if count >= n_points:
+        return np.arange(n_points, dtype=np.int64)
+    return np.unique(np.floor(np.linspace(0, n_points - 1, count) + 0.5).astype(np.int64))
+
+
 def tiny_problem(nr_bins: int = 3, seed: int = 0, shape=(12, 12, 6), nd: int = 48, nr: int = 6,
                  nru: int = 3, ndu: int = 8, voxel_cm: float = 2.0) -> SSSProblem:
     """Small case the interpreted reference finishes in seconds."""

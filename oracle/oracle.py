@@ -154,11 +154,12 @@ class _SSSProblem(C.Structure):
         ("step", C.c_int64 * 3), ("nbins", C.c_int64),
         ("tof_table", C.c_void_p), ("eff", C.c_void_p), ("ratio", C.c_void_p),
         ("energy_ref", C.c_int64), ("sp_begin", C.c_int64), ("sp_end", C.c_int64),
+        ("sp_list", C.c_void_p), ("sp_count", C.c_int64),
     ]
 
 
 def _sss_struct(act, mu, image_size, geometry, normals, det_size, nru, ndu, step, tables,
-                sp_begin=0, sp_end=-1):
+                sp_begin=0, sp_end=-1, points=None):
     keep = []
 
     def hold(a, dt):
@@ -190,6 +191,9 @@ def _sss_struct(act, mu, image_size, geometry, normals, det_size, nru, ndu, step
     s.ratio = hold(tables["ratio"], np.float64).ctypes.data
     s.energy_ref = 511
     s.sp_begin, s.sp_end = sp_begin, sp_end
+    if points is not None:
+        lst = hold(np.asarray(points).reshape(-1), np.int64)
+        s.sp_list, s.sp_count = lst.ctypes.data, len(lst)
     return s, keep
 
 
@@ -206,10 +210,13 @@ def scatter_points(act, mu, image_size, step):
 
 def sss_compact(act, mu, image_size, geometry, normals, det_size, att_table, energy_resolution,
                 energy_threshold, nru, ndu, step, tof_resolution, tof_range, nbins,
-                sp_begin=0, sp_end=-1, nthreads=0, tof=None):
+                sp_begin=0, sp_end=-1, nthreads=0, tof=None, points=None):
     """FP64 SSS; returns compact [B, NRU*NRU, NDU, NDU] (pairs di1<=di2 filled).
     ``tof`` replaces the TOF table ([B, 8001], e.g. an emulation of another
-    evaluation of the weights)."""
+    evaluation of the weights).  ``points`` (ascending scatter-point numbers
+    in lattice order) restricts the sum to those points instead of the range
+    [sp_begin, sp_end); each z-slice is then normalised over its listed
+    points, as the engine does for the same subset."""
     tables = problem_tables(att_table, energy_threshold, energy_resolution, nbins, tof_range,
                             tof_resolution)
     if tof is not None:
@@ -217,7 +224,7 @@ def sss_compact(act, mu, image_size, geometry, normals, det_size, att_table, ene
             raise ValueError(f"tof table must be [{nbins}, {TOF_ENTRIES}], got {np.shape(tof)}")
         tables["tof"] = np.ascontiguousarray(tof, dtype=np.float64)
     s, keep = _sss_struct(act, mu, image_size, geometry, normals, det_size, nru, ndu, step,
-                          tables, sp_begin, sp_end)
+                          tables, sp_begin, sp_end, points)
     out = np.zeros((nbins, nru * nru, ndu, ndu))
     st = lib().orc_sss(C.byref(s), _p(out), C.c_int(nthreads))
     if st != 0:

@@ -207,6 +207,9 @@ typedef struct {
     const double *ratio;       /* [2000] water mu(E)/mu(511) */
     int64_t energy_ref;        /* 511 */
     int64_t sp_begin, sp_end;  /* scatter-point range in lattice order; end<0: all */
+    const int64_t *sp_list;    /* NULL, or sp_count ascending scatter-point numbers (lattice
+                                  order) to use instead of the range */
+    int64_t sp_count;
 } orc_sss_problem;
 
 typedef struct {
@@ -300,6 +303,18 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
     orc_scatter_points(p, sxyz, sz);
     int64_t sb = p->sp_begin < 0 ? 0 : p->sp_begin;
     int64_t se = (p->sp_end < 0 || p->sp_end > nsp) ? nsp : p->sp_end;
+    /* the points to use, in lattice order: a list, or the range [sb, se) */
+    int64_t nsel = p->sp_list ? p->sp_count : (se > sb ? se - sb : 0);
+    int64_t *sel = (int64_t *)malloc(sizeof(int64_t) * (nsel > 0 ? nsel : 1));
+    for (int64_t k = 0; k < nsel; ++k) {
+        sel[k] = p->sp_list ? p->sp_list[k] : sb + k;
+        if (sel[k] < 0 || sel[k] >= nsp || (k > 0 && sel[k] <= sel[k - 1])) {
+            free(sel);
+            free(sxyz);
+            free(sz);
+            return -5; /* the list must be ascending point numbers */
+        }
+    }
 
     /* TOF table transposed to [t][b] for locality */
     double *tof = (double *)malloc(sizeof(double) * ORC_TOF_ENTRIES * B);
@@ -319,12 +334,19 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
     const double ds = p->det_size[0] * p->det_size[1] * 1e-2;
     const double eff_ref = p->eff[p->energy_ref * 2 - 1];
 
-    int64_t s = sb;
-    while (s < se && status == 0) {
-        int64_t zcur = sz[s];
-        memset(slice_sum, 0, sizeof(double) * (size_t)ncell * B);
-        memset(slice_cnt, 0, sizeof(double) * (size_t)ncell);
-        for (; s < se && sz[s] == zcur && status == 0; ++s) {
+    int64_t k = 0;
+    while (k < nsel && status == 0) {
+        int64_t zcur = sz[sel[k]];
+        /* the slice accumulators are large (cells x bins): cleared in parallel */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (int64_t c = 0; c < ncell; ++c) {
+            slice_cnt[c] = 0;
+            for (int64_t b = 0; b < B; ++b) slice_sum[b * ncell + c] = 0;
+        }
+        for (; k < nsel && sz[sel[k]] == zcur && status == 0; ++k) {
+            const int64_t s = sel[k];
             const double xS = sxyz[3 * s], yS = sxyz[3 * s + 1], zS = sxyz[3 * s + 2];
             /* legs: SingleScatterSimulationTOF.py:400-430 */
 #ifdef _OPENMP
@@ -459,7 +481,11 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
                 free(ab2);
             }
         }
-        /* per-slice normalisation, NaN -> 0 (SingleScatterSimulationTOF.py:555-557) */
+        /* per-slice normalisation, NaN -> 0 (SingleScatterSimulationTOF.py:555-557);
+         * cells are independent */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
         for (int64_t c = 0; c < ncell; ++c) {
             double cn = slice_cnt[c];
             if (cn == 0) continue;
@@ -477,6 +503,7 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
     free(tof);
     free(sxyz);
     free(sz);
+    free(sel);
     return status;
 }
 

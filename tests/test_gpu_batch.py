@@ -71,6 +71,47 @@ def test_batch_matches_solo_runs(cuda_ok, att_table, workspace_mb):
     b.close()
 
 
+def test_uneven_batch_classes_against_fp64_oracle(cuda_ok, att_table):
+    """One problem of each TOF class (1, 13 and 33 bins) of the 64-instance
+    uneven batch, planned together: each problem's result over a stratified
+    sample of its scatter points (every sampled z-slice) against the FP64
+    oracle on the same points (1e-4, the engine's bar)."""
+    from opensss_gb300 import workloads as W
+    from opensss_gb300.batch import BatchSSS
+    from opensss_gb300.engine import fortran_flat, leg_pair_to_compact, select_points
+    from oracle import oracle as O
+
+    inst = W.uneven_instances(64, seed=0)
+    chosen = {}
+    for pr in inst:
+        work = int(np.prod(pr.grid)) * pr.nr_rings_used * pr.nr_detectors_used
+        if pr.nr_bins not in chosen or work < chosen[pr.nr_bins][0]:
+            chosen[pr.nr_bins] = (work, pr)
+    assert sorted(chosen) == [1, 13, 33]
+    probs = [chosen[b][1] for b in (1, 13, 33)]
+    engines = [_engine(pr, att_table) for pr in probs]
+    jobs, pts, idxs = [], [], []
+    for e, pr in zip(engines, probs):
+        act, mu = fortran_flat(pr.activity, e.device), fortran_flat(pr.attenuation, e.device)
+        p, c = e.scatter_points(e.problem(act, mu, pr.grid, pr.image_size))
+        idx = W.stratified_points(len(p), 24)
+        pts.append(select_points(p, c, idx))
+        idxs.append(idx)
+        jobs.append((e, act, mu, pr.image_size, pr.grid))
+    b = BatchSSS(jobs, points=pts)
+    outs = [o.cpu().numpy() for o in b.run()]
+    b.close()
+    for pr, got, idx in zip(probs, outs, idxs):
+        ref = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                            pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                            pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                            pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                            pr.nr_bins, points=idx)
+        cmp = leg_pair_to_compact(got, pr.nr_rings_used, pr.nr_detectors_used)
+        assert np.abs(ref).max() > 0
+        assert rel_l2(cmp, ref) < 1e-4, pr.name
+
+
 def test_batch_rerun_with_new_activity(cuda_ok, att_table):
     import torch
 

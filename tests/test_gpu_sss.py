@@ -111,14 +111,54 @@ def test_scatter_points_match_oracle(cuda_ok, att_table):
     assert np.array_equal(pts[:, 3].astype(np.int64), sl)
 
 
-@pytest.mark.parametrize("cfg,points", [("tof13_64x64x48", 160), ("tof33_128x128x96", 6)])
-def test_sss_large_problems_against_fp64_oracle(cuda_ok, att_table, cfg, points):
-    """Full benchmark geometry, bounded number of scatter points."""
+def test_tof13_whole_workload_against_fp64_oracle(cuda_ok, att_table):
+    """The 13-bin benchmark workload (64x64x48 @ 6 mm, 760 x 80 scanner,
+    16 x 48 sampled) over all 3,270 scatter points and 24 sampled z-slices:
+    every slice's normalisation (:555-557) and the sum over slices (:201)
+    enter, against the FP64 oracle on the host cores."""
     from opensss_gb300 import workloads as W
 
-    pr = getattr(W, cfg)()
-    got = _gpu_compact(pr, att_table, max_points=points)
-    ref = _oracle_compact(pr, att_table, sp_end=points)
+    pr = W.tof13_64x64x48()
+    got = _gpu_compact(pr, att_table)
+    ref = _oracle_compact(pr, att_table)
+    assert_same_support(got, ref)
+    assert rel_l2(got, ref) < TOL
+    np.testing.assert_allclose(got.astype(np.float64).sum(axis=(1, 2, 3)), ref.sum(axis=(1, 2, 3)), rtol=TOL)
+
+
+def test_tof33_stratified_sample_against_fp64_oracle(cuda_ok, att_table):
+    """The 33-bin precision workload (128x128x96 @ 4 mm, 32 x 96 sampled): 48
+    scatter points spread evenly over its 11,362 in lattice order (one or two
+    in most of its 48 sampled z-slices); engine and oracle run the same point
+    subset and normalise each slice over its kept points."""
+    from opensss_gb300 import workloads as W
+
+    pr = W.tof33_128x128x96()
+    xyz, _ = O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)
+    idx = W.stratified_points(len(xyz), 48)
+    got = _gpu_compact(pr, att_table, points=idx)
+    ref = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                        pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                        pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                        pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                        pr.nr_bins, points=idx)
+    assert_same_support(got, ref)
+    assert rel_l2(got, ref) < TOL
+
+
+def test_point_subset_matches_oracle_subset(cuda_ok, att_table):
+    """An uneven subset of points (some slices emptied, others thinned) is
+    normalised per slice over the kept points, on the GPU as in the oracle."""
+    g = golden("sss_tiny_b5")
+    pr = problem_from_golden(g)
+    xyz, sl = O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)
+    idx = np.array([i for i in range(len(xyz)) if (i % 3 != 1) and sl[i] != sl[len(xyz) // 2]])
+    got = _gpu_compact(pr, att_table, points=idx)
+    ref = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                        pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                        pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                        pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                        pr.nr_bins, points=idx)
     assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
 

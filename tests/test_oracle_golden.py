@@ -185,3 +185,20 @@ def test_oracle_sss_tof13_slice_matches_reference(att_table):
     assert int(np.count_nonzero(flat.any(axis=0))) == int(g["contributing"])
     assert rel_l2(got, ref) < SLICE_TOL
     np.testing.assert_allclose(flat.sum(axis=1), g["bin_totals"], rtol=SLICE_TOL)
+
+
+def test_oracle_point_list_matches_ranges(att_table):
+    """The oracle's explicit point list: all points equal the full run, the
+    first ten equal the range cut, and a list that is not ascending is an
+    error."""
+    g = golden("sss_tiny_b5")
+    pr = problem_from_golden(g)
+    args = (pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry, pr.scanner.normals,
+            pr.scanner.detector_size_mm, att_table, pr.energy_resolution, pr.energy_threshold,
+            pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+            pr.nr_bins)
+    n = len(O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)[0])
+    assert np.array_equal(O.sss_compact(*args, points=np.arange(n)), O.sss_compact(*args))
+    assert np.array_equal(O.sss_compact(*args, points=np.arange(10)), O.sss_compact(*args, sp_end=10))
+    with pytest.raises(RuntimeError, match="status -5"):
+        O.sss_compact(*args, points=np.array([3, 2]))
