@@ -127,8 +127,10 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def oracle_sample(pr, att, points, threads):
-    """FP64 C restatement of the reference on the first `points` scatter points."""
+def oracle_sample(pr, att, idx, threads):
+    """FP64 C restatement of the reference over the scatter points numbered
+    ``idx`` (ascending, lattice order; each z-slice normalised over its kept
+    points)."""
     from oracle import build_oracle
     from oracle import oracle as O
 
@@ -137,8 +139,18 @@ def oracle_sample(pr, att, points, threads):
     out = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
                         pr.scanner.normals, pr.scanner.detector_size_mm, att, pr.energy_resolution,
                         pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step,
-                        pr.tof_resolution, pr.tof_range, pr.nr_bins, sp_end=points, nthreads=threads)
+                        pr.tof_resolution, pr.tof_range, pr.nr_bins, points=idx, nthreads=threads)
     return out, time.perf_counter() - t0
+
+
+def stratified_sample(pr, count):
+    """``count`` scatter points spread evenly over the workload's points in
+    lattice order (every sampled z-slice contributes)."""
+    from opensss_gb300 import workloads as W
+    from oracle import oracle as O
+
+    n = len(O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)[0])
+    return W.stratified_points(n, count), n
 
 
 def run_reference(args, rank):
@@ -148,22 +160,23 @@ def run_reference(args, rank):
     att = _att_table()
     threads = cpu_threads()
     P = _pairs(pr.nr_rings_used, pr.nr_detectors_used)
-    points = args.ref_points
-    units = points * P * pr.nr_bins
+    idx, n_all = stratified_sample(pr, args.ref_points)
+    units = len(idx) * P * pr.nr_bins
     times = []
     for i in range(args.warmup + args.steps):
-        _, dt = oracle_sample(pr, att, points, threads)
+        _, dt = oracle_sample(pr, att, idx, threads)
         if i >= args.warmup:
             times.append(dt)
-    t = max(times) if times else float("nan")
+    t = statistics.mean(times) if times else float("nan")
     v = units / t
+    sample = (f"{len(idx)} of the workload's {n_all} scatter points, evenly spread in lattice order "
+              f"({units:.3e} units per step)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": _config(pr, {"sample_points": points}),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"first {points} scatter points of the workload "
-                                       f"({units:.3e} units per step)"},
+            "data": "synthetic", "config": _config(pr, {"sample_points": len(idx)}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "statistic": "mean over steps"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -240,7 +253,13 @@ def run_ours(args, rank, world, local_rank):
     total_s = max_over_ranks(sum(step_ms) / 1e3, dev)
     value = world * units * args.steps / total_s
 
-    # ---- end to end through the public API, host buffers, copies inside
+    # ---- end to end through the drop-in SingleScatterSimulationTOF: NumPy maps
+    # in, the reference's dense (B, ND+1, ND//2, NRU^2) float32 array out; the
+    # map uploads, the run, the densify and the device-to-host copy are timed
+    dropin = run_dropin(pr, att, dev, args)
+
+    # ---- end to end through the engine (TofSSS.run): pinned host volumes in,
+    # the compact leg-pair result copied back
     act_h = torch.from_numpy(np.ascontiguousarray(pr.activity)).pin_memory()
     mu_h = torch.from_numpy(np.ascontiguousarray(pr.attenuation)).pin_memory()
     res_h = torch.empty((pr.nr_bins, eng.nl, eng.nl), dtype=torch.float32).pin_memory()
@@ -256,9 +275,16 @@ def run_ours(args, rank, world, local_rank):
         if i >= args.warmup:
             e2e_s.append(time.perf_counter() - t0)
     e2e_total = max_over_ranks(sum(e2e_s), dev)
-    e2e_value = world * units * args.steps / e2e_total
-    h2d = act_h.numel() * 4 + mu_h.numel() * 4
-    d2h = res_h.numel() * 4
+    engine_e2e = {"value": world * units * args.steps / e2e_total, "unit": UNIT,
+                  "h2d_bytes_per_step": act_h.numel() * 4 + mu_h.numel() * 4,
+                  "d2h_bytes_per_step": res_h.numel() * 4,
+                  "path": "TofSSS.run on pinned host volumes, compact leg-pair result copied back"}
+    dropin_total = max_over_ranks(dropin["seconds"] * args.steps, dev)
+    e2e = {"value": world * units * args.steps / dropin_total, "unit": UNIT,
+           "h2d_bytes_per_step": dropin["h2d_bytes"], "d2h_bytes_per_step": dropin["d2h_bytes"],
+           "ms_per_step": dropin["seconds"] * 1e3,
+           "path": "opensss_gb300.SingleScatterSimulationTOF (the drop-in): NumPy maps in, the reference's "
+                   f"dense {dropin['shape']} float32 array out (pageable host memory in, page-locked out)"}
     L.sss_set_timing(0)
 
     if rank != 0:
@@ -272,12 +298,28 @@ def run_ours(args, rank, world, local_rank):
     alg_bytes = walked * (4 * pr.nr_bins + 8) if walked else None
     peaks = _probe_peaks()
     achieved = alg_bytes / pair_s / 1e9 if alg_bytes else None
+    # FP32 work of the weights: per term and bin one FMA into the bin's sum and
+    # one multiply of the running power (3 flops); SFU: 2^x of the two legs'
+    # attenuation terms per evaluated pair and scatter point
+    fp32_gflops = 3 * stage[4] / pair_s / 1e9 if stage[4] > 0 else None
+    sfu_g = 2 * stage[5] / pair_s / 1e9 if stage[5] > 0 else None
     roof = {"bound": "smem", "unit": "GB/s", "kernel": "pair_kernel", "achieved": achieved,
             "peak": peaks["smem"], "peak_source": "measured (sss_probe_smem_rate, this run)",
             "frac": achieved / peaks["smem"] if achieved and peaks["smem"] else None,
-            "traffic": _traffic(), "algorithmic_bytes_per_launch": alg_bytes,
+            "traffic": None,
+            "traffic_note": "DRAM bytes come from ncu only (profiles/pair_kernel_tof13_64x64x48.md); "
+                            "the TOF factors are read from shared memory, not DRAM",
+            "algorithmic_bytes_per_launch": alg_bytes,
             "bytes_rule": "(4 B x bins + 8 B) per (voxel, detector pair) term walked",
             "terms_per_launch": walked, "launch_ms": pair_s * 1e3,
+            "fp32_pipe": {"achieved_gflops": fp32_gflops, "peak_gflops": peaks["ffma"],
+                          "frac": fp32_gflops / peaks["ffma"] if fp32_gflops and peaks["ffma"] else None,
+                          "rule": "3 flops (FMA + power multiply) per (voxel, pair) term and bin",
+                          "peak_source": "measured (sss_probe_ffma_rate, FFMA2 chains, this run)"},
+            "sfu": {"achieved_g_per_s": sfu_g, "peak_g_per_s": peaks["ex2"],
+                    "frac": sfu_g / peaks["ex2"] if sfu_g and peaks["ex2"] else None,
+                    "rule": "two 2^x per evaluated (pair, scatter point)",
+                    "peak_source": "measured (sss_probe_ex2_rate, this run)"},
             "l2_reference_gather": {
                 "achieved": achieved, "peak": peaks["l2"], "unit": "GB/s",
                 "frac": achieved / peaks["l2"] if achieved and peaks["l2"] else None,
@@ -285,18 +327,23 @@ def run_ours(args, rank, world, local_rank):
                 "note": "same bytes against the L2 load bandwidth a TOF-table gather would be bound by"},
             "weights_per_s": stage[4] / pair_s if stage[4] > 0 else None}
 
-    # ---- CPU baseline (oracle port on the host cores) and error vs FP64 on the same sample
+    # ---- CPU baseline (oracle port on the host cores) and the error against
+    # FP64 on the same stratified sample of scatter points
     cpu = None
     err = None
     if world == 1 and not args.no_cpu:
         threads = cpu_threads()
-        ref, dt = oracle_sample(pr, att, args.ref_points, threads)
-        u = args.ref_points * P * pr.nr_bins
+        idx, n_all = stratified_sample(pr, args.ref_points)
+        ref, dt = oracle_sample(pr, att, idx, threads)
+        u = len(idx) * P * pr.nr_bins
         cpu = {"value": u / dt, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {args.ref_points} scatter points of the workload ({u:.3e} units)"}
-        sub = eng.run(act, mu, pr.image_size, max_points=args.ref_points).cpu().numpy()
+               "sample": f"{len(idx)} of the workload's {n_all} scatter points, evenly spread in lattice "
+                         f"order ({u:.3e} units)"}
+        sub = eng.run(act, mu, pr.image_size, points=idx).cpu().numpy()
         got = leg_pair_to_compact(sub, pr.nr_rings_used, pr.nr_detectors_used)
-        err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        err = {"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+               "max_bin": float(np.abs(got - ref).max() / np.abs(ref).max()),
+               "sample": cpu["sample"]}
 
     pipeline = None if args.no_pipeline else run_pipeline(eng, pr, out, dev, args)
     batch = None if args.no_batch or world > 1 else run_batch(dev, args, att)
@@ -312,17 +359,50 @@ def run_ours(args, rank, world, local_rank):
             "data": "synthetic", "config": _config(pr, {"scatter_points": nsp,
                                                         "detector_pairs": P,
                                                         "units_per_step": units}),
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h,
-                    "path": "TofSSS.run on pinned host volumes, compact result copied back"},
+            "e2e": e2e, "e2e_engine": engine_e2e, "dropin": dropin,
             "gpu_launches": launches, "clocks": clocks, "roofline": roof,
             "launch_shape": {"pair_warps": eng.pair_warps, "leg_threads": eng.leg_threads,
                              "tuned": tuned},
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
-            "rel_l2_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
+            "error_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
             "batch": batch, "precision": precision, "serving": serving, "listmode": listmode,
             "image_prep": prep}
     print(json.dumps(line), flush=True)
+
+
+def run_dropin(pr, att, dev, args):
+    """The drop-in call a reference script makes, timed on the host clock:
+    ``SingleScatterSimulationTOF`` with NumPy maps and the LOR table, the
+    dense float32 result returned.  Warm-up calls build and cache the engine
+    and page-locked output memory; each timed call drops its result before
+    the next."""
+    import contextlib
+    import io
+
+    import torch
+
+    from opensss_gb300 import SingleScatterSimulationTOF, geometry as G
+
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, pr.scanner.nr_detectors, pr.scanner.nr_rings, ID_Shidt=False)
+    args_ = (pr.image_size, pr.scanner.geometry, lor, pr.scanner.normals, pr.scanner.detector_size_mm, att,
+             pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step,
+             pr.tof_resolution, pr.tof_range, pr.nr_bins, None)
+    act = np.ascontiguousarray(pr.activity)
+    mu = np.ascontiguousarray(pr.attenuation)
+    times, shape = [], None
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize(dev)
+        with contextlib.redirect_stdout(io.StringIO()):  # the reference's timing print
+            t0 = time.perf_counter()
+            dense = SingleScatterSimulationTOF(act, mu, *args_, device=dev)
+            t1 = time.perf_counter()
+        shape = list(dense.shape)
+        nbytes = dense.nbytes
+        del dense
+        if i >= args.warmup:
+            times.append(t1 - t0)
+    return {"seconds": statistics.mean(times), "shape": shape, "h2d_bytes": act.nbytes + mu.nbytes,
+            "d2h_bytes": nbytes, "ms_min": min(times) * 1e3, "ms_max": max(times) * 1e3}
 
 
 def run_pipeline(eng, pr, sampled, dev, args):
@@ -526,9 +606,11 @@ def run_precision(dev, args, att):
     """The precision-stress instance: 128x128x96 @ 4 mm, 32 rings x 96
     crystals, 33 TOF bins of 15 mm.  Full-size throughput with the plain and
     the Kahan-compensated scatter-point reduction, then both against the FP64
-    oracle on the first ``--precision-points`` scatter points: relative L2,
+    oracle on a sample of scatter points: relative L2,
     largest bin error (over the largest reference bin) and the fitted scale
-    of the centre TOF bin (prompts drawn from the FP64 scatter)."""
+    of the centre TOF bin (prompts drawn from the FP64 scatter).  The sample
+    is ``--precision-points`` scatter points spread evenly over the workload
+    in lattice order."""
     import torch
 
     from opensss_gb300 import TofSSS, geometry as G, workloads as W
@@ -566,11 +648,12 @@ def run_precision(dev, args, att):
             full[key] = {"ms_per_step": statistics.mean(ms), "value": units / (statistics.mean(ms) / 1e3),
                          "steps": args.precision_steps, "warmup": args.precision_warmup}
     eng._ws = None
-    # errors on a bounded sample against the FP64 oracle
-    n = args.precision_points
-    ref, _ = oracle_sample(pr, att, n, cpu_threads())
+    # errors on a stratified sample (every sampled z-slice) against the FP64 oracle
+    idx, n_all = stratified_sample(pr, args.precision_points)
+    n = len(idx)
+    ref, _ = oracle_sample(pr, att, idx, cpu_threads())
     nru, ndu = pr.nr_rings_used, pr.nr_detectors_used
-    outs = {k: eng.run_flat(act, mu, pr.grid, pr.image_size, max_points=n, kahan=(k == "kahan"))
+    outs = {k: eng.run_flat(act, mu, pr.grid, pr.image_size, points=idx, kahan=(k == "kahan"))
             for k in ("plain", "kahan")}
     err = {}
     for k, o in outs.items():
@@ -612,7 +695,8 @@ def run_precision(dev, args, att):
             "tof_bins": pr.nr_bins, "scatter_points": nsp, "units_per_step": units, "full": full,
             "clocks": clk.summary(),
             "error_vs_fp64_oracle": err, "fp64_fitted_scale": s_ref, "fit_bin": b,
-            "sample": f"first {n} scatter points ({n * _pairs(nru, ndu) * pr.nr_bins:.3e} units)",
+            "sample": f"{n} of {n_all} scatter points, evenly spread in lattice order "
+                      f"({n * _pairs(nru, ndu) * pr.nr_bins:.3e} units)",
             "fp64_oracle": "oracle/sss_oracle.c (FP64 C restatement), host cores"}
 
 
@@ -791,9 +875,10 @@ def run_listmode(dev, args):
 
 
 def _probe_peaks():
-    """Shared-memory and L2 load bandwidth (GB/s) measured on this device by
-    the probe kernels of libsss300_probe.so (built beside the engine, loaded
-    only here); None where a probe fails."""
+    """Roofline denominators measured on this device by the probe kernels of
+    libsss300_probe.so (built beside the engine, loaded only here): shared
+    memory and L2 load bandwidth (GB/s), FFMA2 rate (GFLOP/s) and 2^x rate
+    (1e9/s); None where a probe fails."""
     import torch
 
     from opensss_gb300 import _build
@@ -801,23 +886,13 @@ def _probe_peaks():
     probe = C.CDLL(_build.PROBE_LIB)
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     out = {}
-    for key, fn in (("smem", "sss_probe_smem_rate"), ("l2", "sss_probe_l2_rate")):
+    for key, fn in (("smem", "sss_probe_smem_rate"), ("l2", "sss_probe_l2_rate"),
+                    ("ffma", "sss_probe_ffma_rate"), ("ex2", "sss_probe_ex2_rate")):
         f = getattr(probe, fn)
         f.restype, f.argtypes = C.c_int, [C.POINTER(C.c_double), C.c_void_p]
         v = C.c_double(0.0)
         out[key] = v.value if f(C.byref(v), st) == 0 and v.value > 0 else None
     return out
-
-
-def _traffic():
-    path = os.path.join(ROOT, "profiles", "pair_kernel_tof13_64x64x48.md")
-    try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_launch:"):
-                return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
 
 
 # ---------------------------------------------------------------- profiler cases

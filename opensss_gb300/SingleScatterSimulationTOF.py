@@ -9,25 +9,89 @@ the GPU through ``libsss300.so``; there is no CPU path.
 
 from __future__ import annotations
 
+import collections
+import hashlib
 import os
+import threading
 import time
 
 import numpy as np
+import torch
 
-from .engine import TofSSS
+from . import geometry
+from .engine import TofSSS, as_device
+
+# Engines of recent calls.  An outer reconstruction loop calls the SSS once
+# per iteration with the same scanner, tables and sampling and a new activity
+# map; the engine (device tables, launch state) and the reference-layout
+# device buffer are kept for such calls, keyed by a SHA-1 of every input but
+# the two maps.
+_CACHE_SIZE = 2
+_cache: "collections.OrderedDict[bytes, _DropIn]" = collections.OrderedDict()
+_lock = threading.Lock()
+
+
+class _DropIn:
+    def __init__(self, eng: TofSSS, lor):
+        self.engine = eng
+        lor = geometry.check_dense_lor(lor, eng.dets_np, eng.nd)
+        self.lor = as_device(np.asarray(lor, dtype=np.int16), torch.int16, eng.device)
+        # the reference layout; cells of unsampled pairs stay 0 across calls
+        self.dense = torch.zeros((eng.nbins, eng.nd + 1, eng.nd // 2, eng.nru * eng.nru),
+                                 dtype=torch.float32, device=eng.device)
+
+
+def _key(arrays, scalars, device) -> bytes:
+    h = hashlib.sha1(usedforsecurity=False)
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(f"{a.dtype.str}{a.shape}".encode())
+        h.update(a.reshape(-1).view(np.uint8))
+    h.update(repr((scalars, str(device))).encode())
+    return h.digest()
+
+
+def _drop_in(Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable, EnergyResolution,
+             EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution, TOFRange, NrBins,
+             device) -> _DropIn:
+    key = _key([Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable, SampleStep],
+               (float(EnergyResolution), float(EnergyThreshold), int(NrRingsUsed), int(NrDetectorsUsed),
+                float(TOFResolution), float(TOFRange), int(NrBins)), device)
+    with _lock:
+        d = _cache.get(key)
+        if d is not None:
+            _cache.move_to_end(key)
+            return d
+    eng = TofSSS(Geometry, NormalVectors, DetectorSize, AttenuationTable, EnergyResolution, EnergyThreshold,
+                 NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution, TOFRange, NrBins, device=device)
+    d = _DropIn(eng, SinogramCoordinates)
+    with _lock:
+        _cache[key] = d
+        while len(_cache) > _CACHE_SIZE:
+            _cache.popitem(last=False)
+    return d
 
 
 def SingleScatterSimulationTOF(ActivityMap, AttenuationMap, ImageSize, Geometry, SinogramCoordinates,
                                NormalVectors, DetectorSize, AttenuationTable, EnergyResolution,
                                EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution,
                                TOFRange, NrBins, SavePath, device="cuda"):
-    """3D TOF single scatter simulation (Watson); see the module docstring."""
+    """3D TOF single scatter simulation (Watson); see the module docstring.
+
+    The result is a fresh float32 array the caller owns.  Its memory is
+    page-locked host memory from torch's pinned-memory cache, so that the
+    device-to-host copy runs at the link's full rate; it returns to the
+    cache when the array is dropped."""
     t0 = time.time()
-    eng = TofSSS(Geometry, NormalVectors, DetectorSize, AttenuationTable, EnergyResolution,
-                 EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution, TOFRange,
-                 NrBins, device=device)
+    d = _drop_in(Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable,
+                 EnergyResolution, EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution,
+                 TOFRange, NrBins, device)
+    eng = d.engine
     compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
-    dense = eng.densify(compact, SinogramCoordinates).cpu().numpy()
+    eng.densify(compact, d.lor, out=d.dense)
+    host = torch.empty(tuple(d.dense.shape), dtype=torch.float32, pin_memory=True)
+    host.copy_(d.dense)
+    dense = host.numpy()
     print("Time for SSS: {:.2f} seconds".format(time.time() - t0))
     if SavePath:
         np.savez_compressed(os.path.join(SavePath, "Scatters_SSS.npz"), dense)

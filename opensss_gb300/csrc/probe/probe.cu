@@ -7,7 +7,8 @@
 // Measurement only: built into its own library (libsss300_probe.so), which
 // the benchmark loads; the engine library does not contain these kernels.
 // Each entry point returns 0 or the failing cudaError_t, synchronises
-// `stream` and writes its rate (GB/s, or 1e9 results/s for 2^x).
+// `stream` and writes its rate (GB/s, 1e9 results/s for 2^x, GFLOP/s for
+// FFMA2).
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -28,6 +29,24 @@ __global__ void __launch_bounds__(256) ex2_probe_kernel(int iters, float* sink)
     float s = 0.f;
 #pragma unroll
     for (int c = 0; c < kChains; ++c) s += x[c];
+    if (s == 123.456f) sink[0] = s;  // keeps the chains alive
+}
+
+// FP32 FMA pipe: independent chains of packed FFMA2 (two FMAs per lane and
+// instruction, the form the pair kernel's bin loop issues).
+__global__ void __launch_bounds__(256) ffma2_probe_kernel(int iters, float* sink)
+{
+    float2 x[kChains];
+    const float2 a = make_float2(0.999f, 0.998f), b = make_float2(1e-3f, 2e-3f);
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) x[c] = make_float2(0.1f * (threadIdx.x & 7) + 0.01f * c, 0.5f);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kChains; ++c) x[c] = __ffma2_rn(x[c], a, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) s += x[c].x + x[c].y;
     if (s == 123.456f) sink[0] = s;  // keeps the chains alive
 }
 
@@ -168,5 +187,27 @@ extern "C" int sss_probe_ex2_rate(double* gex2_per_s, void* stream)
     cudaFreeAsync(sink, st);
     if (rc) return rc;
     *gex2_per_s = (double)blocks * threads * iters * kChains / (ms * 1e-3) / 1e9;
+    return 0;
+}
+
+extern "C" int sss_probe_ffma_rate(double* gflop_per_s, void* stream)
+{
+    if (!gflop_per_s) return (int)cudaErrorInvalidValue;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 8192;
+    float* sink = nullptr;
+    cudaError_t e = cudaMallocAsync(&sink, sizeof(float), st);
+    if (e != cudaSuccess) return (int)e;
+    float ms = 0.f;
+    int rc = time_probe(st, [&](bool warm) {
+        ffma2_probe_kernel<<<blocks, threads, 0, st>>>(warm ? iters / 8 : iters, sink);
+    }, &ms);
+    cudaFreeAsync(sink, st);
+    if (rc) return rc;
+    // two FMAs (four flops) per FFMA2
+    *gflop_per_s = (double)blocks * threads * iters * kChains * 4 / (ms * 1e-3) / 1e9;
     return 0;
 }

@@ -224,13 +224,23 @@ class TofSSS:
         return self._ws
 
     # ------------------------------------------------------------------
-    def densify(self, compact: torch.Tensor, lor) -> torch.Tensor:
-        """Leg-pair layout -> reference layout [B, ND+1, ND//2, NRU^2] (CUDA)."""
+    def densify(self, compact: torch.Tensor, lor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Leg-pair layout -> reference layout [B, ND+1, ND//2, NRU^2] (CUDA).
+
+        ``lor`` is the LORCoordinates table (checked here), or a CUDA int16
+        copy of a table checked before.  ``out``: a dense buffer that this
+        engine densified into before with the same table (or zeros): only
+        the sampled pairs' cells are written, the others stay as they are."""
         dev = self.device
-        lor = geometry.check_dense_lor(lor, self.dets_np, self.nd)
-        lor_t = as_device(np.asarray(lor, dtype=np.int16), torch.int16, dev)
-        dense = torch.zeros((self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru),
-                            dtype=torch.float32, device=dev)
+        if isinstance(lor, torch.Tensor) and lor.is_cuda:
+            lor_t = lor
+        else:
+            lor = geometry.check_dense_lor(lor, self.dets_np, self.nd)
+            lor_t = as_device(np.asarray(lor, dtype=np.int16), torch.int16, dev)
+        shape = (self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru)
+        if out is not None and (tuple(out.shape) != shape or out.dtype != torch.float32 or out.device != dev):
+            raise ValueError(f"densify: out must be float32 {shape} on {dev}")
+        dense = out if out is not None else torch.zeros(shape, dtype=torch.float32, device=dev)
         st = torch.cuda.current_stream(dev)
         _lib.check(_lib.lib().sss_tof_densify(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd,
                                               _ptr(lor_t), _ptr(self.dets), _ptr(dense),

@@ -34,7 +34,8 @@ def test_reference_arm_prints_one_contract_line():
     assert line["config"]["workload"] == "tof13-64x64x48"
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
-    assert cb["unit"] == line["unit"] and "2 scatter points" in cb["sample"]
+    assert cb["unit"] == line["unit"] and cb["sample"].startswith("2 of the workload's 3270 scatter points")
+    assert cb["statistic"] == "mean over steps"
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

@@ -211,6 +211,18 @@ def test_dropin_dense_output(cuda_ok, att_table, tmp_path):
     assert_same_support(out, ref)
     assert rel_l2(out, ref) < TOL
     assert (tmp_path / "Scatters_SSS.npz").exists()
+    # a second call (the cached engine and device buffer) with twice the
+    # activity: a fresh array, twice the first (the SSS is linear in the
+    # activity), and the first result left as it was
+    first = out.copy()
+    out2 = SingleScatterSimulationTOF(2 * pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry,
+                                      lor, pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+                                      pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used,
+                                      pr.nr_detectors_used, pr.sample_step, pr.tof_resolution,
+                                      pr.tof_range, pr.nr_bins, None)
+    assert out2 is not out and not np.shares_memory(out2, out)
+    assert np.array_equal(out, first)
+    assert rel_l2(out2, 2 * first) < 1e-6
 
 
 def test_tof_bins_sum_to_nontof(cuda_ok, att_table):
