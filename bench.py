@@ -364,6 +364,9 @@ def run_ours(args, rank, world, local_rank):
             "launch_shape": {"pair_warps": eng.pair_warps, "leg_threads": eng.leg_threads,
                              "tuned": tuned},
             "stages_ms": {"legs": statistics.mean(leg_ms), "pairs": statistics.mean(pair_ms)},
+            "device_rates": {"fp64_add_g_per_s": peaks["dadd"], "ffma2_gflops": peaks["ffma"],
+                             "ex2_g_per_s": peaks["ex2"], "smem_gbs": peaks["smem"], "l2_gbs": peaks["l2"],
+                             "source": "probe kernels of libsss300_probe.so, this run"},
             "error_vs_fp64_oracle": err, "cpu_baseline": cpu, "pipeline": pipeline,
             "batch": batch, "precision": precision, "serving": serving, "listmode": listmode,
             "image_prep": prep}
@@ -877,8 +880,8 @@ def run_listmode(dev, args):
 def _probe_peaks():
     """Roofline denominators measured on this device by the probe kernels of
     libsss300_probe.so (built beside the engine, loaded only here): shared
-    memory and L2 load bandwidth (GB/s), FFMA2 rate (GFLOP/s) and 2^x rate
-    (1e9/s); None where a probe fails."""
+    memory and L2 load bandwidth (GB/s), FFMA2 rate (GFLOP/s), 2^x and FP64
+    add rates (1e9/s); None where a probe fails."""
     import torch
 
     from opensss_gb300 import _build
@@ -887,7 +890,8 @@ def _probe_peaks():
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     out = {}
     for key, fn in (("smem", "sss_probe_smem_rate"), ("l2", "sss_probe_l2_rate"),
-                    ("ffma", "sss_probe_ffma_rate"), ("ex2", "sss_probe_ex2_rate")):
+                    ("ffma", "sss_probe_ffma_rate"), ("ex2", "sss_probe_ex2_rate"),
+                    ("dadd", "sss_probe_dadd_rate")):
         f = getattr(probe, fn)
         f.restype, f.argtypes = C.c_int, [C.POINTER(C.c_double), C.c_void_p]
         v = C.c_double(0.0)

@@ -7,8 +7,8 @@
 // Measurement only: built into its own library (libsss300_probe.so), which
 // the benchmark loads; the engine library does not contain these kernels.
 // Each entry point returns 0 or the failing cudaError_t, synchronises
-// `stream` and writes its rate (GB/s, 1e9 results/s for 2^x, GFLOP/s for
-// FFMA2).
+// `stream` and writes its rate (GB/s, 1e9 results/s for 2^x and DADD,
+// GFLOP/s for FFMA2).
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -48,6 +48,23 @@ __global__ void __launch_bounds__(256) ffma2_probe_kernel(int iters, float* sink
 #pragma unroll
     for (int c = 0; c < kChains; ++c) s += x[c].x + x[c].y;
     if (s == 123.456f) sink[0] = s;  // keeps the chains alive
+}
+
+// FP64 adds: independent chains of DADD (the ray walk's step before it moved
+// to the integer pipe).
+__global__ void __launch_bounds__(256) dadd_probe_kernel(int iters, double* sink)
+{
+    double x[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) x[c] = 0.1 * (threadIdx.x & 7) + 0.01 * c;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kChains; ++c) x[c] = __dadd_rn(x[c], 1e-3);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) s += x[c];
+    if (s == 123.456) sink[0] = s;
 }
 
 // Shared-memory loads: every warp reads 512 contiguous bytes per LDS.128
@@ -209,5 +226,26 @@ extern "C" int sss_probe_ffma_rate(double* gflop_per_s, void* stream)
     if (rc) return rc;
     // two FMAs (four flops) per FFMA2
     *gflop_per_s = (double)blocks * threads * iters * kChains * 4 / (ms * 1e-3) / 1e9;
+    return 0;
+}
+
+extern "C" int sss_probe_dadd_rate(double* gadd_per_s, void* stream)
+{
+    if (!gadd_per_s) return (int)cudaErrorInvalidValue;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 1024;
+    double* sink = nullptr;
+    cudaError_t e = cudaMallocAsync(&sink, sizeof(double), st);
+    if (e != cudaSuccess) return (int)e;
+    float ms = 0.f;
+    int rc = time_probe(st, [&](bool warm) {
+        dadd_probe_kernel<<<blocks, threads, 0, st>>>(warm ? iters / 8 : iters, sink);
+    }, &ms);
+    cudaFreeAsync(sink, st);
+    if (rc) return rc;
+    *gadd_per_s = (double)blocks * threads * iters * kChains / (ms * 1e-3) / 1e9;
     return 0;
 }

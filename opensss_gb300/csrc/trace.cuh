@@ -158,33 +158,107 @@ __device__ __forceinline__ int64_t sub2ind(const Grid& g, int X, int Y, int Z)
     return (int64_t)X + (int64_t)(Y - 1) * g.ny + (int64_t)(Z - 1) * g.ny * g.nx;
 }
 
+// IEEE-754 binary64 addition, round to nearest even, of two non-negative
+// finite values given as bit patterns, with integer operations only (on this
+// GPU the FP64 pipe issues a small fraction of the integer rate).  Written
+// from the format's definition: the larger operand's significand (hidden bit
+// restored, 10 guard bits) plus the smaller one's shifted right by the
+// exponent difference with a sticky bit; a carry out shifts right once
+// (sticky kept); the 53-bit result is rounded to nearest, ties to even, and
+// the exponent is added back so that a rounding carry or a subnormal sum that
+// reaches the normal range moves the exponent field by itself.  The caller
+// keeps the exact sum below 2^1023 (no overflow to infinity).
+__host__ __device__ __forceinline__ uint64_t add_nonneg_bits(uint64_t a, uint64_t b)
+{
+    constexpr uint64_t kFrac = (1ull << 52) - 1;
+    const uint64_t hi = a > b ? a : b, lo = a > b ? b : a;  // bit order = value order here
+    const uint32_t eh = (uint32_t)(hi >> 52), el = (uint32_t)(lo >> 52);
+    const uint32_t sh = eh ? eh : 1u, sl = el ? el : 1u;  // subnormals: exponent field 0 counts as 1
+    const uint64_t mh = ((hi & kFrac) | ((uint64_t)(eh != 0) << 52)) << 10;
+    const uint64_t ml = ((lo & kFrac) | ((uint64_t)(el != 0) << 52)) << 10;
+    const uint32_t d = sh - sl;
+    uint64_t al;
+    if (d == 0)
+        al = ml;
+    else if (d < 63)
+        al = (ml >> d) | (uint64_t)((ml & ((1ull << d) - 1)) != 0);
+    else
+        al = (uint64_t)(ml != 0);
+    uint64_t sum = mh + al;  // below 2^64: mh < 2^63, al < 2^63
+    uint32_t e = sh;
+    if (sum >> 63) {
+        sum = (sum >> 1) | (sum & 1);
+        e += 1;
+    }
+    uint64_t m = sum >> 10;  // 53 bits with the hidden one at bit 52 (below it for a subnormal sum)
+    const uint32_t rest = (uint32_t)sum & 0x3FFu;
+    m += (uint64_t)(rest > 0x200u || (rest == 0x200u && (m & 1)));
+    return ((uint64_t)(e - 1) << 52) + m;
+}
+
+__device__ __forceinline__ uint64_t dbits(double x) { return (uint64_t)__double_as_longlong(x); }
+__device__ __forceinline__ double bitsd(uint64_t b) { return __longlong_as_double((long long)b); }
+
 // Walk the voxels.  For voxel k (0-based) the visitor receives
 // (k, 1-based linear index, t at entry, t at exit).  Returns the voxel
 // count, or -1 if the reference would overrun its Nx+Ny+Nz storage
 // (RayTracing3DTOF.py:71-75, 162) — the visitor has then seen `cap` voxels.
+//
+// The axis choice and the crossing updates are the reference's FP64 ones
+// (:133-150).  They are evaluated on the integer pipe while every crossing
+// parameter is a non-negative finite double and every step is below 2^1000:
+// then `<` between parameters is `<` between their bit patterns, and
+// add_nonneg_bits gives the FP64 sum bit for bit (the walk takes at most cap
+// steps, so no sum comes near overflow).  A start point on a voxel face can
+// put a first crossing a rounding error below 0 (or at -0); such values are
+// the smallest, so the FP64 steps that consume them come first, and the walk
+// continues on the integer pipe once all three are non-negative.  Rays with a
+// step of 2^1000 or more stay in FP64.
 template <class Visit>
 __device__ __forceinline__ int ray_walk(const Grid& g, Ray& r, int cap, Visit&& visit)
 {
+    constexpr uint64_t kLimit = 0x7E70000000000000ull;  // bit pattern of 2^1000
     int64_t cur = sub2ind(g, r.X, r.Y, r.Z);
     double tprev = r.tmin;
     int n = 1;
+    constexpr uint64_t kMag = ~(1ull << 63);  // magnitude bits; NaN and infinity lie above kLimit
+    const bool steps_ok = dbits(r.xd) < kLimit && dbits(r.yd) < kLimit && dbits(r.zd) < kLimit &&
+                          (dbits(r.xt) & kMag) < kLimit && (dbits(r.yt) & kMag) < kLimit &&
+                          (dbits(r.zt) & kMag) < kLimit;
+    bool fp64 = !steps_ok || ((dbits(r.xt) | dbits(r.yt) | dbits(r.zt)) >> 63);
     while (r.X != r.xe || r.Y != r.ye || r.Z != r.ze) {
         if (n >= cap) return -1;
         // The reference's choice (:133-150): x if xt < yt and xt < zt, y if
         // yt <= xt and yt < zt, else z; made with selects so that the lanes of a
-        // warp stepping along different axes share one FP64 add.
-        const bool xy = r.xt < r.yt;
-        const double a = xy ? r.xt : r.yt;
-        const bool pa = a < r.zt;
-        const bool sx = pa && xy, sy = pa && !xy;
-        const double t = pa ? a : r.zt;
-        const double tn = add64(t, sx ? r.xd : (sy ? r.yd : r.zd));
+        // warp stepping along different axes share one add.
+        bool sx, sy, pa;
+        double t, tn;
+        if (fp64) {
+            const bool xy = r.xt < r.yt;
+            const double a = xy ? r.xt : r.yt;
+            pa = a < r.zt;
+            sx = pa && xy;
+            sy = pa && !xy;
+            t = pa ? a : r.zt;
+            tn = add64(t, sx ? r.xd : (sy ? r.yd : r.zd));
+        } else {
+            const uint64_t xb = dbits(r.xt), yb = dbits(r.yt), zb = dbits(r.zt);
+            const bool xy = xb < yb;
+            const uint64_t ab = xy ? xb : yb;
+            pa = ab < zb;
+            sx = pa && xy;
+            sy = pa && !xy;
+            const uint64_t tb = pa ? ab : zb;
+            t = bitsd(tb);
+            tn = bitsd(add_nonneg_bits(tb, dbits(sx ? r.xd : (sy ? r.yd : r.zd))));
+        }
         r.xt = sx ? tn : r.xt;
         r.yt = sy ? tn : r.yt;
         r.zt = pa ? r.zt : tn;
         r.X += sx ? r.xs : 0;
         r.Y += sy ? r.ys : 0;
         r.Z += pa ? 0 : r.zs;
+        fp64 = fp64 && (!steps_ok || ((dbits(r.xt) | dbits(r.yt) | dbits(r.zt)) >> 63));
         visit(n - 1, cur, tprev, t);
         tprev = t;
         cur = sub2ind(g, r.X, r.Y, r.Z);

@@ -25,7 +25,8 @@ def _require_cuda(device):
     dev = torch.device(device)
     if dev.type != "cuda":
         raise ValueError(f"device {dev} is not a CUDA device: the engine has no CPU path")
-    return dev
+    # "cuda" means the current device; name it, so that devices compare equal
+    return dev if dev.index is not None else torch.device("cuda", torch.cuda.current_device())
 
 
 def as_device(a, dtype, device):

@@ -1,0 +1,86 @@
+// Host-side check of sss::add_nonneg_bits (opensss_gb300/csrc/trace.cuh), the
+// integer-pipe FP64 addition of the ray walk: against the host's IEEE
+// binary64 addition (round to nearest even) on seeded random operands of
+// every kind the walk can meet -- equal and distant exponents, near-equal
+// values, subnormals, and running sums of walk-like steps.  Prints the
+// number of cases and of mismatches; exits non-zero on any mismatch.
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#include "trace.cuh"
+
+static uint64_t bits_of(double x)
+{
+    uint64_t u;
+    std::memcpy(&u, &x, 8);
+    return u;
+}
+
+static double double_of(uint64_t u)
+{
+    double x;
+    std::memcpy(&x, &u, 8);
+    return x;
+}
+
+int main(int argc, char** argv)
+{
+    const long cases = argc > 1 ? std::atol(argv[1]) : 4000000;
+    std::mt19937_64 rng(20261204);
+    constexpr uint64_t kPos = 0x7FFFFFFFFFFFFFFFull, kFrac = 0x000FFFFFFFFFFFFFull;
+    long checked = 0, bad = 0;
+    auto check = [&](uint64_t x, uint64_t y) {
+        if ((x >> 52) == 0x7FF || (y >> 52) == 0x7FF) return;
+        const double s = double_of(x) + double_of(y);
+        if (!(s < 8.98846567431158e307)) return;  // the walk keeps sums below 2^1023
+        const uint64_t got = sss::add_nonneg_bits(x, y);
+        ++checked;
+        if (got != bits_of(s)) {
+            if (bad < 8)
+                std::printf("mismatch %016llx + %016llx: %016llx, IEEE %016llx\n", (unsigned long long)x,
+                            (unsigned long long)y, (unsigned long long)got, (unsigned long long)bits_of(s));
+            ++bad;
+        }
+    };
+    for (long i = 0; i < cases; ++i) {
+        uint64_t x = rng() & kPos, y = rng() & kPos;
+        switch (i % 6) {
+        case 1:  // same exponent
+            y = (x & ~kFrac) | (rng() & kFrac);
+            break;
+        case 2:  // within a few ulps
+            y = (x + (rng() % 64) - 32) & kPos;
+            break;
+        case 3: {  // exponent difference below 60
+            const uint64_t e = x >> 52, e2 = e > 60 ? e - rng() % 60 : e;
+            y = (e2 << 52) | (rng() & kFrac);
+            break;
+        }
+        case 4:  // subnormal operands and sums crossing into the normal range
+            x &= kFrac;
+            y &= 0x001FFFFFFFFFFFFFull;
+            break;
+        case 5:  // parameters near 1 plus voxel steps
+            x = (x & 0x3FFFFFFFFFFFFFFFull) | 0x3000000000000000ull;
+            y = (y & kFrac) | ((uint64_t)(0x3FF - rng() % 70) << 52);
+            break;
+        default:
+            break;
+        }
+        check(x, y);
+    }
+    // running sums as a walk forms them: a start near 0 plus a fixed step
+    std::uniform_real_distribution<double> start(0.0, 1e-3), step(1e-4, 0.2);
+    for (int r = 0; r < 4000; ++r) {
+        double t = start(rng);
+        const double d = step(rng);
+        for (int k = 0; k < 300; ++k) {
+            check(bits_of(t), bits_of(d));
+            t = t + d;
+        }
+    }
+    std::printf("checked %ld, mismatches %ld\n", checked, bad);
+    return bad != 0;
+}
