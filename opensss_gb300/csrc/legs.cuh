@@ -55,8 +55,20 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
         const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
         const float inv_c = (float)(1.0 / kLightCmPerPs);
         const double t0 = r.tmin;
+        // parameter gaps in fixed point (exact differences, no FP64 subtraction)
+        // while the parameters stay below 4 in magnitude, else in FP64
+        const bool ok0 = fix61_ok(t0);
+        const int64_t f0 = fix61(t0);
+        int64_t fprev = f0;
+        bool okprev = ok0;
         float2* out = P.vox ? P.vox + ((long long)s * P.nl + l) * P.cap : nullptr;
         int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
+            const bool okb = fix61_ok(tb);
+            const int64_t fb = fix61(tb);
+            const bool okab = okb && okprev, ok0b = okb && ok0;
+            const int64_t fa = fprev;
+            fprev = fb;
+            okprev = okb;
             long long v = lin - 1;
             if (v < 0 || v >= P.nvox) {
                 raise_error(P.status, kErrVoxel);
@@ -65,15 +77,15 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
             // |vec| * |dt|; for near-zero steps the reference's own FP64 length
             // expression decides whether a corner-grazing segment is zero or
             // not (that decides whether a leg carries activity, :483-488)
-            const double dt = tb - ta;
-            const float adt = (float)fabs(dt);  // the threshold is compared in FP32
+            const float adt = okab ? unfix61_abs(fb - fa) : (float)fabs(tb - ta);
             float len = adt < 1e-9f ? (float)ref_length(r, ta, tb) : vlen * adt;
             float a = __ldg(P.act + v) * len;
             musum = fmaf(__ldg(P.mu + v), len, musum);
             asum += a;
             if (a != 0.f && out) {
                 // sample = half the distance walked to the voxel's exit (:155-156)
-                float rho = vlen * (float)(tb - t0) * inv_c;
+                const float dt0 = ok0b ? unfix61_abs(fb - f0) : (float)(tb - t0);
+                float rho = vlen * dt0 * inv_c;
                 out[nlist] = make_float2(a, rho);
                 ++nlist;
             }

@@ -199,6 +199,31 @@ __host__ __device__ __forceinline__ uint64_t add_nonneg_bits(uint64_t a, uint64_
 __device__ __forceinline__ uint64_t dbits(double x) { return (uint64_t)__double_as_longlong(x); }
 __device__ __forceinline__ double bitsd(uint64_t b) { return __longlong_as_double((long long)b); }
 
+// Fixed-point form of a walk parameter, in units of 2^-61, for |t| < 4
+// (fix61_ok): exact for |t| >= 2^-8 and truncated below, an absolute error
+// under 2^-61.  Differences of such values are exact, so parameter gaps need
+// no FP64 subtraction.
+__device__ __forceinline__ bool fix61_ok(double t) { return ((dbits(t) >> 52) & 0x7FF) <= 1024; }
+__device__ __forceinline__ int64_t fix61(double t)
+{
+    const uint64_t b = dbits(t);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const uint64_t m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1023 + 9;  // value = m 2^(ex - 1075) = (m 2^sh) 2^-61
+    uint64_t v = 0;
+    if (ex != 0) v = sh >= 0 ? m << sh : (sh > -64 ? m >> -sh : 0);
+    return (b >> 63) ? -(int64_t)v : (int64_t)v;
+}
+// |x| 2^-61 as a float, truncated to 24 significant bits.
+__device__ __forceinline__ float unfix61_abs(int64_t x)
+{
+    const uint64_t u = x < 0 ? (uint64_t)(-x) : (uint64_t)x;
+    if (u == 0) return 0.f;
+    const int lz = __clzll((long long)u);
+    const uint32_t man = (uint32_t)((u << lz) >> 40);  // 24 bits, the leading one at bit 23
+    return __uint_as_float(((uint32_t)(129 - lz) << 23) | (man & 0x7FFFFFu));
+}
+
 // Walk the voxels.  For voxel k (0-based) the visitor receives
 // (k, 1-based linear index, t at entry, t at exit).  Returns the voxel
 // count, or -1 if the reference would overrun its Nx+Ny+Nz storage
