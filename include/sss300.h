@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SSS300_ABI_VERSION 3
+#define SSS300_ABI_VERSION 4
 
 enum {
     SSS_OK = 0,
@@ -233,23 +233,27 @@ int sss_upsample(const float *sampled, int64_t bin_stride, int32_t nbins, const 
  * (not the same crystal) is traced through map (device float32, Fortran
  * order; attenuation in cm^-1, or activity when use_activity) in FP64.
  * out[cell*nr*nr + sino_index[Ring1][Ring2]] = 1 where 1/exp(-sum mu*len) == 1
- * (attenuation) or sum act*len <= 0 (activity).  out (device uint8,
+ * (attenuation) or sum act*len <= 0 (activity).  acf_below = 0 keeps that
+ * rule (the reference's, :145-151); acf_below > 1 masks instead where the
+ * attenuation factor 1/exp(-sum mu*len) is below acf_below (no reference
+ * counterpart: a looser tail definition, e.g. 1.03).  out (device uint8,
  * [(nd+1)*(nd/2)][nr*nr]) must be zeroed by the caller. */
 int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float *map, int32_t use_activity,
                   int32_t nr, int32_t nd, const double *geometry, const int16_t *lor,
-                  const int16_t *sino_index, int32_t af, uint8_t *out, int32_t *status, void *stream);
+                  const int16_t *sino_index, int32_t af, double acf_below, uint8_t *out, int32_t *status,
+                  void *stream);
 
 /* Tail mask with span.  Replaces MaskGeneratorMashing / MaskDetectorsMashing
  * (Python/openSSS/TailsMask.py:230-377): the LORs are those of the npairs ring
  * pairs pairs[p] = (Ring1, Ring2, slice) (device int32 [npairs][3]) on the
  * expanded geometry (nr = 2*rings - 1, Python/openSSS/Geometry.py:161-197),
- * crystal pairs as in sss_tail_mask; LOR (p, d1, d2) marks
+ * crystal pairs and acf_below as in sss_tail_mask; LOR (p, d1, d2) marks
  * out[cell*nslices + slice].  out (device uint8 [(nd+1)*(nd/2)][nslices])
  * must be zeroed by the caller. */
 int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const float *map, int32_t use_activity,
                         int32_t nr, int32_t nd, const double *geometry, const int16_t *lor, const int32_t *pairs,
-                        int32_t npairs, int32_t nslices, int32_t af, uint8_t *out, int32_t *status,
-                        void *stream);
+                        int32_t npairs, int32_t nslices, int32_t af, double acf_below, uint8_t *out,
+                        int32_t *status, void *stream);
 
 /* Back-projection scale fit.  Replaces BackProjectionScatterRandFit
  * (Python/openSSS/BackProjection.py:115-215) and BackProjection (:31-113).

@@ -26,10 +26,16 @@ def _ptr(t):
 
 
 def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramIndex,
-                     AccelerationFactor=1, use_activity=False, device="cuda", span: bool = False) -> torch.Tensor:
+                     AccelerationFactor=1, use_activity=False, device="cuda", span: bool = False,
+                     acf_below: float | None = None) -> torch.Tensor:
     """uint8 CUDA tensor [(ND+1)*(ND//2), slices]: NR*NR slices, or with
     ``span`` the mashed sinograms of ``SinogramIndex`` (float [n, 2], from
-    SinogramLUT) on the expanded ``Geometry``."""
+    SinogramLUT) on the expanded ``Geometry``.  ``acf_below`` None keeps the
+    reference's rule (attenuation factor exactly 1); a bound above 1 marks the
+    LORs whose factor 1/exp(-sum mu*len) is below it instead."""
+    acf = 0.0 if acf_below is None else float(acf_below)
+    if not (acf == 0.0 or acf > 1.0):
+        raise ValueError("acf_below must be None or above 1")
     if not torch.cuda.is_available():
         raise _lib.EngineUnavailable("no CUDA device: the engine has no CPU path")
     geom = np.asarray(Geometry, dtype=np.float64)
@@ -50,14 +56,14 @@ def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramI
         _lib.check(_lib.lib().sss_tail_mask_pairs(
             grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), _ptr(vol),
             int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(pairs), nslices, nslices,
-            int(AccelerationFactor or 1), _ptr(out), _ptr(status), C.c_void_p(st.cuda_stream)))
+            int(AccelerationFactor or 1), acf, _ptr(out), _ptr(status), C.c_void_p(st.cuda_stream)))
     else:
         si = as_device(geometry.check_slice_table(SinogramIndex, nr).astype(np.int16), torch.int16, device)
         out = torch.zeros(((nd + 1) * (nd // 2), nr * nr), dtype=torch.uint8, device=device)
         _lib.check(_lib.lib().sss_tail_mask(grid.ctypes.data_as(C.c_void_p),
                                             bounds.ctypes.data_as(C.c_void_p), _ptr(vol),
                                             int(bool(use_activity)), nr, nd, _ptr(g), _ptr(lor), _ptr(si),
-                                            int(AccelerationFactor or 1), _ptr(out), _ptr(status),
+                                            int(AccelerationFactor or 1), acf, _ptr(out), _ptr(status),
                                             C.c_void_p(st.cuda_stream)))
     st.synchronize()
     _lib.check_status(int(status.item()))
@@ -65,19 +71,24 @@ def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramI
 
 
 def MaskGenerator(ActivityMap, AttenuationMap, ImageSize, Geometry, SinogramCoordinates,
-                  SinogramIndex, UseAttenuation, AccelerationFactor=1, device="cuda"):
+                  SinogramIndex, UseAttenuation, AccelerationFactor=1, device="cuda", AttenuationThreshold=None):
+    """``AttenuationThreshold`` (no reference counterpart): None keeps the
+    reference's tails (attenuation factor exactly 1); a value above 1 marks
+    the LORs whose attenuation factor lies below it, e.g. 1.03."""
     t0 = time.time()
     geom = np.asarray(Geometry)
     nr, nd = geom.shape[:2]
     vol = AttenuationMap if UseAttenuation else ActivityMap
     m = tail_mask_device(vol, ImageSize, geom, SinogramCoordinates, SinogramIndex,
-                         AccelerationFactor, use_activity=not UseAttenuation, device=device)
+                         AccelerationFactor, use_activity=not UseAttenuation, device=device,
+                         acf_below=AttenuationThreshold)
     print("Time for Generate Tail Mask:", time.time() - t0, "seconds")
     return m.cpu().numpy().reshape(nd + 1, nd // 2, nr * nr)
 
 
 def MaskGeneratorMashing(ActivityMap, AttenuationMap, ImageSize, Geometry, SinogramCoordinates,
-                         MashedSinogramIndices, UseAttenuation, AccelerationFactor=1, device="cuda"):
+                         MashedSinogramIndices, UseAttenuation, AccelerationFactor=1, device="cuda",
+                         AttenuationThreshold=None):
     """Tail mask with span (``TailsMask.py:311-377``): ``Geometry`` is the
     expanded geometry and ``MashedSinogramIndices`` the mashed SinogramIndex
     of SinogramLUT.  uint8 (ND+1, ND//2, mashed sinograms)."""
@@ -86,23 +97,25 @@ def MaskGeneratorMashing(ActivityMap, AttenuationMap, ImageSize, Geometry, Sinog
     nd = geom.shape[1]
     vol = AttenuationMap if UseAttenuation else ActivityMap
     m = tail_mask_device(vol, ImageSize, geom, SinogramCoordinates, MashedSinogramIndices,
-                         AccelerationFactor, use_activity=not UseAttenuation, device=device, span=True)
+                         AccelerationFactor, use_activity=not UseAttenuation, device=device, span=True,
+                         acf_below=AttenuationThreshold)
     print("Time for Generate Tail Mask:", time.time() - t0, "seconds")
     return m.cpu().numpy().reshape(nd + 1, nd // 2, -1)
 
 
 def GenerateTailsMask(SavePath, ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
                       extendedGeometry, LORCoordinates, SinogramIndex, AccelerationFactor,
-                      UseAttenuation=True, Overwrite=False, device="cuda"):
+                      UseAttenuation=True, Overwrite=False, device="cuda", AttenuationThreshold=None):
     path = os.path.join(SavePath, "AttenuationMask.npy")
     if os.path.isfile(path) and not Overwrite:
         return np.load(path)
     if np.asarray(extendedGeometry).shape[0] != 0:  # span (TailsMask.py:70-74)
         mask = MaskGeneratorMashing(ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize,
                                     extendedGeometry, LORCoordinates, SinogramIndex, UseAttenuation,
-                                    AccelerationFactor, device)
+                                    AccelerationFactor, device, AttenuationThreshold)
     else:
         mask = MaskGenerator(ActivityMapDownscaled, AttenuationMapDownscaled, ImageSize, Geometry,
-                             LORCoordinates, SinogramIndex, UseAttenuation, AccelerationFactor, device)
+                             LORCoordinates, SinogramIndex, UseAttenuation, AccelerationFactor, device,
+                             AttenuationThreshold)
     np.save(path, mask)
     return mask

@@ -138,6 +138,8 @@ struct MaskParams {
     const int32_t* pairs;       // span: [npairs][3] (Ring1, Ring2, slice), else null
     int npairs, nslices;
     int nr, nd, na, af, cap;
+    double acf_below;           // 0: the reference's rule ACF == 1; else mask where ACF < acf_below
+    double decided;             // a line integral above this fixes the LOR as not masked
     uint8_t* out;
     int32_t* status;
 };
@@ -171,9 +173,10 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
         double sum = 0.0;
         bool bad = false;
         // With a map of non-negative values the sum only grows: once it is
-        // above kDecided the mask value is fixed (1/exp(-s) != 1, activity > 0)
-        // and the remaining lengths need not be evaluated.  The walk itself
-        // always runs to the end, so an overrun is still reported.
+        // above P.decided the mask value is fixed (the factor is past the rule's
+        // bound, or activity > 0) and the remaining lengths need not be
+        // evaluated.  The walk itself always runs to the end, so an overrun is
+        // still reported.
         const bool nonneg = !(*(volatile const int32_t*)P.status & kNoteMapSigned);
         int c = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
             const long long v = lin - 1;
@@ -184,13 +187,15 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
             // a zero voxel adds exactly +0 whatever its length, so the FP64
             // length (the walk's dominant cost) is evaluated only where it counts
             const float mu = __ldg(P.mu + v);
-            if (mu != 0.f && !(nonneg && sum > kDecided)) sum = add64(sum, mul64((double)mu, ref_length(r, t0, t1)));
+            if (mu != 0.f && !(nonneg && sum > P.decided)) sum = add64(sum, mul64((double)mu, ref_length(r, t0, t1)));
         });
         if (c < 0) raise_error(P.status, kErrOverrun);
         if (bad) raise_error(P.status, kErrVoxel);
         acf = P.use_activity ? (sum > 0.0 ? 0.0 : 1.0) : div64(1.0, exp(-sum));  // :144-156
     }
-    if (acf == 1.0) {  // :150-161, one LOR per (cell, slice)
+    // :150-161 (ACF == 1), or the caller's bound on the factor; one LOR per (cell, slice)
+    const bool tail = (P.acf_below > 0.0 && !P.use_activity) ? acf < P.acf_below : acf == 1.0;
+    if (tail) {
         const int ang = P.lor[2 * ((long long)d1 * P.nd + d2)];
         const int rad = P.lor[2 * ((long long)d1 * P.nd + d2) + 1];
         if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2) {  // unset coordinates
@@ -439,10 +444,16 @@ namespace {
 
 int tail_mask(const int32_t grid[3], const double bounds[6], const float* map, int32_t use_activity, int32_t nr,
               int32_t nd, const double* geometry, const int16_t* lor, const int16_t* sino_index,
-              const int32_t* pairs, int32_t npairs, int32_t nslices, int32_t af, uint8_t* out, int32_t* status,
-              void* stream)
+              const int32_t* pairs, int32_t npairs, int32_t nslices, int32_t af, double acf_below, uint8_t* out,
+              int32_t* status, void* stream)
 {
+    if (!(acf_below == 0.0 || acf_below > 1.0))
+        return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask: acf_below must be 0 (ACF == 1) or above 1");
     MaskParams P;
+    P.acf_below = acf_below;
+    // the factor 1/exp(-s) passes acf_below once s > log(acf_below), with a
+    // margin far above FP64 rounding
+    P.decided = acf_below > 0.0 ? log(acf_below) * (1.0 + 1e-9) + 1e-12 : kDecided;
     P.pairs = pairs;
     P.npairs = npairs;
     P.nslices = pairs ? nslices : nr * nr;
@@ -475,28 +486,28 @@ int tail_mask(const int32_t grid[3], const double bounds[6], const float* map, i
 
 extern "C" int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float* map,
                              int32_t use_activity, int32_t nr, int32_t nd, const double* geometry,
-                             const int16_t* lor, const int16_t* sino_index, int32_t af, uint8_t* out,
-                             int32_t* status, void* stream)
+                             const int16_t* lor, const int16_t* sino_index, int32_t af, double acf_below,
+                             uint8_t* out, int32_t* status, void* stream)
 {
     int rc = check_grid(grid, bounds, "sss_tail_mask");
     if (rc) return rc;
     if (!map || !geometry || !lor || !sino_index || !out || nr < 1 || nd < 2 || af < 1)
         return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask: bad argument");
-    return tail_mask(grid, bounds, map, use_activity, nr, nd, geometry, lor, sino_index, nullptr, 0, 0, af, out,
-                     status, stream);
+    return tail_mask(grid, bounds, map, use_activity, nr, nd, geometry, lor, sino_index, nullptr, 0, 0, af,
+                     acf_below, out, status, stream);
 }
 
 extern "C" int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const float* map,
                                    int32_t use_activity, int32_t nr, int32_t nd, const double* geometry,
                                    const int16_t* lor, const int32_t* pairs, int32_t npairs, int32_t nslices,
-                                   int32_t af, uint8_t* out, int32_t* status, void* stream)
+                                   int32_t af, double acf_below, uint8_t* out, int32_t* status, void* stream)
 {
     int rc = check_grid(grid, bounds, "sss_tail_mask_pairs");
     if (rc) return rc;
     if (!map || !geometry || !lor || !pairs || !out || nr < 1 || nd < 2 || af < 1 || npairs < 0 || nslices < 1)
         return sss_set_error(SSS_ERR_INVALID, "sss_tail_mask_pairs: bad argument");
     return tail_mask(grid, bounds, map, use_activity, nr, nd, geometry, lor, nullptr, pairs, npairs, nslices, af,
-                     out, status, stream);
+                     acf_below, out, status, stream);
 }
 
 namespace {

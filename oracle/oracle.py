@@ -248,7 +248,9 @@ def densify(compact, lor, nd, nru, ndu):
 # ---------------------------------------------------------------- mask / fit
 
 
-def mask(mu, image_size, geometry, lor, sino_index, af, nthreads=0, use_activity=False):
+def mask(mu, image_size, geometry, lor, sino_index, af, nthreads=0, use_activity=False, acf_below=0.0):
+    """Tail mask (TailsMask.py:84-228): LORs whose attenuation factor is
+    exactly 1, or with ``acf_below`` > 1 below that bound."""
     grid = np.ascontiguousarray(mu.shape, dtype=np.int64)
     muf = np.ascontiguousarray(mu.flatten(order="F"), dtype=np.float32)
     gb = np.ascontiguousarray(image_size, dtype=np.float64)
@@ -259,7 +261,7 @@ def mask(mu, image_size, geometry, lor, sino_index, af, nthreads=0, use_activity
     out = np.zeros((nd + 1, nd // 2, nr * nr), np.uint8)
     st = lib().orc_mask(_p(grid), _p(muf), _p(gb), C.c_int64(nr), C.c_int64(nd), _p(geom), _p(lor),
                         _p(si), C.c_int64(af), C.c_int(int(use_activity)), _p(out),
-                        C.c_int(nthreads))
+                        C.c_int(nthreads), C.c_double(acf_below))
     if st:
         raise RuntimeError(f"oracle mask failed {st}")
     return out
@@ -300,7 +302,7 @@ def upsample_bin(sampled_bin, nru, ndu, nr, nd, lut, ringmap, sino_index):
     return out
 
 
-def mask_pairs(mu, image_size, geometry, lor, pairs, nslices, af, nthreads=0, use_activity=False):
+def mask_pairs(mu, image_size, geometry, lor, pairs, nslices, af, nthreads=0, use_activity=False, acf_below=0.0):
     """Span tail mask on the expanded geometry (TailsMask.py:230-377)."""
     grid = np.ascontiguousarray(mu.shape, dtype=np.int64)
     muf = np.ascontiguousarray(mu.flatten(order="F"), dtype=np.float32)
@@ -312,7 +314,7 @@ def mask_pairs(mu, image_size, geometry, lor, pairs, nslices, af, nthreads=0, us
     out = np.zeros((nd + 1, nd // 2, nslices), np.uint8)
     st = lib().orc_mask_pairs(_p(grid), _p(muf), _p(gb), C.c_int64(nr), C.c_int64(nd), _p(geom), _p(lor),
                               _p(pairs), C.c_int64(pairs.shape[0]), C.c_int64(nslices), C.c_int64(af),
-                              C.c_int(int(use_activity)), _p(out), C.c_int(nthreads))
+                              C.c_int(int(use_activity)), _p(out), C.c_int(nthreads), C.c_double(acf_below))
     if st:
         raise RuntimeError(f"oracle span mask failed {st}")
     return out

@@ -513,7 +513,7 @@ int orc_sss(const orc_sss_problem *p, double *out, int nthreads)
  * out: uint8 [(nd+1)][nd/2][nr*nr], slice SinogramIndex[Ring1, Ring2]. */
 int orc_mask(const int64_t *grid, const float *mu, const double *gb, int64_t nr, int64_t nd,
              const double *geom, const int16_t *lor, const int16_t *sino_index, int64_t af,
-             int use_activity, uint8_t *out, int nthreads)
+             int use_activity, uint8_t *out, int nthreads, double acf_below)
 {
     const int64_t nang = nd / 2, nsino = nr * nr;
     const int cap = (int)(grid[0] + grid[1] + grid[2]);
@@ -550,7 +550,9 @@ int orc_mask(const int64_t *grid, const float *mu, const double *gb, int64_t nr,
                     } else {
                         att = 1;
                     }
-                    if (att != 1) att = 0;
+                    /* the reference's tails (factor exactly 1), or a bound on the factor */
+                    if (acf_below > 0 && !use_activity) att = att < acf_below ? 1 : 0;
+                    else if (att != 1) att = 0;
                     int64_t sidx = sino_index[ring1 * nr + ring2];
                     uint8_t *cell = out + ((rad * nang + ang) * nsino + sidx);
                     *cell = (uint8_t)(*cell + (uint8_t)att);
@@ -667,7 +669,8 @@ int orc_fit(const int64_t *grid, const double *gb, int64_t nr, int64_t nd, const
  * per-sinogram images are summed in sinogram order (:381-385). */
 int orc_mask_pairs(const int64_t *grid, const float *mu, const double *gb, int64_t nr, int64_t nd,
                    const double *geom, const int16_t *lor, const int32_t *pairs, int64_t npairs,
-                   int64_t nslices, int64_t af, int use_activity, uint8_t *out, int nthreads)
+                   int64_t nslices, int64_t af, int use_activity, uint8_t *out, int nthreads,
+                   double acf_below)
 {
     const int64_t nang = nd / 2;
     const int cap = (int)(grid[0] + grid[1] + grid[2]);
@@ -700,7 +703,8 @@ int orc_mask_pairs(const int64_t *grid, const float *mu, const double *gb, int64
                     for (int k = 0; k < n; ++k) s += (double)mu[ix[k] - 1] * len[k];
                     att = use_activity ? (s > 0 ? 0.0 : 1.0) : 1 / exp(-s);  /* :289-301 */
                 }
-                if (att != 1) att = 0;
+                if (acf_below > 0 && !use_activity) att = att < acf_below ? 1 : 0;
+                else if (att != 1) att = 0;
                 uint8_t *cell = out + ((rad * nang + ang) * nslices + slice);
                 *cell = (uint8_t)(*cell + (uint8_t)att);
             }

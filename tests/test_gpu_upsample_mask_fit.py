@@ -229,3 +229,24 @@ def test_tail_mask_with_signed_map_matches_oracle(cuda_ok):
     m = MaskGenerator(np.ones_like(mu), mu, g["case0_bounds"], g["case0_geometry"], lor, si, True, af)
     ref = O.mask(mu, g["case0_bounds"], g["case0_geometry"], lor, si, af)
     assert np.array_equal(m, ref)
+
+
+@pytest.mark.parametrize("case", range(4))
+@pytest.mark.parametrize("bound", [1.03, 1.5])
+def test_tail_mask_threshold_matches_oracle(cuda_ok, case, bound):
+    """A bound on the attenuation factor instead of the reference's ACF == 1
+    (the benchmark's non-TOF workload masks where the factor is below 1.03):
+    bit-exact against the FP64 oracle's restatement of the same rule, and a
+    superset of the reference's mask."""
+    from opensss_gb300.TailsMask import MaskGenerator
+
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    lor, si, _ = _sino(nd, nr)
+    for scale in (1.0, 0.02):  # the golden map, and a faint one with many factors in (1, bound)
+        mu = (g[f"case{case}_mu"] * np.float32(scale)).astype(np.float32)
+        m = MaskGenerator(np.ones_like(mu), mu, g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, si, True,
+                          af, AttenuationThreshold=bound)
+        ref = O.mask(mu, g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, si, af, acf_below=bound)
+        assert np.array_equal(m, ref), scale
+        assert np.all(m >= O.mask(mu, g[f"case{case}_bounds"], g[f"case{case}_geometry"], lor, si, af))

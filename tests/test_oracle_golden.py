@@ -202,3 +202,28 @@ def test_oracle_point_list_matches_ranges(att_table):
     assert np.array_equal(O.sss_compact(*args, points=np.arange(10)), O.sss_compact(*args, sp_end=10))
     with pytest.raises(RuntimeError, match="status -5"):
         O.sss_compact(*args, points=np.array([3, 2]))
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_oracle_mask_threshold_rule(case):
+    """The oracle's bound on the attenuation factor: a bound just above 1
+    gives exactly the reference's tails; a larger bound only adds LORs, and
+    on a faint map it adds crossing LORs whose factor lies below it."""
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g[f"case{case}_dims"])
+    from opensss_gb300 import geometry as G
+
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    mu, b, geo = g[f"case{case}_mu"], g[f"case{case}_bounds"], g[f"case{case}_geometry"]
+    ref = g[f"case{case}_mask"]
+    assert np.array_equal(O.mask(mu, b, geo, lor, si, af), ref)
+    tight = O.mask(mu, b, geo, lor, si, af, acf_below=1.0 + 1e-15)
+    assert np.array_equal(tight, ref)
+    assert np.all(O.mask(mu, b, geo, lor, si, af, acf_below=1.03) >= ref)
+    # a faint map (2% of the values) puts many crossing LORs between 1 and 1.03
+    faint = (mu * np.float32(0.02)).astype(np.float32)
+    exact = O.mask(faint, b, geo, lor, si, af)
+    loose = O.mask(faint, b, geo, lor, si, af, acf_below=1.03)
+    assert np.all(loose >= exact)
+    if mu.max() > 0:  # one fixture is the empty map, where every LOR is a tail either way
+        assert loose.sum() > exact.sum()
