@@ -735,8 +735,13 @@ def run_serving(dev, args, att):
                                                        seed=2026))
     s, p = latency_summary(served, beds), latency_summary(plain, beds)
     offered = sum(beds[r.bed].units for r in served) / args.serve_seconds
-    # error of served results against the FP64 oracle, for the first small requests
-    errs = []
+    # served results against the FP64 oracle: small requests whole, large
+    # ones on a stratified sample of their scatter points (the served result
+    # is first compared with the same request run alone, 1e-5, then that
+    # run's point sample with the oracle's)
+    from opensss_gb300.engine import select_points
+
+    errs_small, errs_large, solo_large = [], [], []
     for r in [r for r in served if not beds[r.bed].large][:args.serve_check]:
         bed, pr = beds[r.bed], problems[r.bed]
         act = request_activity(bed, r.seed).cpu().numpy().reshape(bed.shape, order="F")
@@ -745,7 +750,26 @@ def run_serving(dev, args, att):
                             pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step, pr.tof_resolution,
                             pr.tof_range, pr.nr_bins, nthreads=cpu_threads())
         got = leg_pair_to_compact(r.out.cpu().numpy(), pr.nr_rings_used, pr.nr_detectors_used)
-        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        errs_small.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    seen_beds = set()
+    for r in [r for r in served if beds[r.bed].large]:
+        if r.bed in seen_beds or len(seen_beds) >= 2:
+            continue
+        seen_beds.add(r.bed)
+        bed, pr = beds[r.bed], problems[r.bed]
+        act_t = request_activity(bed, r.seed)
+        alone = bed.engine.run_flat(act_t, bed.mu, bed.shape, bed.image_size).cpu().numpy()
+        solo_large.append(float(np.linalg.norm(r.out.cpu().numpy() - alone) / np.linalg.norm(alone)))
+        idx = W.stratified_points(int(bed.counts.sum()), 16)
+        sub = bed.engine.run_flat(act_t, bed.mu, bed.shape, bed.image_size, points=idx).cpu().numpy()
+        act = act_t.cpu().numpy().reshape(bed.shape, order="F")
+        ref = O.sss_compact(act, pr.attenuation, pr.image_size, pr.scanner.geometry, pr.scanner.normals,
+                            pr.scanner.detector_size_mm, att, pr.energy_resolution, pr.energy_threshold,
+                            pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step, pr.tof_resolution,
+                            pr.tof_range, pr.nr_bins, points=idx, nthreads=cpu_threads())
+        got = leg_pair_to_compact(sub, pr.nr_rings_used, pr.nr_detectors_used)
+        errs_large.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    sweep = run_serving_sweep(beds, args)
     return {"workload": f"Poisson {args.serve_rate:g} req/s for {args.serve_seconds:g} s (seed 2026), "
                         "70% small / 30% large over 8 resident beds",
             "beds": [{"name": pr.name, "volume": list(pr.grid), "rings": pr.nr_rings_used,
@@ -753,7 +777,41 @@ def run_serving(dev, args, att):
                      for pr, b in zip(problems, beds)],
             "offered_units_per_s": offered, "hbm_budget_gb": 80, "served": s, "plain": p,
             "p99_speedup": p["p99_ms"] / s["p99_ms"], "throughput_ratio": s["units_per_s"] / p["units_per_s"],
-            "server_stats": dict(srv.stats), "rel_l2_vs_fp64_small": errs, "clocks": clk.summary()}
+            "server_stats": dict(srv.stats), "clocks": clk.summary(),
+            "rel_l2_vs_fp64_small": errs_small, "rel_l2_served_vs_alone_large": solo_large,
+            "rel_l2_vs_fp64_large_sample": errs_large,
+            "large_sample": "16 scatter points spread evenly over the bed's points, same points in the oracle",
+            "sweep": sweep}
+
+
+def run_serving_sweep(beds, args):
+    """Latency against offered rate: the same 70/30 mix at several Poisson
+    rates for ``--sweep-seconds`` of arrivals each, the batching server and the
+    plain one, and the highest rate each sustains with its p99 under
+    ``--p99-bound-ms`` (a rate sustains when the work is done within the
+    window plus the bound, i.e. no growing backlog)."""
+    from opensss_gb300.serving import PlainServer, ScatterServer, latency_summary, poisson_stream
+
+    rates = [float(x) for x in args.sweep_rates.split(",") if x]
+    rows = []
+    for rate in rates:
+        row = {"rate": rate}
+        for name, mk in (("served", lambda: ScatterServer(beds, hbm_budget=80 << 30)),
+                         ("plain", lambda: PlainServer(beds))):
+            reqs = mk().serve(poisson_stream(rate, args.sweep_seconds, beds, 0.7, seed=int(rate * 10) + 7))
+            summ = latency_summary(reqs, beds)
+            row[name] = {k: summ[k] for k in ("requests", "p50_ms", "p99_ms", "small_p99_ms", "large_p99_ms",
+                                              "requests_per_s", "makespan_s")}
+        rows.append(row)
+
+    def best(name):
+        ok = [r["rate"] for r in rows
+              if r[name]["p99_ms"] is not None and r[name]["p99_ms"] <= args.p99_bound_ms
+              and r[name]["makespan_s"] <= args.sweep_seconds + args.p99_bound_ms / 1e3]
+        return max(ok) if ok else None
+
+    return {"rates": rates, "seconds": args.sweep_seconds, "p99_bound_ms": args.p99_bound_ms, "rows": rows,
+            "sustained_rate_served": best("served"), "sustained_rate_plain": best("plain")}
 
 
 def run_prep(dev, args):
@@ -1061,8 +1119,13 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="mean arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="length of the arrival window")
-    ap.add_argument("--serve-check", type=int, default=2,
+    ap.add_argument("--serve-check", type=int, default=16,
                     help="served small requests checked against the FP64 oracle")
+    ap.add_argument("--sweep-rates", default="4,8,16,24,32,48",
+                    help="offered rates (req/s) of the serving latency sweep")
+    ap.add_argument("--sweep-seconds", type=float, default=2.0, help="arrival window of each sweep point")
+    ap.add_argument("--p99-bound-ms", type=float, default=2000.0,
+                    help="p99 latency bound of the sustained-rate figure")
     ap.add_argument("--no-listmode", action="store_true", help="skip the list-mode histogramming")
     ap.add_argument("--no-prep", action="store_true", help="skip the image preparation (CropAndDownscale)")
     ap.add_argument("--no-autotune", action="store_true", help="run with the library's default launch shapes")

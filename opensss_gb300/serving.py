@@ -15,12 +15,15 @@ a new activity map (the bed's base activity times 1 +- 5% seeded noise).
   in flight (workspaces, outputs, per-request activity maps) plus the new
   batch stays under ``hbm_budget`` bytes; waiting requests keep FIFO order
   within their class;
-* continuous batching: the GPU queue is kept ``depth`` waves deep.  Whenever
-  there is room, waiting small requests are planned together into one batch
-  (``BatchSSS``, planned from the cached scatter points) and enqueued whole;
-  otherwise the next wave of the current large batch is enqueued.  Small
-  requests therefore wait for at most ``depth`` waves of large work, not for
-  whole large requests;
+* continuous batching on two streams: waiting small requests are planned
+  together into one batch (``BatchSSS``, planned from the cached scatter
+  points) and enqueued whole on a high-priority stream, while the current
+  large request runs wave by wave on a low-priority stream that is kept
+  ``depth`` waves deep.  A small request that arrives while large work is on
+  the GPU is admitted at once (memory permitting): its kernels are queued
+  beside the large waves and the block scheduler gives them the
+  multiprocessors that the large kernels free, so the two overlap on the
+  device instead of taking turns;
 * completion times are GPU timestamps (CUDA events against one start event).
 
 ``PlainServer`` is the reference-style baseline: requests in arrival order,
@@ -129,7 +132,10 @@ class ScatterServer:
         self.depth = depth
         self.large_ws = int(large_workspace)
         self.max_small = max_small_batch
-        self.compute = torch.cuda.Stream(self.dev)
+        # lower numbers are higher priorities; the small batches' stream gets the highest
+        lo_prio, hi_prio = torch.cuda.Stream.priority_range()
+        self.compute = torch.cuda.Stream(self.dev, priority=lo_prio)
+        self.small = torch.cuda.Stream(self.dev, priority=hi_prio)
         self.planning = torch.cuda.Stream(self.dev)
         self.resident = sum(b.mu.numel() * 8 + b.points.numel() * 8 for b in beds)
         self.stats = collections.Counter()
@@ -144,7 +150,7 @@ class ScatterServer:
         return min(need, self.large_ws) if large else need
 
     # -- batches -------------------------------------------------------
-    def _start(self, reqs, large: bool, in_flight: int) -> _Batch | None:
+    def _start(self, reqs, large: bool, in_flight: int, stream=None) -> _Batch | None:
         ws_bytes = self._workspace(reqs, large)
         nbytes = ws_bytes + sum(self._out_bytes(r) for r in reqs)
         if self.resident + in_flight + nbytes > self.budget:
@@ -161,29 +167,31 @@ class ScatterServer:
             plan = BatchSSS(jobs, stream=self.planning, points=pts, workspace=ws, outs=[r.out for r in reqs])
             ready = torch.cuda.Event()
             ready.record(self.planning)
-        self.compute.wait_event(ready)
+        (stream or self.compute).wait_event(ready)
         b = _Batch(reqs, plan, nbytes, large)
         b.acts = acts
         self.stats["batches_large" if large else "batches_small"] += 1
         return b
 
-    def _enqueue_wave(self, b: _Batch, waves_in_queue: collections.deque):
-        b.plan.run_waves(b.next_wave, 1, stream=self.compute)
+    def _enqueue_wave(self, b: _Batch, waves_in_queue: collections.deque, stream=None):
+        st = stream or self.compute
+        b.plan.run_waves(b.next_wave, 1, stream=st)
         b.next_wave += 1
         ev = torch.cuda.Event(enable_timing=True)
-        ev.record(self.compute)
+        ev.record(st)
         waves_in_queue.append(ev)
         if b.next_wave == b.plan.waves:
             b.done_event = ev
         self.stats["waves"] += 1
 
-    def _enqueue_all(self, b: _Batch, waves_in_queue: collections.deque):
+    def _enqueue_all(self, b: _Batch, waves_in_queue: collections.deque, stream=None):
+        st = stream or self.compute
         while b.next_wave < b.plan.waves:
-            self._enqueue_wave(b, waves_in_queue)
+            self._enqueue_wave(b, waves_in_queue, st)
         if b.done_event is None:  # no scatter points: nothing to run
-            b.plan.run_waves(0, 0, stream=self.compute)
+            b.plan.run_waves(0, 0, stream=st)
             b.done_event = torch.cuda.Event(enable_timing=True)
-            b.done_event.record(self.compute)
+            b.done_event.record(st)
 
     def serve(self, requests: list[Request]) -> list[Request]:
         """Serve ``requests`` (sorted by arrival) in real time; returns them
@@ -194,10 +202,12 @@ class ScatterServer:
         current_large: _Batch | None = None
         in_flight: list[_Batch] = []
         retired: list[torch.Tensor] = []  # status words of finished batches
-        queue: collections.deque = collections.deque()
+        queue: collections.deque = collections.deque()        # large waves on self.compute
+        small_queue: collections.deque = collections.deque()  # small batches' waves on self.small
         start = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(self.dev)
         start.record(self.compute)
+        self.small.wait_event(start)
         t0 = time.perf_counter()
         i, finished = 0, 0
         while finished < len(reqs):
@@ -221,19 +231,29 @@ class ScatterServer:
                     finished += len(b.reqs)
             while queue and queue[0].query():
                 queue.popleft()
+            while small_queue and small_queue[0].query():
+                small_queue.popleft()
             used = sum(b.nbytes for b in in_flight)
+            # small requests: admitted at once into the high-priority stream,
+            # beside whatever large work is queued
+            if small_q and len(small_queue) < self.depth:
+                n = min(len(small_q), self.max_small)
+                b = None
+                while n >= 1:
+                    take = [small_q.popleft() for _ in range(n)]
+                    b = self._start(take, False, used, self.small)
+                    if b is not None:
+                        break
+                    small_q.extendleft(reversed(take))
+                    n //= 2  # a smaller batch may fit where this one does not
+                if b is None:
+                    if not in_flight:
+                        raise MemoryError("a small request does not fit the HBM budget")
+                else:
+                    in_flight.append(b)
+                    self._enqueue_all(b, small_queue, self.small)
+                    continue
             if len(queue) < self.depth:
-                if small_q:
-                    take = [small_q.popleft() for _ in range(min(len(small_q), self.max_small))]
-                    b = self._start(take, False, used)
-                    if b is None:
-                        if not in_flight:
-                            raise MemoryError("a batch of small requests does not fit the HBM budget")
-                        small_q.extendleft(reversed(take))
-                    else:
-                        in_flight.append(b)
-                        self._enqueue_all(b, queue)
-                        continue
                 if current_large is not None and current_large.next_wave < current_large.plan.waves:
                     self._enqueue_wave(current_large, queue)
                     continue
