@@ -245,6 +245,13 @@ __device__ __forceinline__ float fit_scatter(const FitParams& P, int b, long lon
     return P.scat_clamp ? fmaxf(sv, 0.f) : sv;
 }
 
+// NPB > 0: the plain (not length-weighted) back-projection of at most
+// 2 NPB + 1 bins, whose per-voxel values are the same along the whole LOR
+// (value / voxel count, :108-110): they are formed once per LOR and held in
+// registers, and each voxel issues only its vector atomics.  NPB = 0: the
+// general form, which forms the values per voxel (the length-weighted span
+// fit, :294-297, and more than 17 bins).
+template <int NPB>
 __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
 {
     const long long n = (long long)(P.pairs ? P.npairs : P.nr * P.nr) * P.na * P.na;
@@ -295,6 +302,58 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     const float fn = (float)n_vox;
     const float ar = rv / fn;
     bool bad = false;
+    if constexpr (NPB > 0) {
+        // (P, S) of bin b from this LOR, divided by the voxel count, as below
+        auto contrib = [&](int b) {
+            const float s = P.nbins == 1 ? s0 : m * fit_scatter(P, b, cell, slice);
+            const float pv = P.nbins == 1 ? p0 : m * P.prompts[b * P.prompt_stride + c];
+            return make_float2(pv / fn, s / fn);
+        };
+        const int paired = P.nbins & ~1;
+        float4 cps[NPB], crs[NPB];
+        unsigned pm = 0;  // bin pairs with a bin this LOR contributes to
+#pragma unroll
+        for (int k = 0; k < NPB; ++k) {
+            cps[k] = crs[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (2 * k < paired) {
+                const bool in0 = (bins >> (2 * k)) & 1ull, in1 = (bins >> (2 * k + 1)) & 1ull;
+                const float2 c0 = in0 ? contrib(2 * k) : make_float2(0.f, 0.f);
+                const float2 c1 = in1 ? contrib(2 * k + 1) : make_float2(0.f, 0.f);
+                cps[k] = make_float4(c0.x, c0.y, c1.x, c1.y);
+                crs[k] = make_float4(in0 ? ar : 0.f, in0 ? 1.f : 0.f, in1 ? ar : 0.f, in1 ? 1.f : 0.f);
+                if (in0 || in1) pm |= 1u << k;
+            }
+        }
+        const int lastb = P.nbins - 1;
+        const bool has_last = (P.nbins & 1) && ((bins >> lastb) & 1ull);
+        const float2 clast = has_last ? contrib(lastb) : make_float2(0.f, 0.f);
+        const bool every = bins == all;
+        float2* last = reinterpret_cast<float2*>(P.img + (long long)lastb * 4 * P.nvox);
+        float2* common = reinterpret_cast<float2*>(P.img + (long long)P.nbins * 4 * P.nvox) + P.nvox;
+        const int walked = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double, double) {
+            const long long v = lin - 1;
+            if (v < 0 || v >= P.nvox) {
+                bad = true;
+                return;
+            }
+#pragma unroll
+            for (int k = 0; k < NPB; ++k) {
+                if ((pm >> k) & 1u) {
+                    float4* ps4 = reinterpret_cast<float4*>(P.img + (long long)(2 * k) * 4 * P.nvox);
+                    atomicAdd(ps4 + v, cps[k]);
+                    if (!every) atomicAdd(ps4 + P.nvox + v, crs[k]);  // randoms and sensitivity of these bins
+                }
+            }
+            if (has_last) {
+                atomicAdd(last + v, clast);
+                if (!every) atomicAdd(last + P.nvox + v, make_float2(ar, 1.0f));
+            }
+            if (every) atomicAdd(common + v, make_float2(ar, 1.0f));  // shared by every bin
+        });
+        if (bad) raise_error(P.status, kErrVoxel);
+        if (walked != n_vox) raise_error(P.status, kErrOverrun);
+        return;
+    }
     const int walked = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double t0, double t1) {
         const long long v = lin - 1;
         if (v < 0 || v >= P.nvox) {
@@ -560,7 +619,19 @@ int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, i
         return sss_set_error(SSS_ERR_CUDA, "sss_backproject_fit: memset failed");
     const long long n = (long long)(pairs ? npairs : nr * nr) * P.na * P.na;
     if (n > 0) {
-        bp_kernel<<<blocks_for(n, 128), 128, 0, st>>>(P);
+        const unsigned nb = blocks_for(n, 128);
+        if (length_weighted || nbins > 17)
+            bp_kernel<0><<<nb, 128, 0, st>>>(P);
+        else if (nbins <= 3)
+            bp_kernel<1><<<nb, 128, 0, st>>>(P);
+        else if (nbins <= 5)
+            bp_kernel<2><<<nb, 128, 0, st>>>(P);
+        else if (nbins <= 9)
+            bp_kernel<4><<<nb, 128, 0, st>>>(P);
+        else if (nbins <= 13)
+            bp_kernel<6><<<nb, 128, 0, st>>>(P);
+        else
+            bp_kernel<8><<<nb, 128, 0, st>>>(P);
         if ((rc = sss_check_launch("bp_kernel"))) return rc;
     }
     int dev = 0, sms = 0;

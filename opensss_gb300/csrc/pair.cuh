@@ -28,13 +28,15 @@ constexpr int kGRow = 68;
 
 // Shared memory of a pair block, in this order:
 //   ar    float2 [8001]  (A, r) of each TOF offset (factored weights; A carries
-//         the nearest bin n in its low mantissa bits) or (Y, 0)
+//         the nearest bin n in its low mantissa bits) or (Y, 0), then one
+//         entry (0, 0) at kZeroEntry (factored weights of exactly 0)
 //   n     u8     [8001]  bin of the column's largest weight
 //   vbuf  float2 [warps][32]  staged voxels of each warp's walk
 //   g     float  [nbins][kGRow]
 //   kahan float2 [2 NP][32 kKahanWarps]  (Kahan-compensated launches only,
 //         which run kKahanWarps warps so that 64 bins still fit)
-constexpr int kSmemNOff = (8 * kTofEntries + 15) & ~15;
+constexpr int kZeroEntry = kTofEntries;  // the (0, 0) entry after the table
+constexpr int kSmemNOff = (8 * (kTofEntries + 1) + 15) & ~15;
 constexpr int kSmemVbufOff = (kSmemNOff + kTofEntries + 15) & ~15;
 constexpr int kSmemGOff = kSmemVbufOff + 8 * 32 * kPairWarps;
 static_assert(kSmemGOff % 16 == 0, "shared-memory sections must be 16-byte aligned");
@@ -164,6 +166,7 @@ __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst&
             sAR[i] = make_float2(Y, 0.f);
         }
     }
+    if (threadIdx.x == 0) sAR[kZeroEntry] = make_float2(0.f, 0.f);
     if (T.factored)
         for (int i = threadIdx.x; i < T.nbins * kGRow; i += blockDim.x) {
             const int n = i / kGRow, b = i % kGRow;
@@ -238,14 +241,16 @@ __device__ __forceinline__ int table_offset(float x)
     return t < 0 ? t + kTofEntries : t;
 }
 
-// table_offset for the factored path: an offset at or past tsafe (far past
-// the last bin, or outside the table) is noted in far and replaced by 0.
-__device__ __forceinline__ int lookup_offset(float x, int tsafe, bool& ok, bool& far)
+// Offset index of the factored path's hot loop: floor(x) when it lies in
+// 0..tsafe-1, else kZeroEntry (weights 0) with the miss noted in far.  A
+// negative floor(x) counts as a miss here too; far_voxel then applies
+// numpy's wrap to it.
+__device__ __forceinline__ int lookup_offset(float x, int tsafe, bool& far)
 {
-    const int t = table_offset(x);
-    ok = (unsigned)t < (unsigned)tsafe;
+    const int t = __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
+    const bool ok = (unsigned)t < (unsigned)tsafe;
     far |= !ok;
-    return ok ? t : 0;
+    return ok ? t : kZeroEntry;
 }
 
 // Per-bin weights w_b = 2^(Y - d (beta + gamma d)), d = n - b, each on the
@@ -270,16 +275,24 @@ __device__ __forceinline__ void accumulate_per_bin(float2 (&acc)[NP], float ca, 
     }
 }
 
-// A voxel of the factored path whose table offset t is not below T.tsafe:
-// an offset far past the last bin takes the per-bin weights from its (Y, 0)
-// entry and its bin n; an offset outside the table is flagged and adds
-// nothing.  Runs only for such voxels.
+// A voxel the factored path's hot loop left out (floor(x) outside
+// 0..T.tsafe-1), at x: numpy's wrap of a negative index; a wrapped offset
+// below T.tsafe takes the factored weights, one far past the last bin the
+// per-bin weights from its (Y, 0) entry and its bin n, and one outside the
+// table is flagged and adds nothing.  Runs only for such voxels.
 template <int NP, bool ODD>
-__device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, int t, const float2* sAR,
-                                          const unsigned char* sN, const TofConst& T, bool& tof_bad)
+__device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, float x, const float2* sAR,
+                                          const unsigned char* sN, const float* sG, const TofConst& T,
+                                          bool& tof_bad)
 {
+    const int t = table_offset(x);
     if ((unsigned)t >= (unsigned)kTofEntries) {
         tof_bad = true;
+        return;
+    }
+    if (t < T.tsafe) {
+        const float2 ar = sAR[t];
+        accumulate_loaded<NP>(acc, ca, ar, __float_as_int(ar.x) & T.nmask, sG);
         return;
     }
     const float n = (float)sN[t];
@@ -438,33 +451,33 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                 if (c != 0.f) {
                     if (!SINGLE && T.factored) {
                         // the table lookup of voxel j+1 overlaps the accumulation of voxel j
-                        // (offsets at or past T.tsafe, far past the last bin or outside the
-                        // table, add nothing here; they are noted and taken afterwards)
+                        // (offsets outside 0..T.tsafe-1, far past the last bin, wrapped or
+                        // outside the table, add nothing here; they are noted and taken
+                        // afterwards)
                         bool anyfar = false;
                         float2 v = vbuf[0];
-                        bool ok;
-                        int t = lookup_offset(fmaf(sigma, v.y, u), T.tsafe, ok, anyfar);
+                        int t = lookup_offset(fmaf(sigma, v.y, u), T.tsafe, anyfar);
                         float2 ar = sAR[t];
                         int nb = __float_as_int(ar.x) & T.nmask;
-                        float ca = ok ? c * v.x : 0.f;
+                        float ca = c * v.x;
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
                             const float2 v1 = vbuf[j + 1 < jn ? j + 1 : j];
-                            bool ok1;
-                            const int t1 = lookup_offset(fmaf(sigma, v1.y, u), T.tsafe, ok1, anyfar);
+                            const int t1 = lookup_offset(fmaf(sigma, v1.y, u), T.tsafe, anyfar);
                             const float2 ar1 = sAR[t1];
                             const int nb1 = __float_as_int(ar1.x) & T.nmask;
                             accumulate_loaded<NP>(acc, ca, ar, nb, sG);
                             ar = ar1;
                             nb = nb1;
-                            ca = ok1 ? c * v1.x : 0.f;
+                            ca = c * v1.x;
                         }
-                        if (anyfar) {  // rare: per-bin weights for this batch's far voxels
+                        if (anyfar) {  // rare: this batch's voxels outside the factored range
                             for (int j = 0; j < jn; ++j) {
                                 const float2 vf = vbuf[j];
-                                const int tf = table_offset(fmaf(sigma, vf.y, u));
+                                const float xf = fmaf(sigma, vf.y, u);
+                                const int tf = __float_as_int(__fadd_rd(xf, 12582912.0f)) - 0x4B400000;
                                 if ((unsigned)tf >= (unsigned)T.tsafe)
-                                    far_voxel<NP, ODD>(acc, c * vf.x, tf, sAR, sN, T, tof_bad);
+                                    far_voxel<NP, ODD>(acc, c * vf.x, xf, sAR, sN, sG, T, tof_bad);
                             }
                         }
                     } else {
