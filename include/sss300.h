@@ -172,6 +172,18 @@ int sss_tof_run(const sss_tof_problem *p, const double *points, int64_t n_points
 int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
                     const int16_t *lor, const int32_t *detectors, float *dense, void *stream);
 
+/* The same dense layout, every element written (zeros included), so dense
+ * needs no clearing: for a fresh result array such as the one
+ * SingleScatterSimulationTOF returns (SingleScatterSimulationTOF.py:201-208).
+ * cell_pair (device int32 [(nd+1)*(nd/2)]) gives, per sinogram cell
+ * rad*(nd/2) + ang, the sampled crystal pair di1*ndu + di2 (di1 <= di2) whose
+ * LOR it is, or -1 (every entry below ndu*ndu, each pair in at most one cell).
+ * dense may be device memory or page-locked host memory (written over the
+ * host link at its device address); any other pointer is SSS_ERR_INVALID.
+ * Needs nru*nru a multiple of 4 and a 16-byte aligned dense. */
+int sss_tof_densify_full(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
+                         const int32_t *cell_pair, float *dense, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Batched simulation (no counterpart in the reference, which runs one
  * SingleScatterSimulationTOF call per problem).  sss_batch_plan enumerates the

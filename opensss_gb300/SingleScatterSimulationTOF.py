@@ -34,11 +34,16 @@ _lock = threading.Lock()
 class _DropIn:
     def __init__(self, eng: TofSSS, lor):
         self.engine = eng
-        lor = geometry.check_dense_lor(lor, eng.dets_np, eng.nd)
-        self.lor = as_device(np.asarray(lor, dtype=np.int16), torch.int16, eng.device)
-        # the reference layout; cells of unsampled pairs stay 0 across calls
-        self.dense = torch.zeros((eng.nbins, eng.nd + 1, eng.nd // 2, eng.nru * eng.nru),
-                                 dtype=torch.float32, device=eng.device)
+        self.full = (eng.nru * eng.nru) % 4 == 0
+        if self.full:
+            # every dense element is written straight into the page-locked result
+            self.cells = as_device(geometry.dense_cell_pairs(lor, eng.dets_np, eng.nd), torch.int32, eng.device)
+        else:
+            lor = geometry.check_dense_lor(lor, eng.dets_np, eng.nd)
+            self.lor = as_device(np.asarray(lor, dtype=np.int16), torch.int16, eng.device)
+            # the reference layout; cells of unsampled pairs stay 0 across calls
+            self.dense = torch.zeros((eng.nbins, eng.nd + 1, eng.nd // 2, eng.nru * eng.nru),
+                                     dtype=torch.float32, device=eng.device)
 
 
 def _key(arrays, scalars, device) -> bytes:
@@ -79,18 +84,24 @@ def SingleScatterSimulationTOF(ActivityMap, AttenuationMap, ImageSize, Geometry,
     """3D TOF single scatter simulation (Watson); see the module docstring.
 
     The result is a fresh float32 array the caller owns.  Its memory is
-    page-locked host memory from torch's pinned-memory cache, so that the
-    device-to-host copy runs at the link's full rate; it returns to the
-    cache when the array is dropped."""
+    page-locked host memory from torch's pinned-memory cache, which the GPU
+    writes directly, zeros included, over the host link (when NRU^2 is a
+    multiple of 4; else the dense array is built on the device and copied);
+    it returns to the cache when the array is dropped."""
     t0 = time.time()
     d = _drop_in(Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable,
                  EnergyResolution, EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution,
                  TOFRange, NrBins, device)
     eng = d.engine
     compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
-    eng.densify(compact, d.lor, out=d.dense)
-    host = torch.empty(tuple(d.dense.shape), dtype=torch.float32, pin_memory=True)
-    host.copy_(d.dense)
+    shape = (eng.nbins, eng.nd + 1, eng.nd // 2, eng.nru * eng.nru)
+    host = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+    if d.full:
+        eng.densify_full(compact, d.cells, host)
+        torch.cuda.current_stream(eng.device).synchronize()
+    else:
+        eng.densify(compact, d.lor, out=d.dense)
+        host.copy_(d.dense)
     dense = host.numpy()
     print("Time for SSS: {:.2f} seconds".format(time.time() - t0))
     if SavePath:

@@ -85,6 +85,7 @@ SIGNATURES = {
     "sss_tof_run": (C.c_int, [C.POINTER(TofProblem), _P, _I64, _P, _I64, _I64, _P, C.c_size_t,
                               _P, _P, _P]),
     "sss_tof_densify": (C.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _P, _P]),
+    "sss_tof_densify_full": (C.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _P]),
     "sss_batch_plan": (C.c_int, [C.POINTER(TofProblem), _I32, _P, _P, C.c_size_t, _P,
                                  C.POINTER(_P), _P]),
     "sss_batch_run": (C.c_int, [_P, _P]),

@@ -143,6 +143,37 @@ __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru
     dense[(((long long)b * (nd + 1) + rad) * nang + ang) * nsino + ri2 + ri1 * nru] = cmp[i];
 }
 
+// Every element of the dense layout in one pass, zeros included, four
+// slices (one 16-byte store) a thread: cell (rad, ang) holds sampled pair
+// cell_pair[cell] = di1 * ndu + di2 (di1 <= di2) or -1.  The destination
+// may be page-locked host memory, which the GPU writes over its host link.
+__global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, long long ncell,
+                                    const int32_t* __restrict__ cell_pair, float* __restrict__ dense)
+{
+    const int nl = nru * ndu, nsino = nru * nru;
+    const long long plane = (long long)nl * nl;
+    const long long total4 = (long long)nbins * ncell * nsino / 4;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total4;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long e = 4 * q;
+        const int sino = (int)(e % nsino);
+        const long long cell = (e / nsino) % ncell;
+        const int b = (int)(e / ((long long)nsino * ncell));
+        const int pair = __ldg(cell_pair + cell);
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (pair >= 0) {
+            const int di1 = pair / ndu, di2 = pair % ndu;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int s = sino + k, ri1 = s / nru, ri2 = s % nru;
+                if (di1 < di2 || ri1 != ri2)
+                    v[k] = __ldg(cmp + b * plane + (long long)(di1 * nru + ri1) * nl + di2 * nru + ri2);
+            }
+        }
+        reinterpret_cast<float4*>(dense)[q] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Optional stage timing (events recorded on the caller's stream).
@@ -457,6 +488,40 @@ extern "C" int sss_tof_densify(const float* compact, int32_t nbins, int32_t nru,
     densify_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         compact, nbins, nru, ndu, nd, lor, detectors, dense);
     return sss_check_launch("densify_kernel");
+}
+
+extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
+                                    const int32_t* cell_pair, float* dense, void* stream)
+{
+    if (!compact || !cell_pair || !dense || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
+        return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify_full: bad argument");
+    if ((nru * nru) % 4 != 0 || (uintptr_t)dense % 16 != 0)
+        return sss_set_error(SSS_ERR_INVALID,
+                             "sss_tof_densify_full: needs nru*nru a multiple of 4 and a 16-byte aligned output");
+    // the destination must be memory the device can address: device memory,
+    // or host memory page-locked through CUDA (written at its device address)
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, dense) != cudaSuccess) {
+        cudaGetLastError();
+        return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify_full: output pointer unknown to CUDA");
+    }
+    float* dst = nullptr;
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)
+        dst = dense;
+    else if (attr.type == cudaMemoryTypeHost && attr.devicePointer)
+        dst = (float*)attr.devicePointer;
+    else
+        return sss_set_error(SSS_ERR_INVALID,
+                             "sss_tof_densify_full: output must be device memory or page-locked host memory");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long ncell = (long long)(nd + 1) * (nd / 2);
+    const long long total4 = (long long)nbins * ncell * nru * nru / 4;
+    const long long want = (total4 + 255) / 256;
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
+    densify_full_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair, dst);
+    return sss_check_launch("densify_full_kernel");
 }
 
 // ---------------------------------------------------------------- no-allocation scatter points

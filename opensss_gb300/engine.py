@@ -225,6 +225,22 @@ class TofSSS:
         return self._ws
 
     # ------------------------------------------------------------------
+    def densify_full(self, compact: torch.Tensor, cell_pair: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+        """Leg-pair layout -> every element of the reference layout
+        [B, ND+1, ND//2, NRU^2] float32, zeros included, into ``out``: a CUDA
+        tensor or a page-locked host tensor (written by the GPU over the host
+        link, no separate copy).  ``cell_pair``: CUDA int32 table of
+        ``geometry.dense_cell_pairs``.  Asynchronous on the current stream."""
+        shape = (self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru)
+        if tuple(out.shape) != shape or out.dtype != torch.float32 or not out.is_contiguous():
+            raise ValueError(f"densify_full: out must be contiguous float32 {shape}")
+        if not (out.is_cuda or out.is_pinned()):
+            raise ValueError("densify_full: out must be a CUDA tensor or page-locked host memory")
+        st = torch.cuda.current_stream(self.device)
+        _lib.check(_lib.lib().sss_tof_densify_full(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd,
+                                                   _ptr(cell_pair), _ptr(out), C.c_void_p(st.cuda_stream)))
+        return out
+
     def densify(self, compact: torch.Tensor, lor, out: torch.Tensor | None = None) -> torch.Tensor:
         """Leg-pair layout -> reference layout [B, ND+1, ND//2, NRU^2] (CUDA).
 

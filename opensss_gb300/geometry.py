@@ -77,6 +77,24 @@ def check_dense_lor(lor, detectors, nd: int) -> np.ndarray:
     return lor
 
 
+def dense_cell_pairs(lor, detectors, nd: int) -> np.ndarray:
+    """int32 [(nd+1)*(nd/2)]: for each sinogram cell rad*(nd/2) + ang of the
+    dense layout, the sampled crystal pair di1*ndu + di2 (di1 <= di2) whose
+    LOR lies there, or -1 (the table sss_tof_densify_full reads).  The LOR
+    table is checked as for sss_tof_densify; two sampled pairs in one cell
+    (which the reference would add together) raise ValueError."""
+    lor = check_dense_lor(lor, detectors, nd)
+    d = np.asarray(detectors, dtype=np.int64)
+    ndu = len(d)
+    i1, i2 = np.triu_indices(ndu)
+    cells = lor[d[i1], d[i2], 1].astype(np.int64) * (nd // 2) + lor[d[i1], d[i2], 0]
+    if len(np.unique(cells)) != len(cells):
+        raise ValueError("two sampled crystal pairs share a sinogram cell")
+    out = np.full((nd + 1) * (nd // 2), -1, dtype=np.int32)
+    out[cells] = (i1 * ndu + i2).astype(np.int32)
+    return out
+
+
 def check_slice_table(SinogramIndex, nr: int) -> np.ndarray:
     """SinogramIndex[:nr, :nr] as the tail mask reads it on the device: every
     ring pair's slice in 0..nr^2-1, the mask's slice axis.  Raises IndexError

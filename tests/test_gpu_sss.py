@@ -365,3 +365,58 @@ def test_tof13_slice_matches_reference(cuda_ok, att_table):
     assert_same_support(got, ref)
     assert rel_l2(got, ref) < TOL
     np.testing.assert_allclose(flat.astype(np.float64).sum(axis=1), g["bin_totals"], rtol=TOL)
+
+
+def test_full_densify_to_device_and_pinned_host(cuda_ok, att_table):
+    """sss_tof_densify_full writes every element of the reference layout,
+    zeros included: into device memory and into page-locked host memory (the
+    GPU writes it over the host link) it equals the oracle's densify of the
+    same result; a pageable host pointer is refused before any launch."""
+    import ctypes as C
+
+    import torch
+
+    from opensss_gb300 import _lib, geometry as G
+    from opensss_gb300.engine import leg_pair_to_compact
+
+    g = golden("sss_tiny_b5")  # 4 sampled rings: 16 slices a cell
+    pr = problem_from_golden(g)
+    nd = pr.scanner.nr_detectors
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, pr.scanner.nr_rings, ID_Shidt=False)
+    eng = _engine(pr, att_table)
+    lp = eng.run(pr.activity, pr.attenuation, pr.image_size)
+    ref = O.densify(leg_pair_to_compact(lp.cpu().numpy(), pr.nr_rings_used, pr.nr_detectors_used), lor, nd,
+                    pr.nr_rings_used, pr.nr_detectors_used)
+    cells = torch.from_numpy(G.dense_cell_pairs(lor, eng.dets_np, nd)).cuda()
+    shape = (pr.nr_bins, nd + 1, nd // 2, pr.nr_rings_used ** 2)
+    for out in (torch.full(shape, 7.0, device="cuda"), torch.full(shape, 7.0).pin_memory()):
+        eng.densify_full(lp, cells, out)
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), ref.astype(np.float32))
+    pageable = np.zeros(shape, np.float32)
+    rc = _lib.lib().sss_tof_densify_full(C.c_void_p(lp.data_ptr()), pr.nr_bins, pr.nr_rings_used,
+                                         pr.nr_detectors_used, nd, C.c_void_p(cells.data_ptr()),
+                                         C.c_void_p(pageable.ctypes.data), None)
+    assert rc == 1 and "page-locked" in _lib.last_error()
+    assert not pageable.any()
+
+
+def test_dropin_full_dense_path(cuda_ok, att_table):
+    """The drop-in with NRU^2 a multiple of 4 writes its result straight into
+    page-locked host memory: same array as the oracle's densify."""
+    from opensss_gb300 import SingleScatterSimulationTOF
+    from opensss_gb300.geometry import SinogramCoordinates
+
+    g = golden("sss_tiny_b5")
+    pr = problem_from_golden(g)
+    lor, _, _ = SinogramCoordinates(1, 1, 1, 1, pr.scanner.nr_detectors, pr.scanner.nr_rings, ID_Shidt=False)
+    args = (pr.image_size, pr.scanner.geometry, lor, pr.scanner.normals, pr.scanner.detector_size_mm, att_table,
+            pr.energy_resolution, pr.energy_threshold, pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step,
+            pr.tof_resolution, pr.tof_range, pr.nr_bins, None)
+    out = SingleScatterSimulationTOF(pr.activity, pr.attenuation, *args)
+    ref = O.densify(g["compact"].astype(np.float64), lor, pr.scanner.nr_detectors, pr.nr_rings_used,
+                    pr.nr_detectors_used)
+    assert_same_support(out, ref)
+    assert rel_l2(out, ref) < TOL
+    out2 = SingleScatterSimulationTOF(pr.activity, pr.attenuation, *args)
+    assert not np.shares_memory(out, out2) and rel_l2(out2, out) < 1e-6

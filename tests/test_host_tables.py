@@ -373,3 +373,27 @@ def test_slice_table_check_accepts_reference_tables_and_rejects_bad_ones():
         t[2, 3] = v
         with pytest.raises(IndexError):
             G.check_slice_table(t, 6)
+
+
+@pytest.mark.parametrize("nd,nr,ndu,nru", [(48, 6, 8, 4), (64, 8, 10, 2), (760, 80, 48, 16)])
+def test_dense_cell_pairs_rebuild_the_dense_layout(nd, nr, ndu, nru):
+    """The cell table of the full densify, read the way its kernel reads it
+    (every element: the cell's pair, or zero), rebuilds the oracle's dense
+    layout of a random compact result exactly."""
+    from oracle import oracle as O
+
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
+    dets = G.sampled_detectors(nd, ndu)
+    cells = G.dense_cell_pairs(lor, dets, nd)
+    rng = np.random.default_rng(nd)
+    nb = 2
+    cmp = rng.random((nb, nru * nru, ndu, ndu))
+    for ri in range(nru):  # a crystal with itself on one ring is no pair: zero in every result
+        cmp[:, ri * nru + ri, np.arange(ndu), np.arange(ndu)] = 0.0
+    ref = O.densify(cmp, lor, nd, nru, ndu)
+    pair = cells.reshape(nd + 1, nd // 2)
+    di1, di2 = np.where(pair >= 0, pair // ndu, 0), np.where(pair >= 0, pair % ndu, 0)
+    ri1, ri2 = np.divmod(np.arange(nru * nru), nru)
+    valid = (pair >= 0)[:, :, None] & ((di1 < di2)[:, :, None] | (ri1 != ri2)[None, None, :])
+    got = cmp[:, (ri1 * nru + ri2)[None, None, :], di1[:, :, None], di2[:, :, None]] * valid[None]
+    assert np.array_equal(got.astype(np.float32), ref)
