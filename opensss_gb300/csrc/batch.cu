@@ -151,7 +151,7 @@ size_t item_bytes(const sss_tof_problem& p, long long npts)
     const long long nl = (long long)p.nru * p.ndu;
     const long long cap = (long long)p.nx + p.ny + p.nz;
     const size_t lists = (p.flags & SSS_FLAG_UNIT_TOF) ? 0 : align256(sizeof(float2) * npts * nl * cap);
-    return 2 * align256(sizeof(float4) * npts * nl) + lists;
+    return 3 * align256(sizeof(float4) * npts * nl) + lists;
 }
 
 }  // namespace
@@ -391,6 +391,8 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
             doff += align256(sizeof(float4) * it.count * nl);
             L.p.legB = (float4*)(ws + doff);
             doff += align256(sizeof(float4) * it.count * nl);
+            L.p.legC = (float4*)(ws + doff);
+            doff += align256(sizeof(float4) * it.count * nl);
             if (p.flags & SSS_FLAG_UNIT_TOF) {
                 L.p.vox = nullptr;  // every TOF weight is 1: the pairs use the leg integrals
             } else {
@@ -438,6 +440,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
                 C.points = hleg[j].p.points;
                 C.legA = hleg[j].p.legA;
                 C.legB = hleg[j].p.legB;
+                C.legC = hleg[j].p.legC;
                 C.vox = hleg[j].p.vox;
                 C.unit_tof = (p.flags & SSS_FLAG_UNIT_TOF) != 0;
                 C.out = outs[it.prob];

@@ -25,7 +25,8 @@ struct LegParams {
     const double* points;  // wave's first point, [n][4]
     int npts;
     float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
-    float4* legB;   // [npts][nl]: unit vector to the crystal, voxel-list length (int bits)
+    float4* legB;   // [npts][nl]: unit vector to the crystal (high floats), voxel-list length (int bits)
+    float4* legC;   // [npts][nl]: the unit vector's low floats (FP64 value = high + low), 0
     float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major; null: no lists
     int32_t* status;
 };
@@ -96,9 +97,18 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
     // exp(-I) underflows to 0 in FP64 above ~745.13 (the skip at :451 / :483)
     const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
     P.legA[o] = make_float4(sv, asum, ilog2, (float)(cosa / (vn * vn)));
-    const float inv = (float)(1.0 / vn);
-    P.legB[o] = make_float4((float)vx * inv, (float)vy * inv, (float)vz * inv,
-                            __int_as_float(nlist));
+    // the unit vector in FP64, kept as float pairs (high + low, about 48 bits)
+    // so that the pair stage can form the cosine between two legs to ~1e-14
+    const double inv = 1.0 / vn;
+    const double u[3] = {vx * inv, vy * inv, vz * inv};
+    float hi[3], lo[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        hi[k] = (float)u[k];
+        lo[k] = (float)(u[k] - (double)hi[k]);
+    }
+    P.legB[o] = make_float4(hi[0], hi[1], hi[2], __int_as_float(nlist));
+    P.legC[o] = make_float4(lo[0], lo[1], lo[2], 0.f);
 }
 
 }  // namespace sss

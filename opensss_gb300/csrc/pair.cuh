@@ -75,6 +75,7 @@ struct PairCtx {
     const double* points;    // scatter points the leg arrays are indexed by
     const float4* legA;      // [point][nl]
     const float4* legB;
+    const float4* legC;      // low floats of legB's unit vectors
     const float2* vox;       // [point][nl][cap]
     float* out;              // [nbins][nl][nl]
     int unit_tof;            // one bin, every TOF weight exactly 1: AB = the leg's activity integral
@@ -206,6 +207,42 @@ static __device__ __noinline__ int energy_row_fp64(const PairCtx& C, int s, int 
     // cos(deg2rad(180 - degrees(acos(q)))) is -q up to the round trip's rounding
     double es = floor(add64(div64(511.0, add64(1.0, add64(1.0, q))), 0.5));
     return (int)mul64(es, 2.0) - 1;
+}
+
+// Scattered-energy row of a pair from the two legs' unit vectors held as
+// float pairs (b + c, about 48 bits each), all in FP32: the cosine q between
+// the legs (= -cos of the scatter angle, :495, :498-499) as a float pair from
+// exact products (FMA residuals) and two-sums, d = 2 + q, e = 511 / d with
+// one residual correction, and the fraction of e + 0.5.  Its error is about
+// 1e-11 keV, the FP64 evaluation's (energy_row_fp64) about 1e-12, so the row
+// floor(e + 0.5) * 2 - 1 is decided here unless e + 0.5 lies within 1e-6 of
+// an integer or the legs are within 1e-6 of collinear (where the reference's
+// acos may leave its domain): then -2, and the FP64 evaluation decides.  qc:
+// q in FP32 for the Klein-Nishina factor.
+__device__ __forceinline__ int energy_row_pair(float4 bw, float4 cw, float4 bp, float4 cp, float& qc)
+{
+    const float p0 = bw.x * bp.x, p1 = bw.y * bp.y, p2 = bw.z * bp.z;
+    const float r = fmaf(bw.x, bp.x, -p0) + fmaf(bw.y, bp.y, -p1) + fmaf(bw.z, bp.z, -p2);
+    float s = p0 + p1, v = s - p0;
+    float t = (p0 - (s - v)) + (p1 - v);
+    const float s2 = s + p2;
+    v = s2 - s;
+    t += (s - (s2 - v)) + (p2 - v);
+    const float cross = fmaf(bw.x, cp.x, fmaf(cw.x, bp.x, fmaf(bw.y, cp.y, fmaf(cw.y, bp.y, fmaf(bw.z, cp.z, cw.z * bp.z)))));
+    const float ql = t + r + cross;  // q = s2 + ql
+    qc = fminf(1.f, fmaxf(-1.f, s2 + ql));
+    float dh = 2.f + s2;
+    v = dh - 2.f;
+    float dl = ((2.f - (dh - v)) + (s2 - v)) + ql;
+    const float d1 = dh + dl;
+    dl -= d1 - dh;
+    dh = d1;
+    const float y = __fdiv_rn(511.f, dh);
+    const float el = __fdividef(fmaf(-y, dh, 511.f) - y * dl, dh);  // e = y + el
+    const float n0 = floorf(y + 0.5f);
+    const float f = (y - (n0 - 0.5f)) + el;  // fraction of e + 0.5 (y - (n0 - 0.5) is exact)
+    if (!(f > 1e-6f && f < 1.f - 1e-6f) || fabsf(qc) > 1.f - 1e-6f) return -2;
+    return 2 * (int)n0 - 1;
 }
 
 // Factored weights of one voxel whose table entry is loaded: w_b =
@@ -393,26 +430,18 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
             for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);  // this point's partial
         }
         const long long lo = (long long)s * C.nl;
-        const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw];
-        const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp];
+        const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw], Cw = C.legC[lo + lw];
+        const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp], Cp = C.legC[lo + lp];
         // everything below but the TOF offset's sign is symmetric in the two legs
         bool ok = lane_ok && Aw.z != INFINITY && Ap.z != INFINITY && !(Aw.y == 0.f && Ap.y == 0.f);
         float c = 0.f;
         if (ok) {
             // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
-            float qc = fmaf(Bw.x, Bp.x, fmaf(Bw.y, Bp.y, Bw.z * Bp.z));
-            qc = fminf(1.f, fmaxf(-1.f, qc));
-            // scattered energy: the FP32 estimate is within 3e-4 keV of the FP64
-            // value (unit vectors rounded to FP32, a 2-ulp division), so the FP64
-            // row decides only within 1e-3 keV of a rounding boundary
-            const float e = __fdividef(511.0f, 2.0f + qc);
-            const float eh = e + 0.5f;
-            const float fr = eh - floorf(eh);
-            int row;
-            if (fr < 1e-3f || fr > 1.0f - 1e-3f)
-                row = energy_row_fp64(C, s, rw, dw, rp, dp);
-            else
-                row = 2 * (int)floorf(eh) - 1;
+            // and the scattered energy's row, in FP32 pairs; FP64 only next to a
+            // rounding boundary (about one pair in a million)
+            float qc;
+            int row = energy_row_pair(Bw, Cw, Bp, Cp, qc);
+            if (row == -2) row = energy_row_fp64(C, s, rw, dw, rp, dp);
             if (row < 0 || row >= 2000) {
                 energy_bad = true;
             } else {

@@ -199,7 +199,7 @@ struct StageTimer {
 thread_local StageTimer g_timer;
 
 struct WsLayout {
-    size_t legA, legB, vox, counter, total;
+    size_t legA, legB, legC, vox, counter, total;
 };
 
 WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
@@ -211,6 +211,8 @@ WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
     w.legA = off;
     off = align_up(off + sizeof(float4) * wave_points * nl);
     w.legB = off;
+    off = align_up(off + sizeof(float4) * wave_points * nl);
+    w.legC = off;
     off = align_up(off + sizeof(float4) * wave_points * nl);
     w.vox = off;  // no voxel lists when every TOF weight is 1
     if (!(p.flags & SSS_FLAG_UNIT_TOF)) off = align_up(off + sizeof(float2) * wave_points * cap * nl);
@@ -368,6 +370,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     LP.nvox = (long long)p->nx * p->ny * p->nz;
     LP.legA = (float4*)(ws + w.legA);
     LP.legB = (float4*)(ws + w.legB);
+    LP.legC = (float4*)(ws + w.legC);
     LP.vox = (p->flags & SSS_FLAG_UNIT_TOF) ? nullptr : (float2*)(ws + w.vox);
     LP.status = status;
 
@@ -388,6 +391,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     C.dets = p->detectors;
     C.legA = LP.legA;
     C.legB = LP.legB;
+    C.legC = LP.legC;
     C.vox = LP.vox;
     C.unit_tof = (p->flags & SSS_FLAG_UNIT_TOF) != 0;
     C.out = out;

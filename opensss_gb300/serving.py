@@ -85,7 +85,7 @@ def make_bed(engine: TofSSS, activity, attenuation, image_size, large: bool = Fa
     cap = sum(shape)
     n = int(counts.sum())
     return Bed(engine, mu, act, shape, np.asarray(image_size, dtype=np.float64), pts, counts,
-               n * pairs * engine.nbins, n * nl * (32 + 8 * cap), large)
+               n * pairs * engine.nbins, n * nl * (48 + 8 * cap), large)
 
 
 def request_activity(bed: Bed, seed: int) -> torch.Tensor:
