@@ -7,8 +7,8 @@
 // Measurement only: built into its own library (libsss300_probe.so), which
 // the benchmark loads; the engine library does not contain these kernels.
 // Each entry point returns 0 or the failing cudaError_t, synchronises
-// `stream` and writes its rate (GB/s, 1e9 results/s for 2^x and DADD,
-// GFLOP/s for FFMA2).
+// `stream` and writes its rate (GB/s, 1e9 results/s for 2^x, DADD and
+// DDIV, GFLOP/s for FFMA2).
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -60,6 +60,23 @@ __global__ void __launch_bounds__(256) dadd_probe_kernel(int iters, double* sink
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int c = 0; c < kChains; ++c) x[c] = __dadd_rn(x[c], 1e-3);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) s += x[c];
+    if (s == 123.456) sink[0] = s;
+}
+
+// FP64 divisions: independent chains of IEEE round-to-nearest DDIV (the
+// per-ray set-up of the ray walk holds fifteen of them).
+__global__ void __launch_bounds__(256) ddiv_probe_kernel(int iters, double* sink)
+{
+    double x[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) x[c] = 1.5 + 0.1 * (threadIdx.x & 7) + 0.01 * c;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kChains; ++c) x[c] = __ddiv_rn(x[c], 0.9999999);
     }
     double s = 0.0;
 #pragma unroll
@@ -247,5 +264,26 @@ extern "C" int sss_probe_dadd_rate(double* gadd_per_s, void* stream)
     cudaFreeAsync(sink, st);
     if (rc) return rc;
     *gadd_per_s = (double)blocks * threads * iters * kChains / (ms * 1e-3) / 1e9;
+    return 0;
+}
+
+extern "C" int sss_probe_ddiv_rate(double* gdiv_per_s, void* stream)
+{
+    if (!gdiv_per_s) return (int)cudaErrorInvalidValue;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 128;
+    double* sink = nullptr;
+    cudaError_t e = cudaMallocAsync(&sink, sizeof(double), st);
+    if (e != cudaSuccess) return (int)e;
+    float ms = 0.f;
+    int rc = time_probe(st, [&](bool warm) {
+        ddiv_probe_kernel<<<blocks, threads, 0, st>>>(warm ? iters / 8 : iters, sink);
+    }, &ms);
+    cudaFreeAsync(sink, st);
+    if (rc) return rc;
+    *gdiv_per_s = (double)blocks * threads * iters * kChains / (ms * 1e-3) / 1e9;
     return 0;
 }
