@@ -6,6 +6,8 @@
 // to the reference's.
 #pragma once
 
+#include <cstring>
+
 #include "common.cuh"
 
 namespace sss {
@@ -23,6 +25,7 @@ struct Grid {
     int nx, ny, nz;
     double b[6];   // xMin yMin zMin xMax yMax zMax
     double vs[3];  // voxel sizes (b[3+k] - b[k]) / n_k, set by grid_of (:80-82)
+    double ivs[3]; // 1 / vs[k], for quotients whose ceiling alone is needed
 };
 
 // A grid with its voxel sizes, computed once per launch with the reference's
@@ -36,7 +39,38 @@ __host__ __device__ inline Grid grid_of(int nx, int ny, int nz, const double* bo
     for (int k = 0; k < 6; ++k) g.b[k] = bounds[k];
     const double n[3] = {(double)nx, (double)ny, (double)nz};
     for (int k = 0; k < 3; ++k) g.vs[k] = (bounds[3 + k] - bounds[k]) / n[k];
+    for (int k = 0; k < 3; ++k) g.ivs[k] = 1.0 / g.vs[k];
     return g;
+}
+
+// ceil(RN(num / vs)) from q = RN(num * RN(1 / vs)) without the division:
+// q lies within 2.5 ulps of RN(num / vs), so where q is more than 4 ulps
+// from every integer the two have the same ceiling, read here from q's bits
+// (integer operations only).  Returns false, and leaves c alone, where q is
+// that close to an integer, above 2^52 in magnitude or not finite: the
+// caller then divides.
+__host__ __device__ inline bool ceil_clear(double q, long long& c)
+{
+    uint64_t b;
+    memcpy(&b, &q, 8);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    const bool neg = (b >> 63) != 0;
+    if (ex >= 1023 + 52) return false;  // |q| >= 2^52, infinite or NaN
+    if ((b << 1) == 0) {                // +-0: the quotient is 0 too (num == 0)
+        c = 0;
+        return true;
+    }
+    if (ex < 1022) {  // 0 < |q| < 0.5, the quotient has q's sign: ceil is 1 or 0
+        c = neg ? 0 : 1;
+        return true;
+    }
+    const int fb = 1023 + 52 - ex;  // fraction bits of q, 1..53
+    if (fb < 4) return false;
+    const uint64_t m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const uint64_t ip = m >> fb, fr = m & ((1ull << fb) - 1);
+    if (fr <= 4 || fr >= (1ull << fb) - 4) return false;
+    c = neg ? -(long long)ip : (long long)ip + 1;
+    return true;
 }
 
 // Parametric state of one ray after set-up.
@@ -94,21 +128,27 @@ __device__ __forceinline__ bool box_intersect(const Grid& g, const double* lc, d
 
 // Per-axis set-up (RayTracing3DTOF.py:77-123).  `start`/`end` are the grid
 // entry/exit coordinates, n the voxel count on the axis.
-__device__ __forceinline__ void axis_setup(double lo, double vs, double n, double v,
+// The first and last voxel on an axis: ceil((c - lo) / vs) clamped to 1..n
+// (:89-110).  The ceiling comes from a product with 1/vs where that decides
+// it (ceil_clear), else from the division; the clamp is the reference's
+// min/max pair (both orders give the same integer).
+__device__ __forceinline__ double voxel_of(double c, double lo, double vs, double ivs, int n, bool int_first)
+{
+    const double num = sub64(c, lo);
+    long long k;
+    if (ceil_clear(mul64(num, ivs), k)) return (double)(k < 1 ? 1 : (k > n ? n : k));
+    const double c0 = ceil(div64(num, vs)), nn = (double)n;
+    // z: int() before the clamp (RayTracing3DTOF.py:109-110)
+    return int_first ? pymin(pymax(1.0, c0), nn) : pymax(1.0, pymin(nn, c0));
+}
+
+__device__ __forceinline__ void axis_setup(double lo, double vs, double ivs, int n, double v,
                                            double start, double end, double tmin, double tmax,
                                            bool int_first, int& X, int& Xe, int& st, double& tn,
                                            double& td)
 {
-    double c0 = ceil(div64(sub64(start, lo), vs));
-    double c1 = ceil(div64(sub64(end, lo), vs));
-    double x, xe;
-    if (!int_first) {
-        x = pymax(1.0, pymin(n, c0));
-        xe = pymax(1.0, pymin(n, c1));
-    } else {  // z: int() before the clamp (RayTracing3DTOF.py:109-110)
-        x = pymin(pymax(1.0, c0), n);
-        xe = pymin(pymax(1.0, c1), n);
-    }
+    const double x = voxel_of(start, lo, vs, ivs, n, int_first);
+    const double xe = voxel_of(end, lo, vs, ivs, n, int_first);
     if (v > 0) {
         st = 1;
         td = div64(vs, v);
@@ -133,7 +173,6 @@ __device__ __forceinline__ bool ray_setup(const Grid& g, const double* lc, doubl
     if (!box_intersect(g, lc, eps, tmin, tmax)) return false;
     tmin = pymax(tmin, 0.0);
     tmax = pymin(tmax, 1.0);
-    const double nx = (double)g.nx, ny = (double)g.ny, nz = (double)g.nz;
     const double vx = g.vs[0], vy = g.vs[1], vz = g.vs[2];
     r.xv = sub64(lc[3], lc[0]);
     r.yv = sub64(lc[4], lc[1]);
@@ -142,9 +181,9 @@ __device__ __forceinline__ bool ray_setup(const Grid& g, const double* lc, doubl
            zs = add64(lc[2], mul64(r.zv, tmin));
     double xe = add64(lc[0], mul64(r.xv, tmax)), ye = add64(lc[1], mul64(r.yv, tmax)),
            ze = add64(lc[2], mul64(r.zv, tmax));
-    axis_setup(g.b[0], vx, nx, r.xv, xs, xe, tmin, tmax, false, r.X, r.xe, r.xs, r.xt, r.xd);
-    axis_setup(g.b[1], vy, ny, r.yv, ys, ye, tmin, tmax, false, r.Y, r.ye, r.ys, r.yt, r.yd);
-    axis_setup(g.b[2], vz, nz, r.zv, zs, ze, tmin, tmax, true, r.Z, r.ze, r.zs, r.zt, r.zd);
+    axis_setup(g.b[0], vx, g.ivs[0], g.nx, r.xv, xs, xe, tmin, tmax, false, r.X, r.xe, r.xs, r.xt, r.xd);
+    axis_setup(g.b[1], vy, g.ivs[1], g.ny, r.yv, ys, ye, tmin, tmax, false, r.Y, r.ye, r.ys, r.yt, r.yd);
+    axis_setup(g.b[2], vz, g.ivs[2], g.nz, r.zv, zs, ze, tmin, tmax, true, r.Z, r.ze, r.zs, r.zt, r.zd);
     r.tmin = tmin;
     r.tmax = tmax;
     return true;

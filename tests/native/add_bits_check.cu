@@ -1,9 +1,14 @@
-// Host-side check of sss::add_nonneg_bits (opensss_gb300/csrc/trace.cuh), the
-// integer-pipe FP64 addition of the ray walk: against the host's IEEE
-// binary64 addition (round to nearest even) on seeded random operands of
-// every kind the walk can meet -- equal and distant exponents, near-equal
-// values, subnormals, and running sums of walk-like steps.  Prints the
-// number of cases and of mismatches; exits non-zero on any mismatch.
+// Host-side checks of the ray walk's integer-pipe arithmetic
+// (opensss_gb300/csrc/trace.cuh):
+//  * sss::add_nonneg_bits against the host's IEEE binary64 addition (round
+//    to nearest even) on seeded random operands of every kind the walk can
+//    meet -- equal and distant exponents, near-equal values, subnormals, and
+//    running sums of walk-like steps;
+//  * sss::ceil_clear (the ceiling of a voxel quotient from a product with
+//    the reciprocal) against ceil of the host's division, on coordinates in
+//    and around grids of several voxel sizes, voxel faces included.
+// Prints the number of cases and of mismatches; exits non-zero on any.
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -81,6 +86,37 @@ int main(int argc, char** argv)
             t = t + d;
         }
     }
+    // voxel quotients: ceil((c - lo) / vs) for coordinates on and around the
+    // voxel faces of grids with awkward voxel sizes
+    long long deferred = 0, ceils = 0;
+    const double sizes[] = {0.6, 0.4, 1.0, 2.0 / 3.0, 40.0 / 37.0, 0.15625, 3.1, 51.0 / 17.0};
+    std::uniform_int_distribution<int> face(-3, 140);
+    std::uniform_real_distribution<double> jitter(-1e-9, 1e-9), any(-60.0, 60.0);
+    for (double vs : sizes) {
+        const double lo = -vs * 64.0, inv = 1.0 / vs;
+        for (int i = 0; i < 400000; ++i) {
+            double c;
+            switch (i % 4) {
+            case 0: c = lo + face(rng) * vs; break;                              // on a face
+            case 1: c = (face(rng) + 1) * 2 * (vs * 32.0) / 64.0 - vs * 32.0; break; // scatter-point form
+            case 2: c = lo + face(rng) * vs + jitter(rng); break;                // next to a face
+            default: c = any(rng); break;
+            }
+            const double num = c - lo;
+            long long k = 0;
+            ++ceils;
+            if (!sss::ceil_clear(num * inv, k)) {
+                ++deferred;
+                continue;
+            }
+            if ((double)k != std::ceil(num / vs)) {
+                if (bad < 8) std::printf("ceil mismatch vs=%.17g c=%.17g: %lld, division %.17g\n", vs, c, k,
+                                         std::ceil(num / vs));
+                ++bad;
+            }
+        }
+    }
+    std::printf("ceilings %lld, deferred to the division %lld\n", ceils, deferred);
     std::printf("checked %ld, mismatches %ld\n", checked, bad);
     return bad != 0;
 }
