@@ -31,6 +31,27 @@ struct LegParams {
     int32_t* status;
 };
 
+// A unit-vector component u (|u| <= 1) as a float pair hi + lo: hi is u
+// truncated to 24 significant bits, lo the float nearest the remaining bits
+// (about 48 bits together), formed from u's bit pattern with integer
+// operations.  Components below 2^-74 in magnitude keep hi only.
+__device__ __forceinline__ void split_float_pair(double u, float& hi, float& lo)
+{
+    const uint64_t b = dbits(u);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    const uint32_t sign = (uint32_t)(b >> 63) << 31;
+    if (e < 1023 - 126) {  // |u| < 2^-126: below the float normal range, negligible here
+        hi = 0.f;
+        lo = 0.f;
+        return;
+    }
+    const uint64_t m = b & ((1ull << 52) - 1);
+    hi = __uint_as_float(sign | ((e - 1023 + 127) << 23) | (uint32_t)(m >> 29));
+    const uint32_t low = (uint32_t)(m & ((1u << 29) - 1));  // value low * 2^(e - 1075)
+    lo = e >= 949 ? __uint_as_float(sign | 0x3F800000u) * (float)low * __uint_as_float((e - 1075 + 127) << 23)
+                  : 0.f;
+}
+
 // One leg: scatter point s to sampled crystal leg l.
 __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
 {
@@ -41,19 +62,26 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
     const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
     double lc[6] = {xS, yS, zS, dp[0], dp[1], zD};
 
-    // incidence angle term |cos a| (:424-430, :533-535) and distance (:442-444)
+    // distance (:442-444) and the unit vector to the crystal in FP64; the
+    // unit vector is kept as float pairs for the pair stage's energy row
     const double vx = dp[0] - xS, vy = dp[1] - yS, vz = zD - zS;
-    const double* nv = P.normals + 3 * ((long long)ring * P.nd + det);
     const double vn = sqrt(vx * vx + vy * vy + vz * vz);
-    const double nn = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-    const double cosa = fabs((vx * nv[0] + vy * nv[1] + vz * nv[2]) / (nn * vn));
+    const double inv = 1.0 / vn;
+    float hi[3], lo[3];
+    split_float_pair(vx * inv, hi[0], lo[0]);
+    split_float_pair(vy * inv, hi[1], lo[1]);
+    split_float_pair(vz * inv, hi[2], lo[2]);
+    // incidence term |cos a| / sv^2 (:424-430, :533-535), in FP32: it only
+    // scales the pair's term (relative error ~1e-7)
+    const double* nv = P.normals + 3 * ((long long)ring * P.nd + det);
+    const float nx = (float)nv[0], ny = (float)nv[1], nz = (float)nv[2];
+    const float cosa = fabsf(fmaf(hi[0], nx, fmaf(hi[1], ny, hi[2] * nz))) * rsqrtf(fmaf(nx, nx, fmaf(ny, ny, nz * nz)));
     const float sv = (float)vn;
-
     float asum = 0.f, musum = 0.f;
     int nlist = 0;
     Ray r;
     if (ray_setup(P.g, lc, 1e-20, r)) {
-        const float vlen = (float)sqrt(r.xv * r.xv + r.yv * r.yv + r.zv * r.zv);
+        const float vlen = sv;  // |end - start|: the ray's direction is the leg vector itself
         const float inv_c = (float)(1.0 / kLightCmPerPs);
         const double t0 = r.tmin;
         // parameter gaps in fixed point (exact differences, no FP64 subtraction)
@@ -96,17 +124,7 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
     const long long o = (long long)s * P.nl + l;
     // exp(-I) underflows to 0 in FP64 above ~745.13 (the skip at :451 / :483)
     const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
-    P.legA[o] = make_float4(sv, asum, ilog2, (float)(cosa / (vn * vn)));
-    // the unit vector in FP64, kept as float pairs (high + low, about 48 bits)
-    // so that the pair stage can form the cosine between two legs to ~1e-14
-    const double inv = 1.0 / vn;
-    const double u[3] = {vx * inv, vy * inv, vz * inv};
-    float hi[3], lo[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        hi[k] = (float)u[k];
-        lo[k] = (float)(u[k] - (double)hi[k]);
-    }
+    P.legA[o] = make_float4(sv, asum, ilog2, cosa / (sv * sv));
     P.legB[o] = make_float4(hi[0], hi[1], hi[2], __int_as_float(nlist));
     P.legC[o] = make_float4(lo[0], lo[1], lo[2], 0.f);
 }
