@@ -64,9 +64,16 @@ __global__ void __launch_bounds__(pair_block_warps(NP, false) * 32, MINB)
     unsigned char* sN = smem + kSmemNOff;
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufOff) + (threadIdx.x >> 5) * 32;
     float* sG = reinterpret_cast<float*>(smem + kSmemGOff);
+    // each warp's current item, copied from global memory when the warp moves
+    // to another item, so that the task reads its problem's constants and
+    // pointers from shared memory
+    __shared__ PairItem witem[pair_block_warps(NP, false)];
+    static_assert(sizeof(PairItem) % 4 == 0, "items are copied as words");
     load_pair_tables(tof_log2w, T, sAR, sN, sG);
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    PairItem& it = witem[threadIdx.x >> 5];
+    int cur = -1;
     bool tof_bad = false, energy_bad = false, nonfinite = false;
     unsigned long long walked = 0, npairs = 0;
     for (;;) {
@@ -80,7 +87,14 @@ __global__ void __launch_bounds__(pair_block_warps(NP, false) * 32, MINB)
             if (items[mid].task_begin <= task) lo = mid;
             else hi = mid - 1;
         }
-        const PairItem& it = items[lo];
+        if (lo != cur) {  // warp-uniform: every lane found the same item
+            __syncwarp();
+            const int* src = reinterpret_cast<const int*>(items + lo);
+            int* dst = reinterpret_cast<int*>(&it);
+            for (int w = lane; w < (int)(sizeof(PairItem) / 4); w += 32) dst[w] = __ldg(src + w);
+            __syncwarp();
+            cur = lo;
+        }
         const int rem = (int)(task - it.task_begin);
         walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sAR,
                                           sN, sG, vbuf, nullptr, tof_bad, energy_bad, nonfinite, walked, npairs);
