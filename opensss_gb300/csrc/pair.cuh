@@ -261,13 +261,10 @@ __device__ __forceinline__ void accumulate_loaded(float2 (&acc)[NP], float ca, f
     P2.y = P2.x * ar.y;
     const float r2 = ar.y * ar.y;
     const float2 R2 = make_float2(r2, r2);
-    const float4* G4 = reinterpret_cast<const float4*>(sG + nb * kGRow);
-    float4 g4;
+    const float2* G2 = reinterpret_cast<const float2*>(sG + nb * kGRow);
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
-        if ((k & 1) == 0) g4 = G4[k >> 1];
-        const float2 g2 = (k & 1) ? make_float2(g4.z, g4.w) : make_float2(g4.x, g4.y);
-        acc[k] = __ffma2_rn(P2, g2, acc[k]);
+        acc[k] = __ffma2_rn(P2, G2[k], acc[k]);
         if (k + 1 < NP) P2 = __fmul2_rn(P2, R2);
     }
 }
