@@ -66,7 +66,7 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
     // unit vector is kept as float pairs for the pair stage's energy row
     const double vx = dp[0] - xS, vy = dp[1] - yS, vz = zD - zS;
     const double vn = sqrt(vx * vx + vy * vy + vz * vz);
-    const double inv = 1.0 / vn;
+    const double inv = div64(1.0, vn);
     float hi[3], lo[3];
     split_float_pair(vx * inv, hi[0], lo[0]);
     split_float_pair(vy * inv, hi[1], lo[1]);

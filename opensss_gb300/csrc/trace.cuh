@@ -15,7 +15,10 @@ namespace sss {
 __device__ __forceinline__ double mul64(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add64(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub64(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double div64(double a, double b) { return __ddiv_rn(a, b); }
+// FP64 division, round to nearest: on the integer pipe where div_bits takes
+// the operands (normal values with a normal or zero quotient), else __ddiv_rn;
+// the same IEEE result either way.
+__device__ __forceinline__ double div64(double a, double b);
 // Python's built-in min/max: the first argument wins unless the second
 // compares strictly smaller / larger (RayTracing3DTOF.py:53-54, 77-78).
 __device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b : a; }
@@ -235,8 +238,96 @@ __host__ __device__ __forceinline__ uint64_t add_nonneg_bits(uint64_t a, uint64_
     return ((uint64_t)(e - 1) << 52) + m;
 }
 
+// High 64 bits of a 64 x 64-bit product.
+__host__ __device__ inline uint64_t mulhi64(uint64_t a, uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// IEEE-754 binary64 division, round to nearest even, with integer
+// operations only, for normal (or zero) dividends and normal divisors whose
+// quotient is a normal double or zero; returns false (leaving q alone) for any
+// other operands, which the caller divides in FP64.  Written from the
+// format's definition: with significands ma, mb (hidden bit restored, ma
+// doubled when below mb so that ma/mb lies in [1, 2)), the quotient's 56
+// leading bits are floor(ma 2^55 / mb).  They come from a reciprocal
+// R ~ 2^116 / mb held below its true value: a float seed with a margin, then
+// two Newton steps in 128-bit fixed point (each stays below and squares the
+// error), then q = floor(ma R / 2^61), at most two short, and the exact
+// remainder ma 2^55 - q mb corrects it.  The three extra bits and whether
+// the remainder is zero give round to nearest, ties to even.
+__host__ __device__ inline bool div_bits(uint64_t a, uint64_t b, uint64_t& q)
+{
+    constexpr uint64_t kFrac = (1ull << 52) - 1, kHid = 1ull << 52;
+    const uint32_t ea = (uint32_t)(a >> 52) & 0x7FFu, eb = (uint32_t)(b >> 52) & 0x7FFu;
+    const uint64_t sign = (a ^ b) & (1ull << 63);
+    if (eb == 0 || eb == 0x7FFu || ea == 0x7FFu) return false;  // zero, subnormal, inf or NaN divisor
+    if (ea == 0) {
+        if ((a & ~(1ull << 63)) != 0) return false;  // subnormal dividend
+        q = sign;                                    // zero: a signed zero
+        return true;
+    }
+    uint64_t ma = (a & kFrac) | kHid;
+    const uint64_t mb = (b & kFrac) | kHid;
+    int e = (int)ea - (int)eb + 1023;
+    if (ma < mb) {
+        ma <<= 1;
+        e -= 1;
+    }
+    if (e < 1 || e > 2046) return false;  // the quotient is not a normal double
+    uint64_t quo, rem;
+    if (mb == kHid) {  // a power of two: exact
+        quo = ma << 3;
+        rem = 0;
+    } else {
+        // seed: 2^87 / (mb >> 29) in float, as 2^64-scaled fixed point, minus a
+        // margin above its relative error (< 2^-22.5)
+        const float rf = 1.0f / (float)(uint32_t)(mb >> 29);  // in (2^-24, 2^-23]
+        uint32_t rbits;
+        memcpy(&rbits, &rf, 4);
+        uint64_t R = ((rbits >> 23) & 0xFFu) >= 127u - 23u ? ~0ull : ((uint64_t)((rbits & 0x7FFFFFu) | 0x800000u) << 40);
+        R -= 1ull << 42;
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+            // E = 2^116 - mb R > 0 (R is below 2^116 / mb); R += floor(R E / 2^116)
+            const uint64_t plo = mb * R, phi = mulhi64(mb, R);
+            const uint64_t elo = 0 - plo, ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);
+            const uint64_t t_lo = R * ehi, t_hi = mulhi64(R, ehi);  // R ehi, below 2^96
+            const uint64_t add = mulhi64(R, elo);
+            const uint64_t s_lo = t_lo + add;
+            const uint64_t s_hi = t_hi + (s_lo < t_lo ? 1ull : 0ull);
+            R += (s_hi << 12) | (s_lo >> 52);
+        }
+        const uint64_t plo = ma * R, phi = mulhi64(ma, R);
+        quo = (phi << 3) | (plo >> 61);
+        rem = (ma << 55) - quo * mb;  // exact: the true remainder lies in [0, 3 mb)
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+            if (rem >= mb) {
+                rem -= mb;
+                quo += 1;
+            }
+        }
+    }
+    uint64_t m = quo >> 3;
+    const uint32_t g = (uint32_t)(quo & 7u);
+    m += (uint64_t)(g > 4u || (g == 4u && (rem != 0 || (m & 1))));
+    q = sign | (((uint64_t)(e - 1) << 52) + m);
+    return true;
+}
+
 __device__ __forceinline__ uint64_t dbits(double x) { return (uint64_t)__double_as_longlong(x); }
 __device__ __forceinline__ double bitsd(uint64_t b) { return __longlong_as_double((long long)b); }
+
+__device__ __forceinline__ double div64(double a, double b)
+{
+    uint64_t q;
+    return div_bits(dbits(a), dbits(b), q) ? bitsd(q) : __ddiv_rn(a, b);
+}
 
 // Fixed-point form of a walk parameter, in units of 2^-61, for |t| < 4
 // (fix61_ok): exact for |t| >= 2^-8 and truncated below, an absolute error

@@ -6,7 +6,10 @@
 //    running sums of walk-like steps;
 //  * sss::ceil_clear (the ceiling of a voxel quotient from a product with
 //    the reciprocal) against ceil of the host's division, on coordinates in
-//    and around grids of several voxel sizes, voxel faces included.
+//    and around grids of several voxel sizes, voxel faces included;
+//  * sss::div_bits against the host's IEEE binary64 division: operands of
+//    random exponents and signs, one binade, near-equal significands,
+//    divisors with trailing zero bits, exact quotients and zero dividends.
 // Prints the number of cases and of mismatches; exits non-zero on any.
 #include <cmath>
 #include <cstdint>
@@ -117,6 +120,57 @@ int main(int argc, char** argv)
         }
     }
     std::printf("ceilings %lld, deferred to the division %lld\n", ceils, deferred);
+    // divisions
+    long long divs = 0, div_deferred = 0;
+    auto check_div = [&](double x, double y) {
+        uint64_t q = 0;
+        if (!sss::div_bits(bits_of(x), bits_of(y), q)) {
+            ++div_deferred;
+            return;
+        }
+        ++divs;
+        if (q != bits_of(x / y)) {
+            if (bad < 8) std::printf("div mismatch %.17g / %.17g: %.17g, IEEE %.17g\n", x, y, double_of(q), x / y);
+            ++bad;
+        }
+    };
+    std::uniform_real_distribution<double> wide(-100.0, 100.0), unit(0.1, 10.0);
+    for (long i = 0; i < cases; ++i) {
+        uint64_t x = rng(), y = rng();
+        switch (i % 5) {
+        case 0:  // exponents over a wide range, any signs
+            x = (x & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(900 + rng() % 300) << 52);
+            y = (y & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(900 + rng() % 300) << 52);
+            break;
+        case 1:  // one binade
+            x = (x & 0x800FFFFFFFFFFFFFull) | (1023ull << 52);
+            y = (y & 0x800FFFFFFFFFFFFFull) | (1023ull << 52);
+            break;
+        case 2:  // near-equal significands
+            y = (y & 0x800FFFFFFFFFFFFFull) | (1023ull << 52);
+            x = ((y & kFrac) + rng() % 7 - 3) | (1023ull << 52);
+            break;
+        case 3: {  // set-up-like operands
+            const double a = wide(rng), b = wide(rng);
+            check_div(a, b);
+            check_div(1.0, b);
+            check_div(0.6, b);
+            continue;
+        }
+        default:  // divisors with trailing zero bits
+            y = ((y & kFrac) | (1023ull << 52)) & ~((1ull << (rng() % 50)) - 1);
+            x = (x & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1000 + rng() % 40) << 52);
+            break;
+        }
+        check_div(double_of(x), double_of(y));
+    }
+    for (int i = 0; i < 200000; ++i) {  // exact quotients and zero dividends
+        const double y = unit(rng), k = (double)(rng() % 1000);
+        check_div(k * y, y);
+        check_div(0.0, y);
+        check_div(-0.0, y);
+    }
+    std::printf("divisions %lld, deferred to FP64 %lld\n", divs, div_deferred);
     std::printf("checked %ld, mismatches %ld\n", checked, bad);
     return bad != 0;
 }
