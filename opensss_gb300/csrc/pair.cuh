@@ -431,18 +431,30 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
             for (int k = 0; k < NP; ++k) acc[k] = make_float2(0.f, 0.f);  // this point's partial
         }
         const long long lo = (long long)s * C.nl;
-        const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw], Cw = C.legC[lo + lw];
-        const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp], Cp = C.legC[lo + lp];
+        const float4 Aw = C.legA[lo + lw], Bw = C.legB[lo + lw];
+        const float4 Ap = C.legA[lo + lp], Bp = C.legB[lo + lp];
         // everything below but the TOF offset's sign is symmetric in the two legs
         bool ok = lane_ok && Aw.z != INFINITY && Ap.z != INFINITY && !(Aw.y == 0.f && Ap.y == 0.f);
         float c = 0.f;
         if (ok) {
             // cos of the angle between the legs = -cos(scatter angle) (:495, :498-499)
-            // and the scattered energy's row, in FP32 pairs; FP64 only next to a
-            // rounding boundary (about one pair in a million)
-            float qc;
-            int row = energy_row_pair(Bw, Cw, Bp, Cp, qc);
-            if (row == -2) row = energy_row_fp64(C, s, rw, dw, rp, dp);
+            // and the scattered energy's row.  In FP32 from the legs' high floats
+            // the energy is within 3e-4 keV of the FP64 value, which decides the
+            // row except within 1e-3 keV of a rounding boundary (one pair in 500):
+            // there the float pairs decide it, and FP64 only within 1e-6 keV (about
+            // one pair in a million).
+            float qc = fmaf(Bw.x, Bp.x, fmaf(Bw.y, Bp.y, Bw.z * Bp.z));
+            qc = fminf(1.f, fmaxf(-1.f, qc));
+            const float e = __fdividef(511.0f, 2.0f + qc);
+            const float eh = e + 0.5f;
+            const float fr = eh - floorf(eh);
+            int row;
+            if (fr < 1e-3f || fr > 1.0f - 1e-3f || fabsf(qc) > 1.0f - 1e-5f) {
+                row = energy_row_pair(Bw, C.legC[lo + lw], Bp, C.legC[lo + lp], qc);
+                if (row == -2) row = energy_row_fp64(C, s, rw, dw, rp, dp);
+            } else {
+                row = 2 * (int)floorf(eh) - 1;
+            }
             if (row < 0 || row >= 2000) {
                 energy_bad = true;
             } else {

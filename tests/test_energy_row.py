@@ -1,9 +1,10 @@
-"""The pair kernel's scattered-energy row in FP32 pairs (``energy_row_pair``
-in ``opensss_gb300/csrc/pair.cuh``), emulated in numpy float32, against the
-reference's FP64 evaluation (law of cosines, ``SingleScatterSimulationTOF.py
-:442-444, :216-235, :495-501``) on seeded legs of the 760-crystal ring: every
-row it decides equals the FP64 row, and it defers to FP64 for about one pair
-in a million."""
+"""The pair kernel's scattered-energy row (``walk_task`` and
+``energy_row_pair`` in ``opensss_gb300/csrc/pair.cuh``), emulated in numpy
+float32, against the reference's FP64 evaluation (law of cosines,
+``SingleScatterSimulationTOF.py:442-444, :216-235, :495-501``) on seeded legs of
+the 760-crystal ring: every row the FP32 stage or the float-pair stage
+decides equals the FP64 row; the FP32 stage leaves about one pair in 500 to
+the float pairs, and they defer to FP64 for about one in a million."""
 
 import numpy as np
 
@@ -50,6 +51,20 @@ def _row_pair(bw, cw, bp, cp):
     return np.where(defer, -2, 2 * n0.astype(np.int64) - 1), y.astype(np.float64) + el.astype(np.float64)
 
 
+def _row_fp32(b1, b2):
+    """The first stage of the kernel's row: FP32 from the legs' high floats,
+    undecided (-3) within 1e-3 keV of a rounding boundary or near collinear
+    legs (the hardware's fast division is within 2 ulps of this one)."""
+    with np.errstate(all="ignore"):
+        qc = _fma(b1[:, 0], b2[:, 0], _fma(b1[:, 1], b2[:, 1], b1[:, 2] * b2[:, 2]))
+        qc = np.clip(qc, F(-1), F(1))
+        e = (np.float64(511) / (F(2) + qc).astype(np.float64)).astype(F)
+        eh = e + F(0.5)
+        fr = eh - np.floor(eh)
+        undecided = (fr < F(1e-3)) | (fr > F(1) - F(1e-3)) | (np.abs(qc) > F(1) - F(1e-5))
+    return np.where(undecided, -3, 2 * np.floor(eh).astype(np.int64) - 1)
+
+
 def test_fp32_pair_row_matches_fp64_row():
     rng = np.random.default_rng(5)
     n = 400_000
@@ -75,3 +90,9 @@ def test_fp32_pair_row_matches_fp64_row():
     # the float-pair energy is within 1e-8 keV of the FP64 one: a hundredth of
     # the 1e-6 band inside which the kernel defers to FP64
     assert np.abs(e - 511 / (2 + q))[ok].max() < 1e-8
+    # the kernel's first stage, FP32 from the high floats: every row it decides
+    # is the FP64 row, and it leaves about one pair in 500 to the float pairs
+    first = _row_fp32(b1, b2)
+    decided32 = (first != -3) & ok
+    assert np.array_equal(first[decided32], ref[decided32])
+    assert (first[ok] == -3).mean() < 5e-3
