@@ -41,7 +41,7 @@ import torch
 
 from . import _lib
 from .batch import BatchSSS
-from .engine import TofSSS, fortran_flat
+from .engine import WS_BUDGET_BYTES, TofSSS, fortran_flat
 
 
 @dataclasses.dataclass
@@ -125,7 +125,7 @@ class _Batch:
 
 class ScatterServer:
     def __init__(self, beds: list[Bed], hbm_budget: int = 80 << 30, depth: int = 2,
-                 large_workspace: int = 16 << 30, max_small_batch: int = 64):
+                 large_workspace: int = WS_BUDGET_BYTES, max_small_batch: int = 64):
         self.beds = beds
         self.dev = beds[0].engine.device
         self.budget = int(hbm_budget)
