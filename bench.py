@@ -880,13 +880,13 @@ def run_listmode(dev, args):
 
     import torch
 
-    from opensss_gb300 import Coincidence, Datafile, geometry as G, workloads as W
+    from opensss_gb300 import Coincidence, Datafile, DataReduction as D, geometry as G, workloads as W
 
     n = args.listmode_events
     header = W.listmode_header("bench_df", n)
     ev = W.synthetic_events(header, 760, 80, seed=2026)
     lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, 80, ID_Shidt=False)
-    _, _, lut, _ = G.SinogramLUT(80, 19, 79)
+    _, _, lut, _ = D.SinogramLUT(80, 19, 79)
     raw = torch.from_numpy(ev.view(np.uint8).reshape(-1))
     ev_h = raw.pin_memory()
     ev_d = ev_h.to(dev)
@@ -1043,13 +1043,13 @@ def case_listmode(reps):
     """10M list-mode events into the demo's reduced sinogram (mash 2, span 19)."""
     import torch  # noqa: F401
 
-    from opensss_gb300 import geometry as G, workloads as W  # noqa: F401
+    from opensss_gb300 import DataReduction as D, geometry as G, workloads as W  # noqa: F401
     from opensss_gb300.Datafile import histogram_device
 
     header = W.listmode_header("p_df", 10_000_000)
     ev = torch.from_numpy(W.synthetic_events(header, 760, 80, seed=1).view(np.uint8).reshape(-1)).cuda()
     lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, 80, ID_Shidt=False)
-    _, _, lut, _ = G.SinogramLUT(80, 19, 79)
+    _, _, lut, _ = D.SinogramLUT(80, 19, 79)
     for _ in range(reps):
         histogram_device(ev, header, lor, lut, 6, 1000.0, mash=2)
 

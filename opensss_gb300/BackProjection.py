@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from . import _lib, geometry
+from . import DataReduction, _lib
 from .engine import as_device
 
 
@@ -37,7 +37,7 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
     g = as_device(geom, torch.float64, device)
     lor = as_device(np.asarray(SinogramCoordinates, dtype=np.int16), torch.int16, device)
     if span:
-        pairs_np = geometry.span_ring_pairs(SinogramOrder)
+        pairs_np = DataReduction.span_ring_pairs(SinogramOrder)
         pairs = as_device(pairs_np, torch.int32, device)
     else:
         order = as_device(np.asarray(SinogramOrder, dtype=np.int16)[:nr, :nr], torch.int16, device)
@@ -91,7 +91,7 @@ def fit_bins_device(prompts, randoms, mask, scatters, scat_stride: int, scat_cel
     order = pairs = None
     npairs = nslices = 0
     if span:
-        pairs_np = geometry.span_ring_pairs(SinogramOrder)
+        pairs_np = DataReduction.span_ring_pairs(SinogramOrder)
         pairs = as_device(pairs_np, torch.int32, device)
         npairs = nslices = pairs_np.shape[0]
     else:

@@ -17,7 +17,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib, geometry
+from . import DataReduction, _lib, geometry
 from .engine import as_device, fortran_flat
 
 
@@ -49,7 +49,7 @@ def tail_mask_device(volume, ImageSize, Geometry, SinogramCoordinates, SinogramI
     bounds = np.ascontiguousarray(np.asarray(ImageSize, dtype=np.float64).reshape(-1)[:6])
     st = torch.cuda.current_stream(device)
     if span:
-        pairs_np = geometry.span_ring_pairs(SinogramIndex)
+        pairs_np = DataReduction.span_ring_pairs(SinogramIndex)
         nslices = pairs_np.shape[0]
         pairs = as_device(pairs_np, torch.int32, device)
         out = torch.zeros(((nd + 1) * (nd // 2), nslices), dtype=torch.uint8, device=device)

@@ -11,24 +11,24 @@ pytestmark = pytest.mark.gpu
 
 
 def _span_case(g, ci):
-    from opensss_gb300 import geometry as G
+    from opensss_gb300 import DataReduction as D, geometry as G
 
     nd, nr, span, af = (int(v) for v in g[f"case{ci}_dims"])
     lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
-    si, _, _, _ = G.SinogramLUT(nr, span, nr - 1)
+    si, _, _, _ = D.SinogramLUT(nr, span, nr - 1)
     eg, _ = G.expandRings(g[f"case{ci}_geometry"], np.zeros_like(g[f"case{ci}_geometry"]))
     return nd, nr, af, lor, si, eg
 
 
 def test_span_interpolation_matches_reference(cuda_ok, tmp_path):
-    from opensss_gb300 import geometry as G
+    from opensss_gb300 import DataReduction as D, geometry as G
     from opensss_gb300.Interpolation import InterpolateScatters
     from oracle import oracle as O
 
     g = golden("span")
     nd, nr, nru, ndu, nb, span, mrd = (int(v) for v in g["up_dims"])
     lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
-    si, _, _, _ = G.SinogramLUT(nr, span, mrd)
+    si, _, _, _ = D.SinogramLUT(nr, span, mrd)
     dense = O.densify(g["up_compact"].astype(np.float64), lor, nd, nru, ndu)
     out = InterpolateScatters(dense, nr, nru, nd, ndu, lor, si, str(tmp_path), True)
     assert out.dtype == np.float32

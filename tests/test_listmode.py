@@ -13,11 +13,11 @@ from conftest import golden
 
 
 def _tables(ncr, nr, mash, span, mrd):
-    from opensss_gb300 import geometry as G
+    from opensss_gb300 import DataReduction as D, geometry as G
 
     lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, ncr // mash, nr, ID_Shidt=False)
     if span > 0:
-        msi, _, lut, _ = G.SinogramLUT(nr, span, mrd)
+        msi, _, lut, _ = D.SinogramLUT(nr, span, mrd)
         return lor, si, msi, lut, lut
     return lor, si, si, np.array([]), si
 

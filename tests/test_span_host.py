@@ -10,7 +10,7 @@ from oracle import oracle as O
 
 @pytest.mark.parametrize("case", range(4))
 def test_sinogram_lut_matches_reference(case):
-    from opensss_gb300.geometry import SinogramLUT
+    from opensss_gb300.DataReduction import SinogramLUT
 
     g = golden("span")
     nr, span, mrd = (int(v) for v in g[f"lut{case}_args"])
@@ -23,7 +23,7 @@ def test_sinogram_lut_matches_reference(case):
 
 def test_sinogram_lut_keeps_the_reference_error():
     """Ring counts the reference's sinogram count cannot hold raise IndexError there too."""
-    from opensss_gb300.geometry import SinogramLUT
+    from opensss_gb300.DataReduction import SinogramLUT
 
     with pytest.raises(IndexError):
         SinogramLUT(8, 3, 7)
@@ -43,7 +43,7 @@ def test_expand_and_mash_geometry():
 
 
 def test_sum_lor_counts():
-    from opensss_gb300.geometry import SinogramLUT, SumLORsCounts
+    from opensss_gb300.DataReduction import SinogramLUT, SumLORsCounts
 
     g = golden("span")
     si, _, lut, counts = SinogramLUT(6, 3, 5)
@@ -52,7 +52,7 @@ def test_sum_lor_counts():
 
 
 def test_span_ring_pairs_use_float32_doubling():
-    from opensss_gb300.geometry import SinogramLUT, span_ring_pairs
+    from opensss_gb300.DataReduction import SinogramLUT, span_ring_pairs
 
     si, ring_lut, _, _ = SinogramLUT(10, 3, 9)
     pairs = span_ring_pairs(si)
@@ -66,13 +66,13 @@ def test_span_ring_pairs_use_float32_doubling():
 def test_span_upsampling_tables_reproduce_reference(layout):
     """Gathering the sampled sinogram through the span tables gives the
     reference's InterpolateAllBinsSpan output bit for bit."""
-    from opensss_gb300 import geometry as G
+    from opensss_gb300 import DataReduction as D, geometry as G
     from opensss_gb300.engine import compact_to_leg_pair
 
     g = golden("span")
     nd, nr, nru, ndu, nb, span, mrd = (int(v) for v in g["up_dims"])
     lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
-    si, _, _, _ = G.SinogramLUT(nr, span, mrd)
+    si, _, _, _ = D.SinogramLUT(nr, span, mrd)
     cmp = g["up_compact"]
     if layout == "dense":
         src = O.densify(cmp.astype(np.float64), lor, nd, nru, ndu).astype(np.float32)
@@ -94,14 +94,14 @@ def test_span_upsampling_tables_reproduce_reference(layout):
 def test_oracle_span_mask_and_fit_match_reference(ci):
     """The C oracle's span mask (bit-exact, both rules) and length-weighted
     fit (1e-5) against the reference's outputs."""
-    from opensss_gb300 import geometry as G
+    from opensss_gb300 import DataReduction as D, geometry as G
 
     g = golden("span")
     nd, nr, span, af = (int(v) for v in g[f"case{ci}_dims"])
     lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, nr, ID_Shidt=False)
-    si, _, _, _ = G.SinogramLUT(nr, span, nr - 1)
+    si, _, _, _ = D.SinogramLUT(nr, span, nr - 1)
     eg, _ = G.expandRings(g[f"case{ci}_geometry"], np.zeros_like(g[f"case{ci}_geometry"]))
-    pairs = G.span_ring_pairs(si)
+    pairs = D.span_ring_pairs(si)
     m = O.mask_pairs(g[f"case{ci}_mu"], g[f"case{ci}_bounds"], eg, lor, pairs, si.shape[0], af)
     assert np.array_equal(m, g[f"case{ci}_mask"])
     ma = O.mask_pairs(g[f"case{ci}_act"], g[f"case{ci}_bounds"], eg, lor, pairs, si.shape[0], af,
