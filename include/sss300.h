@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SSS300_ABI_VERSION 4
+#define SSS300_ABI_VERSION 5
 
 enum {
     SSS_OK = 0,
@@ -39,9 +39,12 @@ enum {
     SSS_ERR_CAPACITY = 8,   /* an output capacity was too small */
     SSS_ERR_EVENT = 9,      /* a list-mode event addresses a crystal or ring outside the sinogram
                                tables; the reference raises IndexError (Timber/Datafile.py:90-92) */
-    SSS_ERR_NONFINITE = 10  /* a scatter term came out infinite or NaN; no reference counterpart
+    SSS_ERR_NONFINITE = 10, /* a scatter term came out infinite or NaN; no reference counterpart
                                (the reference's nan_to_num, SingleScatterSimulationTOF.py:557, only
                                hides 0/0 of empty slices): the result must not be used */
+    SSS_ERR_TABLE = 11      /* a device index table the caller passed (sampled rings or crystals,
+                               LOR coordinates, cell table, slice table) holds an entry outside its
+                               range; the kernels skip such entries, so the result is incomplete */
 };
 
 /* Thread-local text of the last error. */
@@ -84,8 +87,8 @@ typedef struct sss_tof_problem {
     int32_t nru, ndu;              /* sampled rings, sampled crystals per ring */
     const int32_t *rings;          /* device, [nru] ring numbers (:153), each in 0..nr-1 */
     const int32_t *detectors;      /* device, [ndu] crystal numbers (:159-167), each in 0..nd-1;
-                                      the library reads both arrays on the device only and does
-                                      not check their values */
+                                      a leg whose ring or crystal is outside is left empty and
+                                      sets SSS_ERR_TABLE in the status word */
     int32_t sample_step[3];        /* scatter-point lattice step, voxels */
     int32_t nbins;                 /* TOF bins, 1..64 */
     double tof_bin_width;          /* ps, 2*TOFRange/NrBins */
@@ -166,23 +169,27 @@ int sss_tof_run(const sss_tof_problem *p, const double *points, int64_t n_points
 
 /* Expand the leg-pair output to the reference's dense layout
  * [nbins][nd+1][nd/2][nru*nru] (SingleScatterSimulationTOF.py:171).  lor
- * (device) is LORCoordinates int16 [nd][nd][2] (Python/openSSS/Sinogram.py:121-122), every
- * entry in range (angular < nd/2, radial <= nd; not checked on the device).
- * dense must be zeroed by the caller. */
+ * (device) is LORCoordinates int16 [nd][nd][2] (Python/openSSS/Sinogram.py:121-122);
+ * the entries of the sampled crystal pairs must lie in range (angular < nd/2,
+ * radial <= nd), and detectors[] in 0..nd-1.  Entries outside are skipped and
+ * set SSS_ERR_TABLE in *status (device int32, OR-ed).  dense must be zeroed by
+ * the caller. */
 int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
-                    const int16_t *lor, const int32_t *detectors, float *dense, void *stream);
+                    const int16_t *lor, const int32_t *detectors, float *dense, int32_t *status,
+                    void *stream);
 
 /* The same dense layout, every element written (zeros included), so dense
  * needs no clearing: for a fresh result array such as the one
  * SingleScatterSimulationTOF returns (SingleScatterSimulationTOF.py:201-208).
  * cell_pair (device int32 [(nd+1)*(nd/2)]) gives, per sinogram cell
  * rad*(nd/2) + ang, the sampled crystal pair di1*ndu + di2 (di1 <= di2) whose
- * LOR it is, or -1 (every entry below ndu*ndu, each pair in at most one cell).
- * dense may be device memory or page-locked host memory (written over the
- * host link at its device address); any other pointer is SSS_ERR_INVALID.
+ * LOR it is, or -1 (each pair in at most one cell).  An entry that is not -1
+ * or such a pair writes zeros and sets SSS_ERR_TABLE in *status (device int32,
+ * OR-ed).  dense may be device memory or page-locked host memory (written over
+ * the host link at its device address); any other pointer is SSS_ERR_INVALID.
  * Needs nru*nru a multiple of 4 and a 16-byte aligned dense. */
 int sss_tof_densify_full(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
-                         const int32_t *cell_pair, float *dense, void *stream);
+                         const int32_t *cell_pair, float *dense, int32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Batched simulation (no counterpart in the reference, which runs one
@@ -249,7 +256,9 @@ int sss_upsample(const float *sampled, int64_t bin_stride, int32_t nbins, const 
  * rule (the reference's, :145-151); acf_below > 1 masks instead where the
  * attenuation factor 1/exp(-sum mu*len) is below acf_below (no reference
  * counterpart: a looser tail definition, e.g. 1.03).  out (device uint8,
- * [(nd+1)*(nd/2)][nr*nr]) must be zeroed by the caller. */
+ * [(nd+1)*(nd/2)][nr*nr]) must be zeroed by the caller.  A sino_index entry
+ * outside 0..nr*nr-1, or LOR coordinates outside the sinogram, skip the LOR
+ * and set SSS_ERR_TABLE in *status. */
 int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float *map, int32_t use_activity,
                   int32_t nr, int32_t nd, const double *geometry, const int16_t *lor,
                   const int16_t *sino_index, int32_t af, double acf_below, uint8_t *out, int32_t *status,
@@ -261,7 +270,8 @@ int sss_tail_mask(const int32_t grid[3], const double bounds[6], const float *ma
  * expanded geometry (nr = 2*rings - 1, Python/openSSS/Geometry.py:161-197),
  * crystal pairs and acf_below as in sss_tail_mask; LOR (p, d1, d2) marks
  * out[cell*nslices + slice].  out (device uint8 [(nd+1)*(nd/2)][nslices])
- * must be zeroed by the caller. */
+ * must be zeroed by the caller.  A pair with a ring outside 0..nr-1 or a slice
+ * outside 0..nslices-1 is skipped and sets SSS_ERR_TABLE in *status. */
 int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const float *map, int32_t use_activity,
                         int32_t nr, int32_t nd, const double *geometry, const int16_t *lor, const int32_t *pairs,
                         int32_t npairs, int32_t nslices, int32_t af, double acf_below, uint8_t *out,

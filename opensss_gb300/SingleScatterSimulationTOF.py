@@ -98,10 +98,10 @@ def SingleScatterSimulationTOF(ActivityMap, AttenuationMap, ImageSize, Geometry,
     host = torch.empty(shape, dtype=torch.float32, pin_memory=True)
     if d.full:
         eng.densify_full(compact, d.cells, host)
-        torch.cuda.current_stream(eng.device).synchronize()
     else:
         eng.densify(compact, d.lor, out=d.dense)
         host.copy_(d.dense)
+    eng.check_status()
     dense = host.numpy()
     print("Time for SSS: {:.2f} seconds".format(time.time() - t0))
     if SavePath:

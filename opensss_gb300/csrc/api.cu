@@ -51,6 +51,10 @@ extern "C" int sss_status_code(int32_t s)
         return sss_set_error(SSS_ERR_NONFINITE,
                              "a detector pair's scatter term came out infinite or NaN (the result is not "
                              "usable)");
+    if (s & kErrTable)
+        return sss_set_error(SSS_ERR_TABLE,
+                             "an index table (sampled rings or crystals, LOR coordinates, cell or slice "
+                             "table) holds an entry outside its range");
     if (s & kErrEvent)
         return sss_set_error(SSS_ERR_EVENT,
                              "a list-mode event addresses a crystal or ring outside the sinogram tables "

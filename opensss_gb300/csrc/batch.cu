@@ -393,6 +393,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
             L.p.normals = p.normals;
             L.p.rings = p.rings;
             L.p.dets = p.detectors;
+            L.p.nr = p.nr;
             L.p.nd = p.nd;
             L.p.nru = p.nru;
             L.p.ndu = p.ndu;

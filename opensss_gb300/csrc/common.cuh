@@ -18,6 +18,8 @@ enum DeviceError : int32_t {
     kErrCapacity = 1 << 4,   // an internal list capacity was exceeded
     kErrEvent = 1 << 5,      // a list-mode event outside the sinogram tables (reference: IndexError)
     kErrNonFinite = 1 << 6,  // a detector pair's slice term came out infinite or NaN
+    kErrTable = 1 << 7,      // a caller's index table (sampled rings or crystals, LOR, cell or
+                             // slice table) holds an entry outside its range; nothing is read there
     // not an error: set by the tail mask's pre-pass when the map has a negative
     // or NaN value (its line integrals can then shrink); sss_status_code ignores it
     kNoteMapSigned = 1 << 30,

@@ -72,6 +72,13 @@ __device__ __forceinline__ LorRef lor_ref(long long id, int nr, int na, const in
     return R;
 }
 
+// The caller-table parts of a LOR: its slice in 0..nslices-1 and (span
+// pair lists) its rings in 0..nr-1.
+__device__ __forceinline__ bool lor_ref_ok(const LorRef& L, int nr, int nslices)
+{
+    return (unsigned)L.slice < (unsigned)nslices && (unsigned)L.r1 < (unsigned)nr && (unsigned)L.r2 < (unsigned)nr;
+}
+
 __device__ __forceinline__ void lor_line(const double* geom, int nd, int r1, int d1, int r2, int d2,
                                          double* lc)
 {
@@ -165,6 +172,10 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
     const LorRef L = lor_ref(id, P.nr, P.na, P.sino, P.pairs, P.npairs);
     const int d1 = L.i1 * P.af, d2 = L.i2 * P.af;
     if ((d1 == d2 && L.r1 == L.r2) || d1 > d2) return;  // TailsMask.py:129, :273
+    if (!lor_ref_ok(L, P.nr, P.nslices)) {  // the caller's slice or ring-pair table
+        raise_error(P.status, kErrTable);
+        return;
+    }
     double lc[6];
     lor_line(P.geom, P.nd, L.r1, d1, L.r2, d2, lc);
     double acf = 1.0;  // a miss gives Attenuation = 1 (:146-148)
@@ -198,8 +209,8 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
     if (tail) {
         const int ang = P.lor[2 * ((long long)d1 * P.nd + d2)];
         const int rad = P.lor[2 * ((long long)d1 * P.nd + d2) + 1];
-        if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2) {  // unset coordinates
-            raise_error(P.status, kErrCapacity);
+        if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2) {  // the caller's LOR table
+            raise_error(P.status, kErrTable);
             return;
         }
         const long long cell = (long long)rad * (P.nd / 2) + ang;
@@ -263,8 +274,8 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
     const int ang = P.lor[2 * ((long long)d1 * P.nd + d2)];
     const int rad = P.lor[2 * ((long long)d1 * P.nd + d2) + 1];
     const int slice = L.slice;
-    if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2 || slice < 0 || slice >= P.nslices) {
-        raise_error(P.status, kErrCapacity);  // unset coordinates or a bad slice order
+    if (rad < 0 || rad > P.nd || ang < 0 || ang >= P.nd / 2 || !lor_ref_ok(L, P.nr, P.nslices)) {
+        raise_error(P.status, kErrTable);  // the caller's LOR, slice-order or ring-pair table
         return;
     }
     const long long cell = (long long)rad * (P.nd / 2) + ang;

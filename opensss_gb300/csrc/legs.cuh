@@ -20,7 +20,7 @@ struct LegParams {
     const double* normals;
     const int32_t* rings;
     const int32_t* dets;
-    int nd, nru, ndu, nl, cap;
+    int nr, nd, nru, ndu, nl, cap;
     long long nvox;
     const double* points;  // wave's first point, [n][4]
     int npts;
@@ -57,6 +57,16 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
 {
     const int di = l / P.nru, ri = l % P.nru;  // legs are crystal-major
     const int ring = P.rings[ri], det = P.dets[di];
+    const long long o = (long long)s * P.nl + l;
+    if ((unsigned)ring >= (unsigned)P.nr || (unsigned)det >= (unsigned)P.nd) {
+        // the caller's ring or crystal table: an empty leg (mu integral +inf,
+        // so no pair uses it) and the error bit
+        raise_error(P.status, kErrTable);
+        P.legA[o] = make_float4(0.f, 0.f, INFINITY, 0.f);
+        P.legB[o] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+        P.legC[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
     const double* dp = P.geom + 3 * ((long long)ring * P.nd + det);
     const double zD = P.geom[3 * ((long long)ring * P.nd) + 2];  // :402 (crystal 0's z)
     const double xS = P.points[4 * s], yS = P.points[4 * s + 1], zS = P.points[4 * s + 2];
@@ -121,7 +131,6 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
         });
         if (c < 0) raise_error(P.status, kErrOverrun);
     }
-    const long long o = (long long)s * P.nl + l;
     // exp(-I) underflows to 0 in FP64 above ~745.13 (the skip at :451 / :483)
     const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
     P.legA[o] = make_float4(sv, asum, ilog2, cosa / (sv * sv));

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kLegThreadsMax) leg_kernel(LegParams P)
 
 __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, int nd,
                                const int16_t* __restrict__ lor, const int32_t* __restrict__ dets,
-                               float* __restrict__ dense)
+                               float* __restrict__ dense, int32_t* status)
 {
     const int nl = nru * ndu;
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,9 +137,17 @@ __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru
     const int di1 = l1 / nru, ri1 = l1 % nru, di2 = l2 / nru, ri2 = l2 % nru;
     if (di1 > di2 || (di1 == di2 && ri1 == ri2)) return;
     const int d1 = dets[di1], d2 = dets[di2];
+    if ((unsigned)d1 >= (unsigned)nd || (unsigned)d2 >= (unsigned)nd) {  // the caller's crystal table
+        raise_error(status, kErrTable);
+        return;
+    }
     const int ang = lor[2 * ((long long)d1 * nd + d2)];
     const int rad = lor[2 * ((long long)d1 * nd + d2) + 1];
     const int nang = nd / 2, nsino = nru * nru;
+    if (rad < 0 || rad > nd || ang < 0 || ang >= nang) {  // the caller's LOR table
+        raise_error(status, kErrTable);
+        return;
+    }
     dense[(((long long)b * (nd + 1) + rad) * nang + ang) * nsino + ri2 + ri1 * nru] = cmp[i];
 }
 
@@ -148,7 +156,8 @@ __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru
 // cell_pair[cell] = di1 * ndu + di2 (di1 <= di2) or -1.  The destination
 // may be page-locked host memory, which the GPU writes over its host link.
 __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, long long ncell,
-                                    const int32_t* __restrict__ cell_pair, float* __restrict__ dense)
+                                    const int32_t* __restrict__ cell_pair, float* __restrict__ dense,
+                                    int32_t* status)
 {
     const int nl = nru * ndu, nsino = nru * nru;
     const long long plane = (long long)nl * nl;
@@ -161,8 +170,10 @@ __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, in
         const int b = (int)(e / ((long long)nsino * ncell));
         const int pair = __ldg(cell_pair + cell);
         float v[4] = {0.f, 0.f, 0.f, 0.f};
-        if (pair >= 0) {
-            const int di1 = pair / ndu, di2 = pair % ndu;
+        const int di1 = pair / ndu, di2 = pair % ndu;
+        if (pair < -1 || pair >= ndu * ndu || (pair >= 0 && di1 > di2)) {  // the caller's cell table
+            raise_error(status, kErrTable);
+        } else if (pair >= 0) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int s = sino + k, ri1 = s / nru, ri2 = s % nru;
@@ -362,6 +373,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     LP.normals = p->normals;
     LP.rings = p->rings;
     LP.dets = p->detectors;
+    LP.nr = p->nr;
     LP.nd = p->nd;
     LP.nru = p->nru;
     LP.ndu = p->ndu;
@@ -483,21 +495,21 @@ extern "C" int sss_get_timing(double out[6])
 
 extern "C" int sss_tof_densify(const float* compact, int32_t nbins, int32_t nru, int32_t ndu,
                                int32_t nd, const int16_t* lor, const int32_t* detectors,
-                               float* dense, void* stream)
+                               float* dense, int32_t* status, void* stream)
 {
-    if (!compact || !lor || !detectors || !dense || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
+    if (!compact || !lor || !detectors || !dense || !status || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
         return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify: bad argument");
     long long nl = (long long)nru * ndu;
     long long total = (long long)nbins * nl * nl;
     densify_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        compact, nbins, nru, ndu, nd, lor, detectors, dense);
+        compact, nbins, nru, ndu, nd, lor, detectors, dense, status);
     return sss_check_launch("densify_kernel");
 }
 
 extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
-                                    const int32_t* cell_pair, float* dense, void* stream)
+                                    const int32_t* cell_pair, float* dense, int32_t* status, void* stream)
 {
-    if (!compact || !cell_pair || !dense || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
+    if (!compact || !cell_pair || !dense || !status || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
         return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify_full: bad argument");
     if ((nru * nru) % 4 != 0 || (uintptr_t)dense % 16 != 0)
         return sss_set_error(SSS_ERR_INVALID,
@@ -524,7 +536,8 @@ extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t
     const long long total4 = (long long)nbins * ncell * nru * nru / 4;
     const long long want = (total4 + 255) / 256;
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
-    densify_full_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair, dst);
+    densify_full_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair, dst,
+                                                                      status);
     return sss_check_launch("densify_full_kernel");
 }
 

@@ -230,15 +230,18 @@ class TofSSS:
         [B, ND+1, ND//2, NRU^2] float32, zeros included, into ``out``: a CUDA
         tensor or a page-locked host tensor (written by the GPU over the host
         link, no separate copy).  ``cell_pair``: CUDA int32 table of
-        ``geometry.dense_cell_pairs``.  Asynchronous on the current stream."""
-        shape = (self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru)
+        ``geometry.dense_cell_pairs``.  Asynchronous on the current stream; a
+        table entry out of range is OR-ed into the engine's status word
+        (``check_status``)."""
+        shape =(self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru)
         if tuple(out.shape) != shape or out.dtype != torch.float32 or not out.is_contiguous():
             raise ValueError(f"densify_full: out must be contiguous float32 {shape}")
         if not (out.is_cuda or out.is_pinned()):
             raise ValueError("densify_full: out must be a CUDA tensor or page-locked host memory")
         st = torch.cuda.current_stream(self.device)
         _lib.check(_lib.lib().sss_tof_densify_full(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd,
-                                                   _ptr(cell_pair), _ptr(out), C.c_void_p(st.cuda_stream)))
+                                                   _ptr(cell_pair), _ptr(out), _ptr(self._status),
+                                                   C.c_void_p(st.cuda_stream)))
         return out
 
     def densify(self, compact: torch.Tensor, lor, out: torch.Tensor | None = None) -> torch.Tensor:
@@ -247,7 +250,9 @@ class TofSSS:
         ``lor`` is the LORCoordinates table (checked here), or a CUDA int16
         copy of a table checked before.  ``out``: a dense buffer that this
         engine densified into before with the same table (or zeros): only
-        the sampled pairs' cells are written, the others stay as they are."""
+        the sampled pairs' cells are written, the others stay as they are.
+        Asynchronous; a table entry out of range is OR-ed into the engine's
+        status word (``check_status``)."""
         dev = self.device
         if isinstance(lor, torch.Tensor) and lor.is_cuda:
             lor_t = lor
@@ -260,9 +265,16 @@ class TofSSS:
         dense = out if out is not None else torch.zeros(shape, dtype=torch.float32, device=dev)
         st = torch.cuda.current_stream(dev)
         _lib.check(_lib.lib().sss_tof_densify(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd,
-                                              _ptr(lor_t), _ptr(self.dets), _ptr(dense),
+                                              _ptr(lor_t), _ptr(self.dets), _ptr(dense), _ptr(self._status),
                                               C.c_void_p(st.cuda_stream)))
         return dense
+
+    def check_status(self):
+        """Wait for the current stream, then raise for any error bit of the
+        engine's status word (set by ``run`` and by the densify calls since
+        the last ``run``)."""
+        torch.cuda.current_stream(self.device).synchronize()
+        _lib.check_status(int(self._status.item()))
 
 
 def select_points(pts: torch.Tensor, counts: np.ndarray, points):

@@ -41,7 +41,7 @@ def test_python_binding_covers_header():
 
 
 def test_abi_version(lib):
-    assert lib.sss_abi_version() == 4
+    assert lib.sss_abi_version() == 5
 
 
 def test_invalid_arguments_fail_before_any_device_work(lib):
@@ -60,6 +60,10 @@ def test_invalid_arguments_fail_before_any_device_work(lib):
     rc = lib.sss_raytrace(grid.ctypes.data_as(C.c_void_p), ok.ctypes.data_as(C.c_void_p), None, 0,
                           2, 12, C.c_void_p(8), None, None, C.c_void_p(8), None, None, None)
     assert rc == 1
+    # the densify calls need a status word for their table checks
+    fake = C.c_void_p(8)
+    assert lib.sss_tof_densify(fake, 1, 2, 2, 8, fake, fake, fake, None, None) == 1
+    assert lib.sss_tof_densify_full(fake, 1, 2, 2, 8, fake, fake, None, None) == 1
     plan = C.c_void_p(0)
     rc = lib.sss_batch_plan(None, 0, None, None, 0, None, C.byref(plan), None)
     assert rc == 1 and not plan.value
@@ -74,6 +78,8 @@ def test_status_codes(lib):
     assert lib.sss_status_code(1) == 3
     assert "IndexError" in _lib.last_error()
     assert lib.sss_status_code(2) == 4
+    assert lib.sss_status_code(1 << 7) == 11  # a caller's index table out of range
+    assert "table" in _lib.last_error()
     with pytest.raises(_lib.SSSError):
         _lib.check_status(1)
 

@@ -330,6 +330,61 @@ def test_tof_offsets_past_the_table_are_an_error(cuda_ok, att_table):
     assert e.value.code == 4
 
 
+def test_caller_index_tables_out_of_range_are_an_error(cuda_ok, att_table):
+    """The device index tables a C caller passes are checked where they are
+    read: a cell-table entry past the sampled pairs (sss_tof_densify_full),
+    LOR coordinates past the sinogram (sss_tof_densify), and a sampled crystal
+    or ring past the scanner (sss_tof_run) each set SSS_ERR_TABLE; the
+    kernels read nothing at such an entry."""
+    import ctypes as C
+
+    import torch
+
+    from opensss_gb300 import _lib, geometry as G
+    from opensss_gb300._lib import SSSError
+
+    def ptr(t):
+        return C.c_void_p(t.data_ptr())
+
+    g = golden("sss_tiny_b5")
+    pr = problem_from_golden(g)
+    nd, nru, ndu = pr.scanner.nr_detectors, pr.nr_rings_used, pr.nr_detectors_used
+    lor, _, _ = G.SinogramCoordinates(1, 1, 1, 1, nd, pr.scanner.nr_rings, ID_Shidt=False)
+    eng = _engine(pr, att_table)
+    lp = eng.run(pr.activity, pr.attenuation, pr.image_size).clone()
+    L = _lib.lib()
+    shape = (pr.nr_bins, nd + 1, nd // 2, nru * nru)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    cells = torch.from_numpy(G.dense_cell_pairs(lor, eng.dets_np, nd)).cuda()
+    bad_cells = cells.clone()
+    bad_cells[int(torch.nonzero(cells >= 0)[0])] = ndu * ndu + 3
+    out = torch.zeros(shape, device="cuda")
+    assert L.sss_tof_densify_full(ptr(lp), pr.nr_bins, nru, ndu, nd, ptr(bad_cells), ptr(out), ptr(st), None) == 0
+    torch.cuda.synchronize()
+    assert L.sss_status_code(int(st.item())) == 11
+
+    d = eng.dets_np
+    bad_lor = torch.from_numpy(np.ascontiguousarray(lor, dtype=np.int16)).cuda()
+    bad_lor[int(d[0]), int(d[1]), 0] = nd // 2  # one past the last angle
+    st.zero_()
+    out.zero_()
+    assert L.sss_tof_densify(ptr(lp), pr.nr_bins, nru, ndu, nd, ptr(bad_lor), ptr(eng.dets), ptr(out), ptr(st),
+                             None) == 0
+    torch.cuda.synchronize()
+    assert L.sss_status_code(int(st.item())) == 11
+
+    for table, bad in ((eng.dets, nd + 2), (eng.rings, pr.scanner.nr_rings)):
+        keep = int(table[1])
+        table[1] = bad
+        with pytest.raises(SSSError) as e:
+            eng.run(pr.activity, pr.attenuation, pr.image_size)
+        assert e.value.code == 11
+        table[1] = keep
+    again = eng.run(pr.activity, pr.attenuation, pr.image_size)
+    assert torch.equal(again, lp)
+
+
 @pytest.mark.parametrize("name", ["sss_tiny_far", "sss_wide_body_tof13"])
 def test_far_tof_offsets_match_reference(cuda_ok, att_table, name):
     """TOF offsets far past the last bin centre, where the pair kernel takes
@@ -394,9 +449,10 @@ def test_full_densify_to_device_and_pinned_host(cuda_ok, att_table):
         torch.cuda.synchronize()
         assert np.array_equal(out.cpu().numpy(), ref.astype(np.float32))
     pageable = np.zeros(shape, np.float32)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
     rc = _lib.lib().sss_tof_densify_full(C.c_void_p(lp.data_ptr()), pr.nr_bins, pr.nr_rings_used,
                                          pr.nr_detectors_used, nd, C.c_void_p(cells.data_ptr()),
-                                         C.c_void_p(pageable.ctypes.data), None)
+                                         C.c_void_p(pageable.ctypes.data), C.c_void_p(st.data_ptr()), None)
     assert rc == 1 and "page-locked" in _lib.last_error()
     assert not pageable.any()
 

@@ -63,6 +63,66 @@ def test_tail_mask_matches_reference_bit_exact(cuda_ok, case):
     assert np.array_equal(m, g[f"case{case}_mask"])
 
 
+def test_tail_mask_tables_out_of_range_are_an_error(cuda_ok):
+    """A slice table entry past the nr^2 slices (sss_tail_mask), a ring-pair
+    entry with a ring past the scanner or a slice past nslices
+    (sss_tail_mask_pairs) and LOR coordinates past the sinogram set
+    SSS_ERR_TABLE; those LORs are skipped, the others marked as before."""
+    import ctypes as C
+
+    import torch
+
+    from opensss_gb300 import _lib
+    from opensss_gb300.engine import fortran_flat
+
+    def ptr(t):
+        return C.c_void_p(t.data_ptr())
+
+    g = golden("mask")
+    nd, nr, af = (int(v) for v in g["case0_dims"])
+    lor, si, _ = _sino(nd, nr)
+    mu = fortran_flat(g["case0_mu"], torch.device("cuda"))
+    grid = np.array(g["case0_mu"].shape, np.int32)
+    bounds = np.ascontiguousarray(np.asarray(g["case0_bounds"], np.float64).reshape(-1)[:6])
+    geom = torch.from_numpy(np.ascontiguousarray(g["case0_geometry"], np.float64)).cuda()
+    lor_t = torch.from_numpy(np.ascontiguousarray(lor, np.int16)).cuda()
+    L = _lib.lib()
+    args = (grid.ctypes.data_as(C.c_void_p), bounds.ctypes.data_as(C.c_void_p), ptr(mu), 0, nr, nd, ptr(geom))
+    ncell = (nd + 1) * (nd // 2)
+
+    def mask(lor_dev, si_np):
+        out = torch.zeros((ncell, nr * nr), dtype=torch.uint8, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        si_dev = torch.from_numpy(np.ascontiguousarray(si_np[:nr, :nr], np.int16)).cuda()
+        assert L.sss_tail_mask(*args, ptr(lor_dev), ptr(si_dev), af, 0.0, ptr(out), ptr(st), None) == 0
+        torch.cuda.synchronize()
+        return out.cpu().numpy(), int(st.item())
+
+    good, st = mask(lor_t, si)
+    assert st == 0 and np.array_equal(good, g["case0_mask"])
+    bad_si = np.array(si[:nr, :nr], np.int64)
+    bad_si[0, 1] = nr * nr
+    got, st = mask(lor_t, bad_si)
+    assert L.sss_status_code(st) == 11
+    keep = np.ones(nr * nr, bool)
+    keep[int(si[0, 1])] = False  # the slice whose LORs were skipped
+    assert np.array_equal(got[:, keep], good[:, keep]) and not got[:, ~keep].any()
+    bad_lor = lor_t.clone()
+    bad_lor[0, af, 1] = nd + 1  # one past the last radius
+    _, st = mask(bad_lor, si)
+    assert L.sss_status_code(st) == 11
+
+    pairs = np.array([[0, 1, 0], [1, 0, 1], [nr, 0, 2], [0, 0, 7]], np.int32)  # a bad ring, a bad slice
+    pairs_dev = torch.from_numpy(pairs).cuda()
+    out = torch.zeros((ncell, 3), dtype=torch.uint8, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert L.sss_tail_mask_pairs(*args, ptr(lor_t), ptr(pairs_dev), len(pairs), 3, af, 0.0, ptr(out), ptr(st),
+                                 None) == 0
+    torch.cuda.synchronize()
+    assert L.sss_status_code(int(st.item())) == 11
+    assert not out[:, 2].any()
+
+
 def test_activity_mask_matches_oracle(cuda_ok):
     """UseAttenuation=False marks LORs that see no activity (TailsMask.py:153-161)."""
     from opensss_gb300 import workloads as W
