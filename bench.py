@@ -1012,23 +1012,23 @@ def case_mask(reps):
         tail_mask_device(pr.attenuation, pr.image_size, sc.geometry, lor, si, 4)
 
 
-def case_fit(reps):
-    """Back-projection fit of four TOF bins of seeded sinograms in one pass on
-    a 380 x 40 scanner, AF 4."""
+def case_fit(reps, nbins=4, rings=40):
+    """Back-projection fit of ``nbins`` TOF bins of seeded sinograms in one
+    pass on a 380 x ``rings`` scanner, AF 4."""
     import torch  # noqa: F401
 
     from opensss_gb300 import geometry as G, workloads as W  # noqa: F401
     from opensss_gb300.BackProjection import fit_bins_device
 
     pr = W.tof13_64x64x48()
-    sc = W.ring_scanner(380, 40, radius_cm=41.0, ring_pitch_cm=0.64)
-    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, 40, ID_Shidt=False)
-    shp = (381 * 190, 1600)
+    sc = W.ring_scanner(380, rings, radius_cm=41.0, ring_pitch_cm=0.64)
+    lor, si, _ = G.SinogramCoordinates(1, 1, 1, 1, 380, rings, ID_Shidt=False)
+    shp = (381 * 190, rings * rings)
     g = torch.Generator(device="cuda")
     g.manual_seed(1)
-    prm = torch.poisson(torch.full((4,) + shp, 3.0, device="cuda"), generator=g)
+    prm = torch.poisson(torch.full((nbins,) + shp, 3.0, device="cuda"), generator=g)
     rnd = torch.full(shp, 0.3, device="cuda")
-    scat = torch.rand((4,) + shp, device="cuda", generator=g)
+    scat = torch.rand((nbins,) + shp, device="cuda", generator=g)
     mask = (torch.rand(shp, device="cuda", generator=g) < 0.3).to(torch.uint8)
     cell = np.arange(shp[0], dtype=np.int64) * shp[1]
     ring = np.arange(shp[1], dtype=np.int64)
@@ -1036,7 +1036,13 @@ def case_fit(reps):
     bounds = np.array([pr.image_size[0], pr.image_size[1], -zr, pr.image_size[3], pr.image_size[4], zr])
     for _ in range(reps):
         fit_bins_device(prm, rnd, mask, scat, shp[0] * shp[1], cell, ring, np.array([40, 40, 26]), bounds,
-                        sc.geometry, lor, si[:40, :40].T, 4)
+                        sc.geometry, lor, si[:rings, :rings].T, 4)
+
+
+def case_fit13(reps):
+    """The same fit over 13 TOF bins (the 13-bin workload's bin count) on a
+    380 x 16 scanner: 1.9 GB of seeded sinograms."""
+    case_fit(reps, nbins=13, rings=16)
 
 
 def case_listmode(reps):
@@ -1095,8 +1101,8 @@ def case_prep(reps):
     torch.cuda.synchronize()
 
 
-PROFILE_CASES = {"upsample": case_upsample, "mask": case_mask, "fit": case_fit, "listmode": case_listmode,
-         "pair": case_pair, "batch": case_batch, "prep": case_prep}
+PROFILE_CASES = {"upsample": case_upsample, "mask": case_mask, "fit": case_fit, "fit13": case_fit13,
+                 "listmode": case_listmode, "pair": case_pair, "batch": case_batch, "prep": case_prep}
 
 
 
