@@ -256,14 +256,33 @@ __device__ __forceinline__ float fit_scatter(const FitParams& P, int b, long lon
     return P.scat_clamp ? fmaxf(sv, 0.f) : sv;
 }
 
+// A 16-byte shared-memory load issued where it stands: the per-LOR values
+// are re-read at every voxel instead of being held in registers across the
+// walk, which keeps the kernel's register count (and so its occupancy) at that
+// of the walk alone.
+__device__ __forceinline__ float4 lds_v4(const float4* p)
+{
+    float4 v;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+    return v;
+}
+
+constexpr int kBpThreads = 128;  // threads of a bp_kernel block
+
+// One thread per lattice LOR; lattice order keeps a warp on one crystal pair
+// over neighbouring ring pairs (similar voxel paths, similar walk lengths).
 // NPB > 0: the plain (not length-weighted) back-projection of at most
 // 2 NPB + 1 bins, whose per-voxel values are the same along the whole LOR
-// (value / voxel count, :108-110): they are formed once per LOR and held in
-// registers, and each voxel issues only its vector atomics.  NPB = 0: the
-// general form, which forms the values per voxel (the length-weighted span
-// fit, :294-297, and more than 17 bins).
+// (value / voxel count, :108-110): they are formed once per LOR and kept in
+// the thread's own shared-memory column, and each voxel issues only its
+// vector atomics.  With those values out of the registers the walk sets the
+// register count; six blocks a multiprocessor (80 registers) hold it without
+// spilling but the odd word.  NPB = 0: the general form, which forms the
+// values per voxel (the length-weighted span fit, :294-297, and more than 17
+// bins), with its own register count.
 template <int NPB>
-__global__ void __launch_bounds__(128) bp_kernel(FitParams P)
+__global__ void __launch_bounds__(kBpThreads, NPB > 0 ? 6 : 0) bp_kernel(FitParams P)
 {
     const long long n = (long long)(P.pairs ? P.npairs : P.nr * P.nr) * P.na * P.na;
     const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -321,19 +340,20 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
             return make_float2(pv / fn, s / fn);
         };
         const int paired = P.nbins & ~1;
-        float4 cps[NPB], crs[NPB];
+        // this thread's (P, S, P, S) of each bin pair, in its own shared-memory column
+        __shared__ float4 s_cps[NPB][kBpThreads];
         unsigned pm = 0;  // bin pairs with a bin this LOR contributes to
 #pragma unroll
         for (int k = 0; k < NPB; ++k) {
-            cps[k] = crs[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (2 * k < paired) {
                 const bool in0 = (bins >> (2 * k)) & 1ull, in1 = (bins >> (2 * k + 1)) & 1ull;
                 const float2 c0 = in0 ? contrib(2 * k) : make_float2(0.f, 0.f);
                 const float2 c1 = in1 ? contrib(2 * k + 1) : make_float2(0.f, 0.f);
-                cps[k] = make_float4(c0.x, c0.y, c1.x, c1.y);
-                crs[k] = make_float4(in0 ? ar : 0.f, in0 ? 1.f : 0.f, in1 ? ar : 0.f, in1 ? 1.f : 0.f);
+                v = make_float4(c0.x, c0.y, c1.x, c1.y);
                 if (in0 || in1) pm |= 1u << k;
             }
+            s_cps[k][threadIdx.x] = v;
         }
         const int lastb = P.nbins - 1;
         const bool has_last = (P.nbins & 1) && ((bins >> lastb) & 1ull);
@@ -351,8 +371,12 @@ __global__ void __launch_bounds__(128) bp_kernel(FitParams P)
             for (int k = 0; k < NPB; ++k) {
                 if ((pm >> k) & 1u) {
                     float4* ps4 = reinterpret_cast<float4*>(P.img + (long long)(2 * k) * 4 * P.nvox);
-                    atomicAdd(ps4 + v, cps[k]);
-                    if (!every) atomicAdd(ps4 + P.nvox + v, crs[k]);  // randoms and sensitivity of these bins
+                    atomicAdd(ps4 + v, lds_v4(&s_cps[k][threadIdx.x]));
+                    if (!every) {  // randoms and sensitivity of these bins
+                        const bool in0 = (bins >> (2 * k)) & 1ull, in1 = (bins >> (2 * k + 1)) & 1ull;
+                        atomicAdd(ps4 + P.nvox + v,
+                                  make_float4(in0 ? ar : 0.f, in0 ? 1.f : 0.f, in1 ? ar : 0.f, in1 ? 1.f : 0.f));
+                    }
                 }
             }
             if (has_last) {
@@ -630,19 +654,19 @@ int backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, i
         return sss_set_error(SSS_ERR_CUDA, "sss_backproject_fit: memset failed");
     const long long n = (long long)(pairs ? npairs : nr * nr) * P.na * P.na;
     if (n > 0) {
-        const unsigned nb = blocks_for(n, 128);
+        const unsigned nb = blocks_for(n, kBpThreads);
         if (length_weighted || nbins > 17)
-            bp_kernel<0><<<nb, 128, 0, st>>>(P);
+            bp_kernel<0><<<nb, kBpThreads, 0, st>>>(P);
         else if (nbins <= 3)
-            bp_kernel<1><<<nb, 128, 0, st>>>(P);
+            bp_kernel<1><<<nb, kBpThreads, 0, st>>>(P);
         else if (nbins <= 5)
-            bp_kernel<2><<<nb, 128, 0, st>>>(P);
+            bp_kernel<2><<<nb, kBpThreads, 0, st>>>(P);
         else if (nbins <= 9)
-            bp_kernel<4><<<nb, 128, 0, st>>>(P);
+            bp_kernel<4><<<nb, kBpThreads, 0, st>>>(P);
         else if (nbins <= 13)
-            bp_kernel<6><<<nb, 128, 0, st>>>(P);
+            bp_kernel<6><<<nb, kBpThreads, 0, st>>>(P);
         else
-            bp_kernel<8><<<nb, 128, 0, st>>>(P);
+            bp_kernel<8><<<nb, kBpThreads, 0, st>>>(P);
         if ((rc = sss_check_launch("bp_kernel"))) return rc;
     }
     int dev = 0, sms = 0;

@@ -382,7 +382,8 @@ def test_caller_index_tables_out_of_range_are_an_error(cuda_ok, att_table):
         assert e.value.code == 11
         table[1] = keep
     again = eng.run(pr.activity, pr.attenuation, pr.image_size)
-    assert torch.equal(again, lp)
+    # the two tasks of a pair add to its cells with atomics, in either order
+    assert rel_l2(again.cpu().numpy(), lp.cpu().numpy()) < 1e-6
 
 
 @pytest.mark.parametrize("name", ["sss_tiny_far", "sss_wide_body_tof13"])
