@@ -611,9 +611,10 @@ def _small_batch(dev, args, att):
 
 def run_precision(dev, args, att):
     """The precision-stress instance: 128x128x96 @ 4 mm, 32 rings x 96
-    crystals, 33 TOF bins of 15 mm.  Full-size throughput with the plain and
-    the Kahan-compensated scatter-point reduction, then both against the FP64
-    oracle on a sample of scatter points: relative L2,
+    crystals, 33 TOF bins of 15 mm.  Full-size throughput of the plain launch
+    and of the precision launch ("kahan": SSS_FLAG_KAHAN, Kahan-compensated
+    scatter-point reduction and float-pair TOF offsets), then both against the
+    FP64 oracle on a sample of scatter points: relative L2,
     largest bin error (over the largest reference bin) and the fitted scale
     of the centre TOF bin (prompts drawn from the FP64 scatter).  The sample
     is ``--precision-points`` scatter points spread evenly over the workload
@@ -704,7 +705,9 @@ def run_precision(dev, args, att):
             "error_vs_fp64_oracle": err, "fp64_fitted_scale": s_ref, "fit_bin": b,
             "sample": f"{n} of {n_all} scatter points, evenly spread in lattice order "
                       f"({n * _pairs(nru, ndu) * pr.nr_bins:.3e} units)",
-            "fp64_oracle": "oracle/sss_oracle.c (FP64 C restatement), host cores"}
+            "fp64_oracle": "oracle/sss_oracle.c (FP64 C restatement), host cores",
+            "kahan": "SSS_FLAG_KAHAN: Kahan-compensated scatter-point sums and TOF offsets from float-pair "
+                     "distances and samples"}
 
 
 def run_serving(dev, args, att):

@@ -111,10 +111,15 @@ typedef struct sss_tof_problem {
  * block (no reference counterpart: the bound of the launch-shape tuner). */
 int sss_pair_warps_max(int32_t nbins, int32_t flags);
 
-/* sss_tof_problem.flags.  SSS_FLAG_KAHAN: sum each detector pair's per-point
- * terms over a z-slice's scatter points with Kahan's compensated addition
- * (the reference sums them in FP32 too, :551).  Honoured by sss_tof_run;
- * sss_batch_* always uses the plain reduction. */
+/* sss_tof_problem.flags.  SSS_FLAG_KAHAN: the precision launch.  Each
+ * detector pair's per-point terms are summed over a z-slice's scatter points
+ * with Kahan's compensated addition (the reference sums them in FP32 too,
+ * :551), and each voxel's TOF offset is formed from float-pair distances and
+ * samples (about 44 bits; the voxel lists carry a third float per entry), so
+ * that it takes the reference's FP64 table column (:520, :526) except within
+ * about 1e-9 ps of a column boundary; the plain launch's FP32 offset can take
+ * the neighbouring column within about 1e-3 ps.  Honoured by sss_tof_run;
+ * sss_batch_* always uses the plain launch. */
 #define SSS_FLAG_KAHAN 1
 /* sss_tof_problem.flags.  SSS_FLAG_UNIT_TOF: the caller asserts that every
  * tof_log2w entry is (0, 0), i.e. one bin whose normalised TOF weight is

@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(pair_block_warps(NP, false) * 32, MINB)
         }
         const int rem = (int)(task - it.task_begin);
         walk_task<NP, SINGLE, ODD, false>(it.ctx, T, 0, it.npts, rem / it.nchunks, rem % it.nchunks, lane, sAR,
-                                          sN, sG, vbuf, nullptr, tof_bad, energy_bad, nonfinite, walked, npairs);
+                                          sN, sG, vbuf, nullptr, nullptr, tof_bad, energy_bad, nonfinite, walked,
+                                          npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, nonfinite, walked, npairs, status, nullptr);
 }
@@ -414,6 +415,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
                 L.p.vox = (float2*)(ws + doff);
                 doff += align256(sizeof(float2) * it.count * nl * cap);
             }
+            L.p.vox_lo = nullptr;
             L.p.status = status;
             L.thread_begin = W.threads;
             W.threads += it.count * nl;
@@ -457,6 +459,7 @@ int plan_items(const sss_tof_problem* problems, int32_t n, float* const* outs,
                 C.legB = hleg[j].p.legB;
                 C.legC = hleg[j].p.legC;
                 C.vox = hleg[j].p.vox;
+                C.vox_lo = nullptr;  // the batched engine runs the plain pair kernel
                 C.unit_tof = (p.flags & SSS_FLAG_UNIT_TOF) != 0;
                 C.out = outs[it.prob];
                 P.npts = (int)it.count;

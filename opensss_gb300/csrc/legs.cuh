@@ -26,8 +26,10 @@ struct LegParams {
     int npts;
     float4* legA;   // [npts][nl]: sv, activity integral, mu integral * log2(e), |cos a|/sv^2
     float4* legB;   // [npts][nl]: unit vector to the crystal (high floats), voxel-list length (int bits)
-    float4* legC;   // [npts][nl]: the unit vector's low floats (FP64 value = high + low), 0
+    float4* legC;   // [npts][nl]: the unit vector's low floats (FP64 value = high + low), the
+                    // distance's low float
     float2* vox;    // [npts][nl][cap]: act*len, 2*sample/c (ps), leg-major; null: no lists
+    float* vox_lo;  // [npts][nl][cap]: the samples' low floats (2*sample/c = high + low), or null
     int32_t* status;
 };
 
@@ -101,6 +103,7 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
         int64_t fprev = f0;
         bool okprev = ok0;
         float2* out = P.vox ? P.vox + ((long long)s * P.nl + l) * P.cap : nullptr;
+        float* out_lo = P.vox_lo ? P.vox_lo + ((long long)s * P.nl + l) * P.cap : nullptr;
         int c = ray_walk(P.g, r, P.cap, [&](int k, int64_t lin, double ta, double tb) {
             const bool okb = fix61_ok(tb);
             const int64_t fb = fix61(tb);
@@ -123,9 +126,17 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
             asum += a;
             if (a != 0.f && out) {
                 // sample = half the distance walked to the voxel's exit (:155-156)
-                const float dt0 = ok0b ? unfix61_abs(fb - f0) : (float)(tb - t0);
-                float rho = vlen * dt0 * inv_c;
-                out[nlist] = make_float2(a, rho);
+                if (out_lo) {
+                    // the precision launch: 2 * sample / c in FP64, kept as a float pair
+                    const double dt = ok0b ? unfix61_abs_d(fb - f0) : tb - t0;
+                    const double rho = vn * dt * (1.0 / kLightCmPerPs);
+                    const float rh = (float)rho;
+                    out[nlist] = make_float2(a, rh);
+                    out_lo[nlist] = (float)(rho - (double)rh);
+                } else {
+                    const float dt0 = ok0b ? unfix61_abs(fb - f0) : (float)(tb - t0);
+                    out[nlist] = make_float2(a, vlen * dt0 * inv_c);
+                }
                 ++nlist;
             }
         });
@@ -135,7 +146,7 @@ __device__ __forceinline__ void leg_one(const LegParams& P, int s, int l)
     const float ilog2 = musum > 745.13f ? INFINITY : musum * 1.4426950408889634f;
     P.legA[o] = make_float4(sv, asum, ilog2, cosa / (sv * sv));
     P.legB[o] = make_float4(hi[0], hi[1], hi[2], __int_as_float(nlist));
-    P.legC[o] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    P.legC[o] = make_float4(lo[0], lo[1], lo[2], (float)(vn - (double)sv));
 }
 
 }  // namespace sss

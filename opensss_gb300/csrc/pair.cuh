@@ -34,7 +34,9 @@ constexpr int kGRow = 68;
 //         whose offsets differ by 16 (which would share a bank pair) do not
 //         collide
 //   n     u8     [8001]  bin of the column's largest weight
-//   vbuf  float2 [warps][32]  staged voxels of each warp's walk
+//   vbuf  float2 [warps][32]  staged voxels of each warp's walk; a
+//         Kahan-compensated launch (kKahanWarps warps) keeps the low floats of
+//         its staged samples after them, float [kKahanWarps][32]
 //   g     float  [nbins][kGRow]
 //   kahan float2 [2 NP][32 kKahanWarps]  (Kahan-compensated launches only,
 //         which run kKahanWarps warps so that 64 bins still fit)
@@ -43,7 +45,9 @@ __host__ __device__ constexpr int ar_slot(int t) { return t + (t >> 4); }
 constexpr int kSmemNOff = (8 * (ar_slot(kZeroEntry) + 1) + 15) & ~15;
 constexpr int kSmemVbufOff = (kSmemNOff + kTofEntries + 15) & ~15;
 constexpr int kSmemGOff = kSmemVbufOff + 8 * 32 * kPairWarps;
+constexpr int kSmemVloOff = kSmemVbufOff + 8 * 32 * kKahanWarps;  // Kahan launches only
 static_assert(kSmemGOff % 16 == 0, "shared-memory sections must be 16-byte aligned");
+static_assert(kSmemVloOff + 4 * 32 * kKahanWarps <= kSmemGOff, "the low floats must fit in the vbuf section");
 
 __host__ __device__ inline int pair_smem_kahan_off(int nbins) { return kSmemGOff + 4 * kGRow * nbins; }
 
@@ -79,8 +83,9 @@ struct PairCtx {
     const double* points;    // scatter points the leg arrays are indexed by
     const float4* legA;      // [point][nl]
     const float4* legB;
-    const float4* legC;      // low floats of legB's unit vectors
+    const float4* legC;      // low floats of legB's unit vectors, and of legA's distance
     const float2* vox;       // [point][nl][cap]
+    const float* vox_lo;     // [point][nl][cap] low floats of the samples (Kahan launches), else null
     float* out;              // [nbins][nl][nl]
     int unit_tof;            // one bin, every TOF weight exactly 1: AB = the leg's activity integral
 };
@@ -269,23 +274,45 @@ __device__ __forceinline__ void accumulate_loaded(float2 (&acc)[NP], float ca, f
     }
 }
 
-// Table offset of x: floor(x) for |x| < 2^22 (a round-down add of 1.5 * 2^23
-// leaves it in the mantissa), with numpy's wrap of negative indices (:521,
-// :527).  The result may still lie outside 0..8000 (the reference's
-// IndexError); the caller compares it with its bound.
-__device__ __forceinline__ int table_offset(float x)
+// floor(x) for |x| < 2^22: a round-down add of 1.5 * 2^23 leaves it in the
+// mantissa.
+__device__ __forceinline__ int floor_small(float x)
 {
-    const int t = __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
-    return t < 0 ? t + kTofEntries : t;
+    return __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
 }
 
-// Offset index of the factored path's hot loop: floor(x) when it lies in
-// 0..tsafe-1, else kZeroEntry (weights 0) with the miss noted in far.  A
-// negative floor(x) counts as a miss here too; far_voxel then applies
-// numpy's wrap to it.
-__device__ __forceinline__ int lookup_offset(float x, int tsafe, bool& far)
+// floor(uh + ul + sigma (rh + rl)), sigma = +-1, for |uh + sigma rh| < 2^22
+// and low parts far below 1: the TOF offset of a voxel from float-pair
+// distances (about 44 bits), which takes the reference's FP64 column (:520,
+// :526) except within about 1e-9 ps of a column boundary.  s = uh + sigma rh
+// and its rounding error e come from a two-sum; floor(s) moves by one when
+// the low parts carry the sum across an integer.  With f = s - floor(s)
+// (exact for s >= 0: s and floor(s) lie within a factor of two) that is
+// low >= 1 - f or low < -f, both compared exactly (1 - f is exact too).
+__device__ __forceinline__ int floor_pair(float uh, float ul, float sigma, float rh, float rl)
 {
-    const int t = __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
+    const float b = sigma * rh;  // exact
+    const float s = uh + b;
+    const float bb = s - uh;
+    const float e = (uh - (s - bb)) + (b - bb);
+    const float low = e + fmaf(sigma, rl, ul);
+    const float y = __fadd_rd(s, 12582912.0f);
+    const int t = __float_as_int(y) - 0x4B400000;
+    const float f = s - (y - 12582912.0f);  // s - floor(s)
+    return t + (low >= 1.f - f ? 1 : 0) - (low < -f ? 1 : 0);
+}
+
+// numpy's wrap of a negative table index (:521, :527).  The result may still
+// lie outside 0..8000 (the reference's IndexError); the caller compares it
+// with its bound.
+__device__ __forceinline__ int wrap_offset(int t) { return t < 0 ? t + kTofEntries : t; }
+
+// Offset index of the factored path's hot loop: t (a raw floor) when it lies
+// in 0..tsafe-1, else kZeroEntry (weights 0) with the miss noted in far.  A
+// negative t counts as a miss here too; far_voxel then applies numpy's wrap
+// to it.
+__device__ __forceinline__ int lookup_offset(int t, int tsafe, bool& far)
+{
     const bool ok = (unsigned)t < (unsigned)tsafe;
     far |= !ok;
     return ok ? t : kZeroEntry;
@@ -313,17 +340,17 @@ __device__ __forceinline__ void accumulate_per_bin(float2 (&acc)[NP], float ca, 
     }
 }
 
-// A voxel the factored path's hot loop left out (floor(x) outside
-// 0..T.tsafe-1), at x: numpy's wrap of a negative index; a wrapped offset
-// below T.tsafe takes the factored weights, one far past the last bin the
-// per-bin weights from its (Y, 0) entry and its bin n, and one outside the
-// table is flagged and adds nothing.  Runs only for such voxels.
+// A voxel the factored path's hot loop left out (raw floor traw outside
+// 0..T.tsafe-1): numpy's wrap of a negative index; a wrapped offset below
+// T.tsafe takes the factored weights, one far past the last bin the per-bin
+// weights from its (Y, 0) entry and its bin n, and one outside the table is
+// flagged and adds nothing.  Runs only for such voxels.
 template <int NP, bool ODD>
-__device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, float x, const float2* sAR,
+__device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, int traw, const float2* sAR,
                                           const unsigned char* sN, const float* sG, const TofConst& T,
                                           bool& tof_bad)
 {
-    const int t = table_offset(x);
+    const int t = wrap_offset(traw);
     if ((unsigned)t >= (unsigned)kTofEntries) {
         tof_bad = true;
         return;
@@ -338,30 +365,27 @@ __device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, float x, 
     accumulate_per_bin<NP, ODD>(acc, ca, sAR[ar_slot(t)].x, n, beta, T);
 }
 
-// Adds ca * w_b(t) to every bin b, t = floor(x) (an offset index into the
-// reference's 8001-entry TOF table, :520-528), where the factored weights are
-// not used (one bin, or bins too wide for them).  w_b is rebuilt from the
-// largest weight of the column, 2^Y at bin n, and the Gaussian's exact ratio
-// between bins: log2 w_b = Y - d (beta + gamma d), d = n - b; NP = number of
-// bin pairs.
+// Adds ca * w_b(t) to every bin b, t = traw (a raw floor: an offset index
+// into the reference's 8001-entry TOF table, :520-528), where the factored
+// weights are not used (one bin, or bins too wide for them).  w_b is rebuilt
+// from the largest weight of the column, 2^Y at bin n, and the Gaussian's
+// exact ratio between bins: log2 w_b = Y - d (beta + gamma d), d = n - b;
+// NP = number of bin pairs.
 template <int NP, bool SINGLE, bool ODD>
-__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, float x,
+__device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, int traw,
                                                  const float2* sAR, const unsigned char* sN,
                                                  const TofConst& T, bool& tof_bad)
 {
-    // floor(x) for |x| < 2^22: round-down add of 1.5*2^23 leaves it in the mantissa
-    const float y = __fadd_rd(x, 12582912.0f);
-    int t = __float_as_int(y) - 0x4B400000;
-    float off = y - 12586912.0f;  // t - 4000, exact
+    int t = traw;
     if ((unsigned)t >= (unsigned)kTofEntries) {
         if (t < 0 && t + kTofEntries >= 0) {  // numpy negative index wraps (:521, :527)
             t += kTofEntries;
-            off = (float)(t - kTimeRange);
         } else {
             tof_bad = true;
             return;
         }
     }
+    const float off = (float)(t - kTimeRange);  // exact
     const float Y = sAR[ar_slot(t)].x;
     const float n = (float)sN[t];
     // beta = 2 kappa w (off - s_n), s_n = s0 + n w
@@ -381,10 +405,13 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, fl
 // so both divide by the same per-slice count (:555-557).  All lanes walk the
 // same voxel list: 32 voxels at a time are staged in the warp's shared
 // buffer and read back as broadcasts, so the trip count is uniform.
+// KAHAN: the precision launch, which also forms each voxel's TOF offset from
+// float-pair distances (floor_pair; the samples' low floats staged in vlo).
 template <int NP, bool SINGLE, bool ODD, bool KAHAN>
 __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, int s_first, int s_count,
                                           int lw, int chunk, int lane, const float2* sAR,
-                                          const unsigned char* sN, const float* sG, float2* vbuf, float2* kahan,
+                                          const unsigned char* sN, const float* sG, float2* vbuf, float* vlo,
+                                          float2* kahan,
                                           bool& tof_bad, bool& energy_bad, bool& nonfinite,
                                           unsigned long long& walked, unsigned long long& npairs)
 {
@@ -477,7 +504,22 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
             }
         }
         // TOF offset index: floor(2((sv1-sv2)/2 -/+ r)/c + 0.5) + 4000 (:520, :526)
-        const float u = fmaf(-sigma * (Aw.x - Ap.x), inv_c, 4000.5f);
+        float u = fmaf(-sigma * (Aw.x - Ap.x), inv_c, 4000.5f), ul = 0.f;
+        if constexpr (KAHAN) {
+            // u = 4000.5 - sigma (sv_w - sv_p) / c as a float pair from the
+            // distances' float pairs (high in legA.x, low in legC.w)
+            const float dw = C.legC[lo + lw].w, dp = C.legC[lo + lp].w;
+            const float dh = Aw.x - Ap.x, dv = dh - Aw.x;
+            const float dl = ((Aw.x - (dh - dv)) + (-Ap.x - dv)) + (dw - dp);  // sv_w - sv_p = dh + dl
+            const float ich = (float)(1.0 / kLightCmPerPs);
+            const float icl = (float)(1.0 / kLightCmPerPs - (double)ich);
+            const float ph = dh * ich;
+            const float pl = fmaf(dh, ich, -ph) + fmaf(dh, icl, dl * ich);  // (sv_w - sv_p) / c = ph + pl
+            const float b = -sigma * ph;
+            u = 4000.5f + b;
+            const float bb = u - 4000.5f;
+            ul = ((4000.5f - (u - bb)) + (b - bb)) - sigma * pl;
+        }
         if (SINGLE && C.unit_tof) {
             // weights of exactly 1: sum(a_v * 1) is the walking leg's activity integral
             acc[0].x = fmaf(c, Aw.y, acc[0].x);
@@ -485,9 +527,19 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
             const int nw = __float_as_int(Bw.w);
             if (c != 0.f) walked += nw;
             const float2* vw = C.vox + (lo + lw) * C.cap;
+            // raw floor of the TOF offset of staged voxel j, v = vbuf[j]
+            auto offset_of = [&](const float2& v, int j) {
+                if constexpr (KAHAN)
+                    return floor_pair(u, ul, sigma, v.y, vlo[j]);
+                else
+                    return floor_small(fmaf(sigma, v.y, u));
+            };
             for (int k0 = 0; k0 < nw; k0 += 32) {
                 __syncwarp();
-                if (k0 + lane < nw) vbuf[lane] = vw[k0 + lane];
+                if (k0 + lane < nw) {
+                    vbuf[lane] = vw[k0 + lane];
+                    if constexpr (KAHAN) vlo[lane] = C.vox_lo[(lo + lw) * C.cap + k0 + lane];
+                }
                 __syncwarp();
                 const int jn = min(32, nw - k0);
                 if (c != 0.f) {
@@ -497,15 +549,16 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                         // outside the table, add nothing here; they are noted and taken
                         // afterwards)
                         bool anyfar = false;
-                        float2 v = vbuf[0];
-                        int t = lookup_offset(fmaf(sigma, v.y, u), T.tsafe, anyfar);
+                        const float2 v = vbuf[0];
+                        int t = lookup_offset(offset_of(v, 0), T.tsafe, anyfar);
                         float2 ar = sAR[ar_slot(t)];
                         int nb = __float_as_int(ar.x) & T.nmask;
                         float ca = c * v.x;
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
-                            const float2 v1 = vbuf[j + 1 < jn ? j + 1 : j];
-                            const int t1 = lookup_offset(fmaf(sigma, v1.y, u), T.tsafe, anyfar);
+                            const int j1 = j + 1 < jn ? j + 1 : j;
+                            const float2 v1 = vbuf[j1];
+                            const int t1 = lookup_offset(offset_of(v1, j1), T.tsafe, anyfar);
                             const float2 ar1 = sAR[ar_slot(t1)];
                             const int nb1 = __float_as_int(ar1.x) & T.nmask;
                             accumulate_loaded<NP>(acc, ca, ar, nb, sG);
@@ -516,18 +569,16 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                         if (anyfar) {  // rare: this batch's voxels outside the factored range
                             for (int j = 0; j < jn; ++j) {
                                 const float2 vf = vbuf[j];
-                                const float xf = fmaf(sigma, vf.y, u);
-                                const int tf = __float_as_int(__fadd_rd(xf, 12582912.0f)) - 0x4B400000;
+                                const int tf = offset_of(vf, j);
                                 if ((unsigned)tf >= (unsigned)T.tsafe)
-                                    far_voxel<NP, ODD>(acc, c * vf.x, xf, sAR, sN, sG, T, tof_bad);
+                                    far_voxel<NP, ODD>(acc, c * vf.x, tf, sAR, sN, sG, T, tof_bad);
                             }
                         }
                     } else {
 #pragma unroll 2
                         for (int j = 0; j < jn; ++j) {
                             const float2 v = vbuf[j];
-                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, fmaf(sigma, v.y, u), sAR, sN, T,
-                                                              tof_bad);
+                            accumulate_voxel<NP, SINGLE, ODD>(acc, c * v.x, offset_of(v, j), sAR, sN, T, tof_bad);
                         }
                     }
                 }

@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(pair_block_warps(NP, KAHAN) * 32, MINB) pair_k
     unsigned char* sN = smem + kSmemNOff;
     float2* vbuf = reinterpret_cast<float2*>(smem + kSmemVbufOff) + (threadIdx.x >> 5) * 32;
     float* sG = reinterpret_cast<float*>(smem + kSmemGOff);
+    float* vlo = KAHAN ? reinterpret_cast<float*>(smem + kSmemVloOff) + (threadIdx.x >> 5) * 32 : nullptr;
     float2* kahan = reinterpret_cast<float2*>(smem + pair_smem_kahan_off(P.ctx.nbins)) + threadIdx.x;
     load_pair_tables(P.tof_log2w, P.T, sAR, sN, sG);
     __syncthreads();
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__(pair_block_warps(NP, KAHAN) * 32, MINB) pair_k
         const int slice = (int)(task / per_slice);
         const int rem = (int)(task % per_slice);
         walk_task<NP, SINGLE, ODD, KAHAN>(P.ctx, P.T, P.slice_first[slice], P.slice_count[slice],
-                                          rem / P.nchunks, rem % P.nchunks, lane, sAR, sN, sG, vbuf, kahan,
+                                          rem / P.nchunks, rem % P.nchunks, lane, sAR, sN, sG, vbuf, vlo, kahan,
                                           tof_bad, energy_bad, nonfinite, walked, npairs);
     }
     finish_pairs(lane, tof_bad, energy_bad, nonfinite, walked, npairs, P.status, P.work);

@@ -210,7 +210,7 @@ struct StageTimer {
 thread_local StageTimer g_timer;
 
 struct WsLayout {
-    size_t legA, legB, legC, vox, counter, total;
+    size_t legA, legB, legC, vox, vox_lo, counter, total;
 };
 
 WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
@@ -226,7 +226,10 @@ WsLayout ws_layout(const sss_tof_problem& p, long long wave_points)
     w.legC = off;
     off = align_up(off + sizeof(float4) * wave_points * nl);
     w.vox = off;  // no voxel lists when every TOF weight is 1
-    if (!(p.flags & SSS_FLAG_UNIT_TOF)) off = align_up(off + sizeof(float2) * wave_points * cap * nl);
+    const bool lists = !(p.flags & SSS_FLAG_UNIT_TOF);
+    if (lists) off = align_up(off + sizeof(float2) * wave_points * cap * nl);
+    w.vox_lo = off;  // the samples' low floats: the precision (Kahan) launch only
+    if (lists && (p.flags & SSS_FLAG_KAHAN)) off = align_up(off + sizeof(float) * wave_points * cap * nl);
     w.counter = off;
     off = align_up(off + 256);
     w.total = off;
@@ -384,6 +387,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     LP.legB = (float4*)(ws + w.legB);
     LP.legC = (float4*)(ws + w.legC);
     LP.vox = (p->flags & SSS_FLAG_UNIT_TOF) ? nullptr : (float2*)(ws + w.vox);
+    LP.vox_lo = (LP.vox && (p->flags & SSS_FLAG_KAHAN)) ? (float*)(ws + w.vox_lo) : nullptr;
     LP.status = status;
 
     PairParams PP;
@@ -405,6 +409,7 @@ extern "C" int sss_tof_run(const sss_tof_problem* p, const double* points, int64
     C.legB = LP.legB;
     C.legC = LP.legC;
     C.vox = LP.vox;
+    C.vox_lo = LP.vox_lo;
     C.unit_tof = (p->flags & SSS_FLAG_UNIT_TOF) != 0;
     C.out = out;
     PP.T = tof_const(*p);

@@ -354,6 +354,16 @@ __device__ __forceinline__ float unfix61_abs(int64_t x)
     return __uint_as_float(((uint32_t)(129 - lz) << 23) | (man & 0x7FFFFFu));
 }
 
+// The same as a double (53 bits, truncated).
+__device__ __forceinline__ double unfix61_abs_d(int64_t x)
+{
+    const uint64_t u = x < 0 ? (uint64_t)(-x) : (uint64_t)x;
+    if (u == 0) return 0.0;
+    const int lz = __clzll((long long)u);
+    const uint64_t man = (u << lz) >> 11;  // 53 bits, the leading one at bit 52
+    return __longlong_as_double((long long)(((uint64_t)(1025 - lz) << 52) | (man & ((1ull << 52) - 1))));
+}
+
 // Walk the voxels.  For voxel k (0-based) the visitor receives
 // (k, 1-based linear index, t at entry, t at exit).  Returns the voxel
 // count, or -1 if the reference would overrun its Nx+Ny+Nz storage
