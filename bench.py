@@ -284,7 +284,9 @@ def run_ours(args, rank, world, local_rank):
            "h2d_bytes_per_step": dropin["h2d_bytes"], "d2h_bytes_per_step": dropin["d2h_bytes"],
            "ms_per_step": dropin["seconds"] * 1e3,
            "path": "opensss_gb300.SingleScatterSimulationTOF (the drop-in): NumPy maps in, the reference's "
-                   f"dense {dropin['shape']} float32 array out (pageable host memory in, page-locked out)"}
+                   f"dense {dropin['shape']} float32 array out (pageable host memory in, page-locked out; the "
+                   "host's cores clear the result during the simulation and the GPU writes its sampled cells "
+                   "over the host link)"}
     L.sss_set_timing(0)
 
     if rank != 0:

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SSS300_ABI_VERSION 5
+#define SSS300_ABI_VERSION 6
 
 enum {
     SSS_OK = 0,
@@ -195,6 +195,14 @@ int sss_tof_densify(const float *compact, int32_t nbins, int32_t nru, int32_t nd
  * Needs nru*nru a multiple of 4 and a 16-byte aligned dense. */
 int sss_tof_densify_full(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
                          const int32_t *cell_pair, float *dense, int32_t *status, void *stream);
+
+/* As sss_tof_densify_full, but only the cells of sampled pairs are written
+ * (every element of them); the other cells of dense are left as they are.
+ * For a destination whose other cells already hold zeros: the drop-in copies
+ * zeros into its page-locked result while the simulation runs and then writes
+ * the sampled cells (well under 1% of the array) with this call. */
+int sss_tof_densify_cells(const float *compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
+                          const int32_t *cell_pair, float *dense, int32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Batched simulation (no counterpart in the reference, which runs one

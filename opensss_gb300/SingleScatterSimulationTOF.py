@@ -36,7 +36,8 @@ class _DropIn:
         self.engine = eng
         self.full = (eng.nru * eng.nru) % 4 == 0
         if self.full:
-            # every dense element is written straight into the page-locked result
+            # the result is page-locked host memory: the host clears it during
+            # the simulation, then the GPU writes the sampled cells into it
             self.cells = as_device(geometry.dense_cell_pairs(lor, eng.dets_np, eng.nd), torch.int32, eng.device)
         else:
             lor = geometry.check_dense_lor(lor, eng.dets_np, eng.nd)
@@ -85,20 +86,31 @@ def SingleScatterSimulationTOF(ActivityMap, AttenuationMap, ImageSize, Geometry,
 
     The result is a fresh float32 array the caller owns.  Its memory is
     page-locked host memory from torch's pinned-memory cache, which the GPU
-    writes directly, zeros included, over the host link (when NRU^2 is a
-    multiple of 4; else the dense array is built on the device and copied);
-    it returns to the cache when the array is dropped."""
+    writes directly over the host link (when NRU^2 is a multiple of 4; else
+    the dense array is built on the device and copied): the host clears it
+    while the simulation runs, and the GPU writes the sampled cells.  The
+    memory returns to the cache when the array is dropped."""
     t0 = time.time()
     d = _drop_in(Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable,
                  EnergyResolution, EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution,
                  TOFRange, NrBins, device)
     eng = d.engine
-    compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
     shape = (eng.nbins, eng.nd + 1, eng.nd // 2, eng.nru * eng.nru)
     host = torch.empty(shape, dtype=torch.float32, pin_memory=True)
     if d.full:
-        eng.densify_full(compact, d.cells, host)
+        # Over 99% of the dense layout is zero: the host's cores clear the
+        # result (torch's parallel fill, in a thread of its own) while the GPU
+        # simulates, and the GPU then writes the sampled cells alone over the
+        # host link instead of the whole array.
+        clearing = threading.Thread(target=host.zero_)
+        clearing.start()
+        try:
+            compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
+        finally:
+            clearing.join()
+        eng.densify_full(compact, d.cells, host, sampled_only=True)
     else:
+        compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
         eng.densify(compact, d.lor, out=d.dense)
         host.copy_(d.dense)
     eng.check_status()

@@ -14,7 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libsss300.so")
 
 SSS_OK = 0
-ABI_VERSION = 5  # SSS300_ABI_VERSION of include/sss300.h
+ABI_VERSION = 6  # SSS300_ABI_VERSION of include/sss300.h
 ERROR_NAMES = {
     1: "SSS_ERR_INVALID", 2: "SSS_ERR_CUDA", 3: "SSS_ERR_OVERRUN", 4: "SSS_ERR_TOF_RANGE",
     5: "SSS_ERR_ENERGY", 6: "SSS_ERR_VOXEL", 7: "SSS_ERR_WORKSPACE", 8: "SSS_ERR_CAPACITY",
@@ -86,6 +86,7 @@ SIGNATURES = {
                               _P, _P, _P]),
     "sss_tof_densify": (C.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P]),
     "sss_tof_densify_full": (C.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _P, _P]),
+    "sss_tof_densify_cells": (C.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _P, _P]),
     "sss_batch_plan": (C.c_int, [C.POINTER(TofProblem), _I32, _P, _P, C.c_size_t, _P,
                                  C.POINTER(_P), _P]),
     "sss_batch_run": (C.c_int, [_P, _P]),

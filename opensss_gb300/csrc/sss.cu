@@ -155,6 +155,9 @@ __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru
 // slices (one 16-byte store) a thread: cell (rad, ang) holds sampled pair
 // cell_pair[cell] = di1 * ndu + di2 (di1 <= di2) or -1.  The destination
 // may be page-locked host memory, which the GPU writes over its host link.
+// SAMPLED_ONLY: the cells of sampled pairs alone (every element of them),
+// for a destination whose other cells already hold zeros.
+template <bool SAMPLED_ONLY>
 __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, long long ncell,
                                     const int32_t* __restrict__ cell_pair, float* __restrict__ dense,
                                     int32_t* status)
@@ -173,6 +176,9 @@ __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, in
         const int di1 = pair / ndu, di2 = pair % ndu;
         if (pair < -1 || pair >= ndu * ndu || (pair >= 0 && di1 > di2)) {  // the caller's cell table
             raise_error(status, kErrTable);
+            if (SAMPLED_ONLY) continue;
+        } else if (SAMPLED_ONLY && pair < 0) {
+            continue;
         } else if (pair >= 0) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -511,20 +517,21 @@ extern "C" int sss_tof_densify(const float* compact, int32_t nbins, int32_t nru,
     return sss_check_launch("densify_kernel");
 }
 
-extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
-                                    const int32_t* cell_pair, float* dense, int32_t* status, void* stream)
+namespace {
+
+int densify_full(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd, const int32_t* cell_pair,
+                 float* dense, int32_t* status, void* stream, bool sampled_only, const char* who)
 {
     if (!compact || !cell_pair || !dense || !status || nbins < 1 || nru < 1 || ndu < 1 || nd < 2)
-        return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify_full: bad argument");
+        return sss_set_error(SSS_ERR_INVALID, "%s: bad argument", who);
     if ((nru * nru) % 4 != 0 || (uintptr_t)dense % 16 != 0)
-        return sss_set_error(SSS_ERR_INVALID,
-                             "sss_tof_densify_full: needs nru*nru a multiple of 4 and a 16-byte aligned output");
+        return sss_set_error(SSS_ERR_INVALID, "%s: needs nru*nru a multiple of 4 and a 16-byte aligned output", who);
     // the destination must be memory the device can address: device memory,
     // or host memory page-locked through CUDA (written at its device address)
     cudaPointerAttributes attr;
     if (cudaPointerGetAttributes(&attr, dense) != cudaSuccess) {
         cudaGetLastError();
-        return sss_set_error(SSS_ERR_INVALID, "sss_tof_densify_full: output pointer unknown to CUDA");
+        return sss_set_error(SSS_ERR_INVALID, "%s: output pointer unknown to CUDA", who);
     }
     float* dst = nullptr;
     if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)
@@ -532,8 +539,7 @@ extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t
     else if (attr.type == cudaMemoryTypeHost && attr.devicePointer)
         dst = (float*)attr.devicePointer;
     else
-        return sss_set_error(SSS_ERR_INVALID,
-                             "sss_tof_densify_full: output must be device memory or page-locked host memory");
+        return sss_set_error(SSS_ERR_INVALID, "%s: output must be device memory or page-locked host memory", who);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -541,9 +547,29 @@ extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t
     const long long total4 = (long long)nbins * ncell * nru * nru / 4;
     const long long want = (total4 + 255) / 256;
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
-    densify_full_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair, dst,
-                                                                      status);
+    if (sampled_only)
+        densify_full_kernel<true><<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair,
+                                                                            dst, status);
+    else
+        densify_full_kernel<false><<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell,
+                                                                             cell_pair, dst, status);
     return sss_check_launch("densify_full_kernel");
+}
+
+}  // namespace
+
+extern "C" int sss_tof_densify_full(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
+                                    const int32_t* cell_pair, float* dense, int32_t* status, void* stream)
+{
+    return densify_full(compact, nbins, nru, ndu, nd, cell_pair, dense, status, stream, false,
+                        "sss_tof_densify_full");
+}
+
+extern "C" int sss_tof_densify_cells(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, int32_t nd,
+                                     const int32_t* cell_pair, float* dense, int32_t* status, void* stream)
+{
+    return densify_full(compact, nbins, nru, ndu, nd, cell_pair, dense, status, stream, true,
+                        "sss_tof_densify_cells");
 }
 
 // ---------------------------------------------------------------- no-allocation scatter points

@@ -147,8 +147,9 @@ class TofSSS:
         like the oracle's bounded samples).  ``points`` (ascending scatter-point
         numbers in lattice order) restricts it to those points, each z-slice
         normalised over its kept points (the oracle's ``points`` sample).
-        ``kahan`` sums each pair's per-point terms with Kahan's compensated
-        addition."""
+        ``kahan`` selects the precision launch (``SSS_FLAG_KAHAN``): each
+        pair's per-point terms summed with Kahan's compensated addition, and
+        the TOF offsets formed from float-pair distances and samples."""
         dev = self.device
         shape = tuple(int(s) for s in ActivityMap.shape)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
@@ -225,23 +226,26 @@ class TofSSS:
         return self._ws
 
     # ------------------------------------------------------------------
-    def densify_full(self, compact: torch.Tensor, cell_pair: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+    def densify_full(self, compact: torch.Tensor, cell_pair: torch.Tensor, out: torch.Tensor,
+                     sampled_only: bool = False) -> torch.Tensor:
         """Leg-pair layout -> every element of the reference layout
         [B, ND+1, ND//2, NRU^2] float32, zeros included, into ``out``: a CUDA
         tensor or a page-locked host tensor (written by the GPU over the host
         link, no separate copy).  ``cell_pair``: CUDA int32 table of
-        ``geometry.dense_cell_pairs``.  Asynchronous on the current stream; a
+        ``geometry.dense_cell_pairs``.  ``sampled_only``: write the cells of
+        sampled pairs alone (``sss_tof_densify_cells``), the other cells of
+        ``out`` holding zeros already.  Asynchronous on the current stream; a
         table entry out of range is OR-ed into the engine's status word
         (``check_status``)."""
-        shape =(self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru)
+        shape = (self.nbins, self.nd + 1, self.nd // 2, self.nru * self.nru)
         if tuple(out.shape) != shape or out.dtype != torch.float32 or not out.is_contiguous():
             raise ValueError(f"densify_full: out must be contiguous float32 {shape}")
         if not (out.is_cuda or out.is_pinned()):
             raise ValueError("densify_full: out must be a CUDA tensor or page-locked host memory")
         st = torch.cuda.current_stream(self.device)
-        _lib.check(_lib.lib().sss_tof_densify_full(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd,
-                                                   _ptr(cell_pair), _ptr(out), _ptr(self._status),
-                                                   C.c_void_p(st.cuda_stream)))
+        fn = _lib.lib().sss_tof_densify_cells if sampled_only else _lib.lib().sss_tof_densify_full
+        _lib.check(fn(_ptr(compact), self.nbins, self.nru, self.ndu, self.nd, _ptr(cell_pair), _ptr(out),
+                      _ptr(self._status), C.c_void_p(st.cuda_stream)))
         return out
 
     def densify(self, compact: torch.Tensor, lor, out: torch.Tensor | None = None) -> torch.Tensor:

@@ -475,6 +475,15 @@ def test_full_densify_to_device_and_pinned_host(cuda_ok, att_table):
         eng.densify_full(lp, cells, out)
         torch.cuda.synchronize()
         assert np.array_equal(out.cpu().numpy(), ref.astype(np.float32))
+    # sss_tof_densify_cells: the sampled pairs' cells alone, every element of them; the rest is left as it is
+    sampled = cells.cpu().numpy() >= 0
+    for out in (torch.full(shape, 7.0, device="cuda"), torch.full(shape, 7.0).pin_memory()):
+        eng.densify_full(lp, cells, out, sampled_only=True)
+        eng.check_status()
+        got = out.cpu().numpy().reshape(shape[0], -1, shape[3])
+        want = ref.astype(np.float32).reshape(shape[0], -1, shape[3])
+        assert np.array_equal(got[:, sampled], want[:, sampled])
+        assert (got[:, ~sampled] == 7.0).all()
     pageable = np.zeros(shape, np.float32)
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
     rc = _lib.lib().sss_tof_densify_full(C.c_void_p(lp.data_ptr()), pr.nr_bins, pr.nr_rings_used,
