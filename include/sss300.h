@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SSS300_ABI_VERSION 6
+#define SSS300_ABI_VERSION 7
 
 enum {
     SSS_OK = 0,
@@ -299,10 +299,9 @@ int sss_tail_mask_pairs(const int32_t grid[3], const double bounds[6], const flo
  * scatter value is scatters[scat_cell[cell] + scat_ring[slice]] (clamped at
  * 0 when scat_clamp), so an upsampled sinogram can be read straight from
  * the sampled one.  images: device workspace 8 * Nx*Ny*Nz floats, 16-byte
- * aligned: the (P, S) float pairs of every voxel, then its (R, sensitivity)
- * pairs, then a block whose second half holds the (R, sensitivity) pairs of
- * the LORs every bin uses; sums: device 2 doubles; scale: device float, the
- * fitted slope (reference: float32 array of shape (1,)). */
+ * aligned, laid out as sss_backproject_fit_bins's for one bin; sums: device
+ * 2 doubles; scale: device float, the fitted slope (reference: float32 array
+ * of shape (1,)). */
 int sss_backproject_fit(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
                         const double *geometry, const int16_t *lor, const int16_t *sino_order,
                         int32_t af, const float *prompts, const float *randoms, const float *mask_f32,
@@ -332,13 +331,17 @@ int sss_backproject_fit_pairs(const int32_t grid[3], const double bounds[6], int
  * prompts[b*prompt_stride + cell*nslices + slice] and the scatter value
  * scatters[b*scat_stride + scat_cell[cell] + scat_ring[slice]]; randoms and
  * the mask are shared.  Either sino_order (all ring pairs) or pairs (span)
- * is given.  images: device float [nbins + 1][4 * Nx*Ny*Nz], 16-byte aligned:
- * bins 2q and 2q+1 share blocks 2q and 2q+1 as float4 per voxel, (P, S, P, S)
- * then (R, sensitivity, R, sensitivity); an odd last bin keeps float2 (P, S)
- * then (R, sensitivity) pairs in its block; the second half of block nbins
- * holds, as float2, the randoms and sensitivity of the LORs every bin uses,
- * so those are added once; sums: device [nbins][2]; scales: device float
- * [nbins];
+ * is given.  images: device float [nbins + 1][4 * Nx*Ny*Nz], 16-byte aligned.
+ * Per voxel and bin they hold D, the back-projected (prompts - randoms) (the
+ * reference's ActivityImage - RandomImage, summed once), S, the scatter, and
+ * the sensitivity: bins 2q and 2q+1 share blocks 2q and 2q+1 as float4 per
+ * voxel, (D, S, D, S) then (0, sensitivity, 0, sensitivity) of the LORs that
+ * use some bins only; an odd last bin L has float4 (D, S, 0, common
+ * sensitivity) in block L, the common sensitivity counting the LORs every
+ * bin uses, and float2 (0, sensitivity) in the first half of block nbins;
+ * with an even bin count the common sensitivity is float2 (0, sensitivity)
+ * in the second half of block nbins; sums: device [nbins][2]; scales: device
+ * float [nbins];
  * 1 <= nbins <= 64. */
 int sss_backproject_fit_bins(const int32_t grid[3], const double bounds[6], int32_t nr, int32_t nd,
                              const double *geometry, const int16_t *lor, const int16_t *sino_order,

@@ -23,7 +23,7 @@ def _ptr(t):
 
 def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize, ImageSize, Geometry,
                SinogramCoordinates, SinogramOrder, AccelerationFactor, scat_clamp=False,
-               device="cuda", return_images=False, span: bool = False):
+               device="cuda", span: bool = False):
     """All sinogram arguments are CUDA tensors [cell, slice] (float32; mask
     float32, or uint8 meaning mask >= 1).  Returns the scale as a float.
     With ``span``, ``Geometry`` is the expanded geometry, ``SinogramOrder`` the
@@ -66,10 +66,6 @@ def fit_device(prompts, randoms, mask, scatters, scat_cell, scat_ring, GridSize,
             _ptr(scale), _ptr(status), C.c_void_p(st.cuda_stream)))
     st.synchronize()
     _lib.check_status(int(status.item()))
-    if return_images:
-        im = images.reshape(2, 2, nvox, 2)  # [block][(P, S) | (R, sens)][voxel][pair]
-        return float(scale.item()), torch.stack([im[0, 0, :, 0], im[0, 0, :, 1], im[0, 1, :, 0] + im[1, 1, :, 0],
-                                                 im[0, 1, :, 1] + im[1, 1, :, 1]])
     return float(scale.item())
 
 

@@ -14,7 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libsss300.so")
 
 SSS_OK = 0
-ABI_VERSION = 6  # SSS300_ABI_VERSION of include/sss300.h
+ABI_VERSION = 7  # SSS300_ABI_VERSION of include/sss300.h
 ERROR_NAMES = {
     1: "SSS_ERR_INVALID", 2: "SSS_ERR_CUDA", 3: "SSS_ERR_OVERRUN", 4: "SSS_ERR_TOF_RANGE",
     5: "SSS_ERR_ENERGY", 6: "SSS_ERR_VOXEL", 7: "SSS_ERR_WORKSPACE", 8: "SSS_ERR_CAPACITY",

@@ -256,6 +256,34 @@ __device__ __forceinline__ float fit_scatter(const FitParams& P, int b, long lon
     return P.scat_clamp ? fmaxf(sv, 0.f) : sv;
 }
 
+// The fit's images, device float [nbins + 1][4 nvox].  Per voxel and bin:
+// D, the sum over the LORs through the voxel of (prompts - randoms) / voxels,
+// S, that of scatter / voxels, and the sensitivity, their count
+// (BackProjection.py:99-110).  The reference keeps prompts and randoms apart
+// and subtracts them after dividing by the sensitivity (:191-204); D is that
+// difference summed once, so that it costs no atomic of its own.
+//   bins 2q, 2q+1: block 2q float4 (D, S, D, S); block 2q+1 float4
+//     (0, sens, 0, sens) of the LORs that use some of the bins only;
+//   an odd last bin L: block L float4 (D, S, 0, common sens), the common
+//     sensitivity counting the LORs every bin uses (one atomic with L's
+//     values); block nbins float2 [0, nvox) (0, sens) of the LORs that use
+//     some bins only;
+//   even bin counts: the common sensitivity in block nbins, float2
+//     [nvox, 2 nvox), (0, sens).
+struct FitImages {
+    float* img;
+    long long nv;
+    int nbins;
+    __device__ float4* pair_ds(int b0) const { return reinterpret_cast<float4*>(img + (long long)b0 * 4 * nv); }
+    __device__ float4* pair_sens(int b0) const
+    {
+        return reinterpret_cast<float4*>(img + (long long)(b0 + 1) * 4 * nv);
+    }
+    __device__ float4* last_ds(int lastb) const { return reinterpret_cast<float4*>(img + (long long)lastb * 4 * nv); }
+    __device__ float2* last_sens() const { return reinterpret_cast<float2*>(img + (long long)nbins * 4 * nv); }
+    __device__ float2* common_sens() const { return last_sens() + nv; }
+};
+
 // A 16-byte shared-memory load issued where it stands: the per-LOR values
 // are re-read at every voxel instead of being held in registers across the
 // walk, which keeps the kernel's register count (and so its occupancy) at that
@@ -333,14 +361,15 @@ __global__ void __launch_bounds__(kBpThreads, NPB > 0 ? 6 : 0) bp_kernel(FitPara
     const float ar = rv / fn;
     bool bad = false;
     if constexpr (NPB > 0) {
-        // (P, S) of bin b from this LOR, divided by the voxel count, as below
+        // (D, S) of bin b from this LOR: prompts minus randoms, and scatter,
+        // each divided by the voxel count, as below
         auto contrib = [&](int b) {
             const float s = P.nbins == 1 ? s0 : m * fit_scatter(P, b, cell, slice);
             const float pv = P.nbins == 1 ? p0 : m * P.prompts[b * P.prompt_stride + c];
-            return make_float2(pv / fn, s / fn);
+            return make_float2(pv / fn - ar, s / fn);
         };
         const int paired = P.nbins & ~1;
-        // this thread's (P, S, P, S) of each bin pair, in its own shared-memory column
+        // this thread's (D, S, D, S) of each bin pair, in its own shared-memory column
         __shared__ float4 s_cps[NPB][kBpThreads];
         unsigned pm = 0;  // bin pairs with a bin this LOR contributes to
 #pragma unroll
@@ -356,11 +385,14 @@ __global__ void __launch_bounds__(kBpThreads, NPB > 0 ? 6 : 0) bp_kernel(FitPara
             s_cps[k][threadIdx.x] = v;
         }
         const int lastb = P.nbins - 1;
-        const bool has_last = (P.nbins & 1) && ((bins >> lastb) & 1ull);
-        const float2 clast = has_last ? contrib(lastb) : make_float2(0.f, 0.f);
+        const bool odd = P.nbins & 1;
+        const bool has_last = odd && ((bins >> lastb) & 1ull);
         const bool every = bins == all;
-        float2* last = reinterpret_cast<float2*>(P.img + (long long)lastb * 4 * P.nvox);
-        float2* common = reinterpret_cast<float2*>(P.img + (long long)P.nbins * 4 * P.nvox) + P.nvox;
+        // the odd last bin's (D, S) with, for LORs every bin uses, one count of
+        // the common sensitivity: one vector atomic
+        const float2 cl = has_last ? contrib(lastb) : make_float2(0.f, 0.f);
+        const float4 clast = make_float4(cl.x, cl.y, 0.f, every ? 1.f : 0.f);
+        const FitImages I{P.img, P.nvox, P.nbins};
         const int walked = ray_walk(P.g, r, P.cap, [&](int, int64_t lin, double, double) {
             const long long v = lin - 1;
             if (v < 0 || v >= P.nvox) {
@@ -370,20 +402,18 @@ __global__ void __launch_bounds__(kBpThreads, NPB > 0 ? 6 : 0) bp_kernel(FitPara
 #pragma unroll
             for (int k = 0; k < NPB; ++k) {
                 if ((pm >> k) & 1u) {
-                    float4* ps4 = reinterpret_cast<float4*>(P.img + (long long)(2 * k) * 4 * P.nvox);
-                    atomicAdd(ps4 + v, lds_v4(&s_cps[k][threadIdx.x]));
-                    if (!every) {  // randoms and sensitivity of these bins
+                    atomicAdd(I.pair_ds(2 * k) + v, lds_v4(&s_cps[k][threadIdx.x]));
+                    if (!every) {  // sensitivity of these bins alone
                         const bool in0 = (bins >> (2 * k)) & 1ull, in1 = (bins >> (2 * k + 1)) & 1ull;
-                        atomicAdd(ps4 + P.nvox + v,
-                                  make_float4(in0 ? ar : 0.f, in0 ? 1.f : 0.f, in1 ? ar : 0.f, in1 ? 1.f : 0.f));
+                        atomicAdd(I.pair_sens(2 * k) + v, make_float4(0.f, in0 ? 1.f : 0.f, 0.f, in1 ? 1.f : 0.f));
                     }
                 }
             }
             if (has_last) {
-                atomicAdd(last + v, clast);
-                if (!every) atomicAdd(last + P.nvox + v, make_float2(ar, 1.0f));
+                atomicAdd(I.last_ds(lastb) + v, clast);
+                if (!every) atomicAdd(I.last_sens() + v, make_float2(0.f, 1.0f));
             }
-            if (every) atomicAdd(common + v, make_float2(ar, 1.0f));  // shared by every bin
+            if (every && !odd) atomicAdd(I.common_sens() + v, make_float2(0.f, 1.0f));  // shared by every bin
         });
         if (bad) raise_error(P.status, kErrVoxel);
         if (walked != n_vox) raise_error(P.status, kErrOverrun);
@@ -397,16 +427,20 @@ __global__ void __launch_bounds__(kBpThreads, NPB > 0 ? 6 : 0) bp_kernel(FitPara
         }
         const double w = P.length_weighted ? div64(ref_length(r, t0, t1), total) : 0.0;
         const float rw = P.length_weighted ? (float)mul64((double)rv, w) : ar;
-        // (P, S) of bin b from this LOR (one bin: the LOR's values, else re-read
-        // per voxel, L1-resident)
+        // (D, S) of bin b from this LOR: prompts minus randoms, and scatter
+        // (one bin: the LOR's values, else re-read per voxel, L1-resident)
         auto contrib = [&](int b) {
             const float s = P.nbins == 1 ? s0 : m * fit_scatter(P, b, cell, slice);
             const float pv = P.nbins == 1 ? p0 : m * P.prompts[b * P.prompt_stride + c];
-            return P.length_weighted ? make_float2((float)mul64((double)pv, w), (float)mul64((double)s, w))
-                                     : make_float2(pv / fn, s / fn);
+            return P.length_weighted
+                       ? make_float2((float)mul64((double)pv, w) - rw, (float)mul64((double)s, w))
+                       : make_float2(pv / fn - rw, s / fn);
         };
-        // Bins 2q and 2q+1 share float4 images, (P, S, P, S) then (R, sens, R, sens):
-        // one vector atomic each for the pair; an odd last bin uses float2 pairs.
+        // Bins 2q and 2q+1 share float4 images, (D, S, D, S) then (0, sens, 0,
+        // sens): one vector atomic each for the pair; an odd last bin has
+        // (D, S, 0, common sens) and a float2 (0, sens) (FitImages).
+        const FitImages I{P.img, P.nvox, P.nbins};
+        const bool every = bins == all, odd = P.nbins & 1;
         const int paired = P.nbins & ~1;
         for (unsigned long long rest = bins; rest;) {
             const int b = __ffsll((long long)rest) - 1;
@@ -416,59 +450,51 @@ __global__ void __launch_bounds__(kBpThreads, NPB > 0 ? 6 : 0) bp_kernel(FitPara
                 rest &= ~(3ull << b0);
                 const float2 c0 = in0 ? contrib(b0) : make_float2(0.f, 0.f);
                 const float2 c1 = in1 ? contrib(b0 + 1) : make_float2(0.f, 0.f);
-                float4* ps4 = reinterpret_cast<float4*>(P.img + (long long)b0 * 4 * P.nvox);
-                atomicAdd(ps4 + v, make_float4(c0.x, c0.y, c1.x, c1.y));
-                if (bins != all)  // randoms and sensitivity of these bins alone
-                    atomicAdd(ps4 + P.nvox + v, make_float4(in0 ? rw : 0.f, in0 ? 1.f : 0.f, in1 ? rw : 0.f,
-                                                            in1 ? 1.f : 0.f));
+                atomicAdd(I.pair_ds(b0) + v, make_float4(c0.x, c0.y, c1.x, c1.y));
+                if (!every)  // sensitivity of these bins alone
+                    atomicAdd(I.pair_sens(b0) + v, make_float4(0.f, in0 ? 1.f : 0.f, 0.f, in1 ? 1.f : 0.f));
             } else {
                 rest &= rest - 1;
-                float2* ps = reinterpret_cast<float2*>(P.img + (long long)b * 4 * P.nvox);
-                atomicAdd(ps + v, contrib(b));
-                if (bins != all) atomicAdd(ps + P.nvox + v, make_float2(rw, 1.0f));
+                const float2 cb = contrib(b);
+                atomicAdd(I.last_ds(b) + v, make_float4(cb.x, cb.y, 0.f, every ? 1.f : 0.f));
+                if (!every) atomicAdd(I.last_sens() + v, make_float2(0.f, 1.0f));
             }
         }
-        if (bins == all) {  // LORs every bin uses share one randoms / sensitivity image
-            float2* rs = reinterpret_cast<float2*>(P.img + (long long)P.nbins * 4 * P.nvox) + P.nvox;
-            atomicAdd(rs + v, make_float2(rw, 1.0f));
-        }
+        if (every && !odd) atomicAdd(I.common_sens() + v, make_float2(0.f, 1.0f));  // shared by every bin
     });
     if (bad) raise_error(P.status, kErrVoxel);
     if (walked != n_vox) raise_error(P.status, kErrOverrun);
 }
 
 // per voxel: Sbp, T (BackProjection.py:191-204); sums of x*T and x*x in FP64;
-// blockIdx.y = bin (images as bp_kernel writes them, sums [bin][2])
+// blockIdx.y = bin (images as FitImages lays them out, sums [bin][2]).  T is
+// D / sens, the reference's ActivityImage / sens - RandomImage / sens.
 __global__ void fit_reduce_kernel(const float* __restrict__ img_all, long long nvox, int nbins,
                                   double* sums_all)
 {
     const int b = blockIdx.y;
-    const bool pair = b < (nbins & ~1);  // float4 images shared with the neighbouring bin
-    const float* blk = img_all + (long long)(pair ? (b & ~1) : b) * 4 * nvox;
-    const float2* common = reinterpret_cast<const float2*>(img_all + (long long)nbins * 4 * nvox) + nvox;
+    const FitImages I{const_cast<float*>(img_all), nvox, nbins};
+    const bool odd = nbins & 1, pair = b < (nbins & ~1);  // float4 images shared with the neighbouring bin
     double* sums = sums_all + 2 * blockIdx.y;
     double sxt = 0.0, sxx = 0.0;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nvox;
          v += (long long)gridDim.x * blockDim.x) {
-        float2 pv, rv;
+        float2 ds;
+        float own;
         if (pair) {
-            const float4 p4 = reinterpret_cast<const float4*>(blk)[v];
-            const float4 r4 = reinterpret_cast<const float4*>(blk)[nvox + v];
-            pv = (b & 1) ? make_float2(p4.z, p4.w) : make_float2(p4.x, p4.y);
-            rv = (b & 1) ? make_float2(r4.z, r4.w) : make_float2(r4.x, r4.y);
+            const float4 p4 = I.pair_ds(b & ~1)[v], s4 = I.pair_sens(b & ~1)[v];
+            ds = (b & 1) ? make_float2(p4.z, p4.w) : make_float2(p4.x, p4.y);
+            own = (b & 1) ? s4.w : s4.y;
         } else {
-            pv = reinterpret_cast<const float2*>(blk)[v];
-            rv = reinterpret_cast<const float2*>(blk)[nvox + v];
+            const float4 l4 = I.last_ds(b)[v];
+            ds = make_float2(l4.x, l4.y);
+            own = I.last_sens()[v].y;
         }
-        const float2 cv = common[v];
-        const float sens = rv.y + cv.y;
-        float sb = pv.y / sens;
-        float ab = pv.x / sens;
-        float rb = (rv.x + cv.x) / sens;
+        const float sens = own + (odd ? I.last_ds(nbins - 1)[v].w : I.common_sens()[v].y);
+        float sb = ds.y / sens;
+        float t = ds.x / sens;
         if (isnan(sb) || isinf(sb)) sb = 0.f;
-        if (isnan(ab) || isinf(ab)) ab = 0.f;
-        if (isnan(rb) || isinf(rb)) rb = 0.f;
-        float t = ab - rb;
+        if (isnan(t) || isinf(t)) t = 0.f;
         if (t < 0.f) t = 0.f;
         const float x = (float)((double)sb * 1e10);  // float32 array * 1e10 (:207)
         sxt += (double)x * (double)t;

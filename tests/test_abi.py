@@ -41,7 +41,7 @@ def test_python_binding_covers_header():
 
 
 def test_abi_version(lib):
-    assert lib.sss_abi_version() == 6
+    assert lib.sss_abi_version() == 7
 
 
 def test_invalid_arguments_fail_before_any_device_work(lib):
