@@ -9,8 +9,6 @@ the GPU through ``libsss300.so``; there is no CPU path.
 
 from __future__ import annotations
 
-import collections
-import hashlib
 import os
 import threading
 import time
@@ -24,10 +22,10 @@ from .engine import TofSSS, as_device
 # Engines of recent calls.  An outer reconstruction loop calls the SSS once
 # per iteration with the same scanner, tables and sampling and a new activity
 # map; the engine (device tables, launch state) and the reference-layout
-# device buffer are kept for such calls, keyed by a SHA-1 of every input but
-# the two maps.
+# device buffer are kept for such calls, found by comparing every input but
+# the two maps with copies kept from the call that built them.
 _CACHE_SIZE = 2
-_cache: "collections.OrderedDict[bytes, _DropIn]" = collections.OrderedDict()
+_cache: "list[tuple[_Inputs, _DropIn]]" = []
 _lock = threading.Lock()
 
 
@@ -47,34 +45,46 @@ class _DropIn:
                                      dtype=torch.float32, device=eng.device)
 
 
-def _key(arrays, scalars, device) -> bytes:
-    h = hashlib.sha1(usedforsecurity=False)
-    for a in arrays:
-        a = np.ascontiguousarray(a)
-        h.update(f"{a.dtype.str}{a.shape}".encode())
-        h.update(a.reshape(-1).view(np.uint8))
-    h.update(repr((scalars, str(device))).encode())
-    return h.digest()
+class _Inputs:
+    """The inputs an engine is built from, kept as contiguous copies: a later
+    call reuses the engine when its inputs are the same bytes (compared in
+    full; a few MB, a fraction of a millisecond)."""
+
+    def __init__(self, arrays, scalars, device):
+        self.arrays = [np.array(a, copy=True, order="C") for a in arrays]
+        self.scalars = (scalars, str(device))
+
+    def same(self, arrays, scalars, device) -> bool:
+        if self.scalars != (scalars, str(device)):
+            return False
+        for mine, a in zip(self.arrays, arrays):
+            a = np.ascontiguousarray(a)
+            if a.dtype != mine.dtype or a.shape != mine.shape:
+                return False
+            words = np.uint64 if a.nbytes % 8 == 0 else np.uint8  # the bytes, compared 8 at a time
+            if not np.array_equal(a.reshape(-1).view(words), mine.reshape(-1).view(words)):
+                return False
+        return True
 
 
 def _drop_in(Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable, EnergyResolution,
              EnergyThreshold, NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution, TOFRange, NrBins,
              device) -> _DropIn:
-    key = _key([Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable, SampleStep],
-               (float(EnergyResolution), float(EnergyThreshold), int(NrRingsUsed), int(NrDetectorsUsed),
-                float(TOFResolution), float(TOFRange), int(NrBins)), device)
+    arrays = [Geometry, SinogramCoordinates, NormalVectors, DetectorSize, AttenuationTable, SampleStep]
+    scalars = (float(EnergyResolution), float(EnergyThreshold), int(NrRingsUsed), int(NrDetectorsUsed),
+               float(TOFResolution), float(TOFRange), int(NrBins))
     with _lock:
-        d = _cache.get(key)
-        if d is not None:
-            _cache.move_to_end(key)
-            return d
+        for i, (inputs, d) in enumerate(_cache):
+            if inputs.same(arrays, scalars, device):
+                _cache.append(_cache.pop(i))  # most recent last
+                return d
     eng = TofSSS(Geometry, NormalVectors, DetectorSize, AttenuationTable, EnergyResolution, EnergyThreshold,
                  NrRingsUsed, NrDetectorsUsed, SampleStep, TOFResolution, TOFRange, NrBins, device=device)
     d = _DropIn(eng, SinogramCoordinates)
     with _lock:
-        _cache[key] = d
+        _cache.append((_Inputs(arrays, scalars, device), d))
         while len(_cache) > _CACHE_SIZE:
-            _cache.popitem(last=False)
+            _cache.pop(0)
     return d
 
 

@@ -155,9 +155,6 @@ __global__ void densify_kernel(const float* __restrict__ cmp, int nbins, int nru
 // slices (one 16-byte store) a thread: cell (rad, ang) holds sampled pair
 // cell_pair[cell] = di1 * ndu + di2 (di1 <= di2) or -1.  The destination
 // may be page-locked host memory, which the GPU writes over its host link.
-// SAMPLED_ONLY: the cells of sampled pairs alone (every element of them),
-// for a destination whose other cells already hold zeros.
-template <bool SAMPLED_ONLY>
 __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, long long ncell,
                                     const int32_t* __restrict__ cell_pair, float* __restrict__ dense,
                                     int32_t* status)
@@ -176,9 +173,6 @@ __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, in
         const int di1 = pair / ndu, di2 = pair % ndu;
         if (pair < -1 || pair >= ndu * ndu || (pair >= 0 && di1 > di2)) {  // the caller's cell table
             raise_error(status, kErrTable);
-            if (SAMPLED_ONLY) continue;
-        } else if (SAMPLED_ONLY && pair < 0) {
-            continue;
         } else if (pair >= 0) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -188,6 +182,43 @@ __global__ void densify_full_kernel(const float* __restrict__ cmp, int nbins, in
             }
         }
         reinterpret_cast<float4*>(dense)[q] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+// The cells of sampled pairs alone, for a destination whose other cells
+// already hold zeros: one warp a cell (the cell's entry read as a broadcast);
+// a sampled cell's nru^2 slices of every bin go out as 16-byte stores, one a
+// lane.  Under 1% of the cells are sampled, so the scan is most of the work
+// and the writes are 0.4% of the layout's bytes.
+__global__ void densify_cells_kernel(const float* __restrict__ cmp, int nbins, int nru, int ndu, long long ncell,
+                                     const int32_t* __restrict__ cell_pair, float* __restrict__ dense,
+                                     int32_t* status)
+{
+    const int nl = nru * ndu, nsino = nru * nru, nq = nsino / 4;
+    const long long plane = (long long)nl * nl;
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long cell = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < ncell; cell += warps) {
+        const int pair = __ldg(cell_pair + cell);
+        if (pair == -1) continue;
+        const int di1 = pair / ndu, di2 = pair % ndu;
+        if (pair < -1 || pair >= ndu * ndu || di1 > di2) {  // the caller's cell table
+            if (lane == 0) raise_error(status, kErrTable);
+            continue;
+        }
+        for (int b = 0; b < nbins; ++b) {
+            float4* dst = reinterpret_cast<float4*>(dense + ((long long)b * ncell + cell) * nsino);
+            const float* src = cmp + b * plane + (long long)di1 * nru * nl + di2 * nru;  // + ri1 * nl + ri2
+            for (int q = lane; q < nq; q += 32) {
+                float v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int sl = 4 * q + k, ri1 = sl / nru, ri2 = sl % nru;
+                    v[k] = (di1 < di2 || ri1 != ri2) ? __ldg(src + (long long)ri1 * nl + ri2) : 0.f;
+                }
+                dst[q] = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
     }
 }
 
@@ -547,12 +578,15 @@ int densify_full(const float* compact, int32_t nbins, int32_t nru, int32_t ndu, 
     const long long total4 = (long long)nbins * ncell * nru * nru / 4;
     const long long want = (total4 + 255) / 256;
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>(want, (long long)sms * 8));
-    if (sampled_only)
-        densify_full_kernel<true><<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair,
-                                                                            dst, status);
-    else
-        densify_full_kernel<false><<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell,
-                                                                             cell_pair, dst, status);
+    if (sampled_only) {
+        const long long cw = (ncell * 32 + 255) / 256;  // one warp a cell
+        const unsigned cb = (unsigned)std::max<long long>(1, std::min<long long>(cw, (long long)sms * 16));
+        densify_cells_kernel<<<cb, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair, dst,
+                                                                   status);
+        return sss_check_launch("densify_cells_kernel");
+    }
+    densify_full_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(compact, nbins, nru, ndu, ncell, cell_pair, dst,
+                                                                  status);
     return sss_check_launch("densify_full_kernel");
 }
 
