@@ -202,7 +202,14 @@ __global__ void __launch_bounds__(128) mask_kernel(MaskParams P)
         });
         if (c < 0) raise_error(P.status, kErrOverrun);
         if (bad) raise_error(P.status, kErrVoxel);
-        acf = P.use_activity ? (sum > 0.0 ? 0.0 : 1.0) : div64(1.0, exp(-sum));  // :144-156
+        if (P.use_activity)
+            acf = sum > 0.0 ? 0.0 : 1.0;  // :153-156
+        else if (nonneg && sum == 0.0)
+            acf = 1.0;  // 1 / exp(-0), exactly
+        else if (nonneg && sum > P.decided)
+            acf = INFINITY;  // past either rule's bound: not masked (the factor's value is not needed)
+        else
+            acf = div64(1.0, exp(-sum));  // :144-148
     }
     // :150-161 (ACF == 1), or the caller's bound on the factor; one LOR per (cell, slice)
     const bool tail = (P.acf_below > 0.0 && !P.use_activity) ? acf < P.acf_below : acf == 1.0;
