@@ -112,12 +112,22 @@ def SingleScatterSimulationTOF(ActivityMap, AttenuationMap, ImageSize, Geometry,
         # result (torch's parallel fill, in a thread of its own) while the GPU
         # simulates, and the GPU then writes the sampled cells alone over the
         # host link instead of the whole array.
-        clearing = threading.Thread(target=host.zero_)
+        failed = []
+
+        def clear():
+            try:
+                host.zero_()
+            except BaseException as e:  # noqa: BLE001 - re-raised in the calling thread
+                failed.append(e)
+
+        clearing = threading.Thread(target=clear)
         clearing.start()
         try:
             compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
         finally:
             clearing.join()
+        if failed:
+            raise failed[0]
         eng.densify_full(compact, d.cells, host, sampled_only=True)
     else:
         compact = eng.run(ActivityMap, AttenuationMap, ImageSize)
