@@ -29,10 +29,7 @@ constexpr int kGRow = 68;
 // Shared memory of a pair block, in this order:
 //   ar    float2 [8001]  (A, r) of each TOF offset (factored weights; A carries
 //         the nearest bin n in its low mantissa bits) or (Y, 0), then one
-//         entry (0, 0) at kZeroEntry (factored weights of exactly 0); entry t
-//         sits at ar_slot(t), one spare slot after every 16, so that lanes
-//         whose offsets differ by 16 (which would share a bank pair) do not
-//         collide
+//         entry (0, 0) at kZeroEntry (factored weights of exactly 0)
 //   n     u8     [8001]  bin of the column's largest weight
 //   vbuf  float2 [warps][32]  staged voxels of each warp's walk; a
 //         Kahan-compensated launch (kKahanWarps warps) keeps the low floats of
@@ -41,8 +38,7 @@ constexpr int kGRow = 68;
 //   kahan float2 [2 NP][32 kKahanWarps]  (Kahan-compensated launches only,
 //         which run kKahanWarps warps so that 64 bins still fit)
 constexpr int kZeroEntry = kTofEntries;  // the (0, 0) entry after the table
-__host__ __device__ constexpr int ar_slot(int t) { return t + (t >> 4); }
-constexpr int kSmemNOff = (8 * (ar_slot(kZeroEntry) + 1) + 15) & ~15;
+constexpr int kSmemNOff = (8 * (kZeroEntry + 1) + 15) & ~15;
 constexpr int kSmemVbufOff = (kSmemNOff + kTofEntries + 15) & ~15;
 constexpr int kSmemGOff = kSmemVbufOff + 8 * 32 * kPairWarps;
 constexpr int kSmemVloOff = kSmemVbufOff + 8 * 32 * kKahanWarps;  // Kahan launches only
@@ -171,12 +167,12 @@ __device__ __forceinline__ void load_pair_tables(const float* g, const TofConst&
                 const double k = floor(e);
                 a = ldexpf(exp2f((float)(e - k)), (int)k);
             }
-            sAR[ar_slot(i)] = make_float2(pack_bin(a, (int)n, T.nmask), exp2f(beta));
+            sAR[i] = make_float2(pack_bin(a, (int)n, T.nmask), exp2f(beta));
         } else {
-            sAR[ar_slot(i)] = make_float2(Y, 0.f);
+            sAR[i] = make_float2(Y, 0.f);
         }
     }
-    if (threadIdx.x == 0) sAR[ar_slot(kZeroEntry)] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0) sAR[kZeroEntry] = make_float2(0.f, 0.f);
     if (T.factored)
         for (int i = threadIdx.x; i < T.nbins * kGRow; i += blockDim.x) {
             const int n = i / kGRow, b = i % kGRow;
@@ -356,13 +352,13 @@ __device__ __forceinline__ void far_voxel(float2 (&acc)[NP], float ca, int traw,
         return;
     }
     if (t < T.tsafe) {
-        const float2 ar = sAR[ar_slot(t)];
+        const float2 ar = sAR[t];
         accumulate_loaded<NP>(acc, ca, ar, __float_as_int(ar.x) & T.nmask, sG);
         return;
     }
     const float n = (float)sN[t];
     const float beta = T.kappa2w * ((float)(t - kTimeRange) - fmaf(n, T.w, T.s0));
-    accumulate_per_bin<NP, ODD>(acc, ca, sAR[ar_slot(t)].x, n, beta, T);
+    accumulate_per_bin<NP, ODD>(acc, ca, sAR[t].x, n, beta, T);
 }
 
 // Adds ca * w_b(t) to every bin b, t = traw (a raw floor: an offset index
@@ -386,7 +382,7 @@ __device__ __forceinline__ void accumulate_voxel(float2 (&acc)[NP], float ca, in
         }
     }
     const float off = (float)(t - kTimeRange);  // exact
-    const float Y = sAR[ar_slot(t)].x;
+    const float Y = sAR[t].x;
     const float n = (float)sN[t];
     // beta = 2 kappa w (off - s_n), s_n = s0 + n w
     const float beta = T.kappa2w * (off - fmaf(n, T.w, T.s0));
@@ -551,7 +547,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                         bool anyfar = false;
                         const float2 v = vbuf[0];
                         int t = lookup_offset(offset_of(v, 0), T.tsafe, anyfar);
-                        float2 ar = sAR[ar_slot(t)];
+                        float2 ar = sAR[t];
                         int nb = __float_as_int(ar.x) & T.nmask;
                         float ca = c * v.x;
 #pragma unroll 2
@@ -559,7 +555,7 @@ __device__ __forceinline__ void walk_task(const PairCtx& C, const TofConst& T, i
                             const int j1 = j + 1 < jn ? j + 1 : j;
                             const float2 v1 = vbuf[j1];
                             const int t1 = lookup_offset(offset_of(v1, j1), T.tsafe, anyfar);
-                            const float2 ar1 = sAR[ar_slot(t1)];
+                            const float2 ar1 = sAR[t1];
                             const int nb1 = __float_as_int(ar1.x) & T.nmask;
                             accumulate_loaded<NP>(acc, ca, ar, nb, sG);
                             ar = ar1;
