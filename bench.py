@@ -748,8 +748,6 @@ def run_serving(dev, args, att):
     # ones on a stratified sample of their scatter points (the served result
     # is first compared with the same request run alone, 1e-5, then that
     # run's point sample with the oracle's)
-    from opensss_gb300.engine import select_points
-
     errs_small, errs_large, solo_large = [], [], []
     for r in [r for r in served if not beds[r.bed].large][:args.serve_check]:
         bed, pr = beds[r.bed], problems[r.bed]

@@ -3,8 +3,6 @@
 
 import json
 
-import pytest
-
 from opensss_gb300 import autotune
 
 

@@ -3,7 +3,6 @@
 a cell can differ), the tuner picks a candidate, and shapes outside the
 compiled bounds are rejected."""
 
-import numpy as np
 import pytest
 
 from conftest import rel_l2
