@@ -8,7 +8,7 @@
 //    reference's wrapping uint16 at the end.  The randoms and normalisation
 //    sinograms keep the value of the last event (file order) of each cell,
 //    as the reference's per-event assignment does: atomicMax of the event
-//    number, then a second pass writes the winners' values.
+//    number, then a pass over the cells writes the winners' values.
 //  * inject_*: InjectScatters (Datafile.py:117-240): events outside the TOF
 //    range or the tables are dropped, the others get a scatter rate inserted
 //    after their correction factors; the kept events keep file order
@@ -114,18 +114,21 @@ __global__ void histogram_finish_kernel(const unsigned int* __restrict__ counts,
         prompts[i] = (uint16_t)(counts[i] & 0xffffu);  // numpy uint16 += 1 wraps
 }
 
+// One thread per cell: the cell's last event (numbered from 1 by the
+// histogram pass, 0 = none) gives its randoms and normalisation values,
+// event[0] * scan_duration / TOF_bins and event[1] (Datafile.py:95-99).  The
+// cells are read in order and only the winning events at random: cheaper
+// than parsing every event again to find the winners.
 __global__ void last_values_kernel(const unsigned char* __restrict__ ev, long long n, sss_listmode_layout L,
-                                   sss_sino_map M, const unsigned long long* __restrict__ last, double duration,
-                                   float* __restrict__ randoms, float* __restrict__ norm)
+                                   long long ncell, int tof_bins, const unsigned long long* __restrict__ last,
+                                   double duration, float* __restrict__ randoms, float* __restrict__ norm)
 {
-    const int ncr = M.nd_lor * M.mash;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-         e += (long long)gridDim.x * blockDim.x) {
-        const unsigned char* rec = ev + e * L.record_bytes;
-        const long long cell = event_cell(parse_event(rec, L, ncr, M.shift), M);
-        if (cell < 0 || last[cell] != (unsigned long long)(e + 1)) continue;
-        // event[0] * scan_duration / TOF_bins and event[1] (Datafile.py:95-99)
-        if (randoms) randoms[cell] = (float)(((double)load_u32(rec, 0) * duration) / M.tof_bins);
+    for (long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x; cell < ncell;
+         cell += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long e1 = last[cell];
+        if (e1 == 0 || e1 > (unsigned long long)n) continue;
+        const unsigned char* rec = ev + (long long)(e1 - 1) * L.record_bytes;
+        if (randoms) randoms[cell] = (float)(((double)load_u32(rec, 0) * duration) / tof_bins);
         if (norm) norm[cell] = load_f32(rec, 4);
     }
 }
@@ -278,9 +281,9 @@ extern "C" int sss_histogram_finish(const void* events, int64_t n_events, const 
     histogram_finish_kernel<<<grid_for(nbins, 256), 256, 0, st>>>(counts, nbins, prompts);
     if ((rc = sss_check_launch("histogram_finish_kernel"))) return rc;
     if ((randoms || norm) && n_events > 0) {
-        last_values_kernel<<<grid_for(n_events, 256), 256, 0, st>>>((const unsigned char*)events, n_events,
-                                                                     *layout, *map, last, duration, randoms,
-                                                                     norm);
+        last_values_kernel<<<grid_for(ncell, 256), 256, 0, st>>>((const unsigned char*)events, n_events, *layout,
+                                                                  ncell, map->tof_bins, last, duration, randoms,
+                                                                  norm);
         return sss_check_launch("last_values_kernel");
     }
     return SSS_OK;
