@@ -100,22 +100,29 @@ __global__ void __launch_bounds__(256) minmax_final_kernel(float* __restrict__ p
 
 // One axis of the Gaussian filter: out = sum_k w[k] in[clamp(i + k - r)] along
 // `axis` (edge samples repeated).  Weights are FP32 copies of the normalised
-// FP64 kernel, staged in shared memory.
+// FP64 kernel, staged in shared memory.  I: the index type, 32-bit unsigned
+// for volumes below 2^31 elements (the index arithmetic is most of the
+// kernel's instructions), 64-bit above.
+template <typename I>
 __global__ void __launch_bounds__(256) gauss_axis_kernel(const float* __restrict__ in, float* __restrict__ out,
                                                          Dims d, int axis, const float* __restrict__ w, int r)
 {
     __shared__ float sw[2 * kMaxRadius + 1];
     for (int i = threadIdx.x; i <= 2 * r; i += blockDim.x) sw[i] = w[i];
     __syncthreads();
-    const long long total = d.count();
-    const long long stride = axis == 2 ? 1 : (axis == 1 ? d.n[2] : (long long)d.n[1] * d.n[2]);
+    const I total = (I)d.count();
+    const I stride = axis == 2 ? (I)1 : (axis == 1 ? (I)d.n[2] : (I)d.n[1] * (I)d.n[2]);
     const int len = d.n[axis];
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int p = (int)((i / stride) % len);  // position along the axis
-        const long long base = i - (long long)p * stride;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
+        const int p = (int)((i / stride) % (I)len);  // position along the axis
+        const I base = i - (I)p * stride;
         float acc = 0.f;
-        for (int k = -r; k <= r; ++k) acc = fmaf(sw[k + r], in[base + (long long)clampi(p + k, 0, len - 1) * stride], acc);
+        if (p >= r && p + r < len) {  // no sample past an end: a running offset
+            I q = base + (I)(p - r) * stride;
+            for (int k = 0; k <= 2 * r; ++k, q += stride) acc = fmaf(sw[k], in[q], acc);
+        } else {
+            for (int k = -r; k <= r; ++k) acc = fmaf(sw[k + r], in[base + (I)clampi(p + k, 0, len - 1) * stride], acc);
+        }
         out[i] = acc;
     }
 }
@@ -139,6 +146,8 @@ __global__ void pad_edge_kernel(const float* __restrict__ f, Dims d, float* __re
 // (Unser's recursive filter: gain 6, causal and anti-causal passes with pole
 // z = sqrt(3) - 2, mirror-symmetric start values).  The 12 edge samples in
 // front of the data make the start values' effect on the data below z^12.
+constexpr int kSplineAhead = 8;  // values loaded ahead of the in-place recursion
+
 __global__ void spline_axis_kernel(float* __restrict__ P, Dims d, int axis)
 {
     const float z = -0.26794919243112270f;  // sqrt(3) - 2
@@ -167,16 +176,41 @@ __global__ void spline_axis_kernel(float* __restrict__ P, Dims d, int axis)
         }
         x[0] = c0;
         float prev = c0;
-        for (int k = 1; k < len; ++k) {
-            prev = fmaf(z, prev, 6.f * x[k * stride]);
-            x[k * stride] = prev;
+        // The recursion runs in place, so each load would otherwise wait for
+        // the store before it: kSplineAhead values are loaded together first
+        // (none of them written yet), then filtered and stored.
+        int k = 1;
+        for (; k + kSplineAhead <= len; k += kSplineAhead) {
+            float v[kSplineAhead];
+#pragma unroll
+            for (int j = 0; j < kSplineAhead; ++j) v[j] = x[(long long)(k + j) * stride];
+#pragma unroll
+            for (int j = 0; j < kSplineAhead; ++j) {
+                prev = fmaf(z, prev, 6.f * v[j]);
+                x[(long long)(k + j) * stride] = prev;
+            }
+        }
+        for (; k < len; ++k) {
+            prev = fmaf(z, prev, 6.f * x[(long long)k * stride]);
+            x[(long long)k * stride] = prev;
         }
         // anti-causal start from the last two causal values
-        float next = (z / (z * z - 1.f)) * fmaf(z, len > 1 ? x[(len - 2) * stride] : prev, prev);
+        float next = (z / (z * z - 1.f)) * fmaf(z, len > 1 ? x[(long long)(len - 2) * stride] : prev, prev);
         x[(long long)(len - 1) * stride] = next;
-        for (int k = len - 2; k >= 0; --k) {
-            next = z * (next - x[k * stride]);
-            x[k * stride] = next;
+        k = len - 2;
+        for (; k - kSplineAhead + 1 >= 0; k -= kSplineAhead) {
+            float v[kSplineAhead];
+#pragma unroll
+            for (int j = 0; j < kSplineAhead; ++j) v[j] = x[(long long)(k - j) * stride];
+#pragma unroll
+            for (int j = 0; j < kSplineAhead; ++j) {
+                next = z * (next - v[j]);
+                x[(long long)(k - j) * stride] = next;
+            }
+        }
+        for (; k >= 0; --k) {
+            next = z * (next - x[(long long)k * stride]);
+            x[(long long)k * stride] = next;
         }
     }
 }
@@ -326,8 +360,12 @@ extern "C" int sss_crop_downscale(const float* image, const int image_dims[3], c
     float* other = tmp;
     for (int d = 0; d < 3; ++d) {
         if (radius[d] < 0) continue;
-        gauss_axis_kernel<<<grid_for(nc), 256, 0, st>>>(cur, other, dc, d, wdev + d * (2 * kMaxRadius + 1),
-                                                        radius[d]);
+        if (nc < (1ll << 31))
+            gauss_axis_kernel<unsigned><<<grid_for(nc), 256, 0, st>>>(cur, other, dc, d,
+                                                                      wdev + d * (2 * kMaxRadius + 1), radius[d]);
+        else
+            gauss_axis_kernel<long long><<<grid_for(nc), 256, 0, st>>>(cur, other, dc, d,
+                                                                       wdev + d * (2 * kMaxRadius + 1), radius[d]);
         float* t = cur;
         cur = other;
         other = t;
