@@ -239,7 +239,8 @@ def test_tof_bins_sum_to_nontof(cuda_ok, att_table):
     assert rel_l2(tof.sum(axis=0), non[0]) < 1e-4
 
 
-@pytest.mark.parametrize("name", ["sss_tiny_b5", "sss_nontof_40x40x20"])
+@pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b5", "sss_tiny_wide", "sss_tiny_far",
+                                  "sss_nontof_40x40x20"])
 def test_kahan_reduction_matches_reference(cuda_ok, att_table, name):
     """The precision launch (SSS_FLAG_KAHAN: compensated sum over the scatter
     points, float-pair TOF offsets) stays within the same 1e-4 bar and is at
