@@ -513,3 +513,14 @@ def test_dropin_full_dense_path(cuda_ok, att_table):
     assert rel_l2(out, ref) < TOL
     out2 = SingleScatterSimulationTOF(pr.activity, pr.attenuation, *args)
     assert not np.shares_memory(out, out2) and rel_l2(out2, out) < 1e-6
+    # with few host threads the GPU writes every element instead of the host clearing the result
+    import torch
+
+    threads = torch.get_num_threads()
+    torch.set_num_threads(2)
+    try:
+        out3 = SingleScatterSimulationTOF(pr.activity, pr.attenuation, *args)
+    finally:
+        torch.set_num_threads(threads)
+    assert_same_support(out3, ref)
+    assert rel_l2(out3, out) < 1e-6
