@@ -309,7 +309,7 @@ def run_ours(args, rank, world, local_rank):
             "peak": peaks["smem"], "peak_source": "measured (sss_probe_smem_rate, this run)",
             "frac": achieved / peaks["smem"] if achieved and peaks["smem"] else None,
             "traffic": None,
-            "traffic_note": "DRAM bytes come from ncu only (profiles/pair_kernel_tof13_64x64x48.md); "
+            "traffic_note": "DRAM bytes come from an ncu capture only, not from this run; "
                             "the TOF factors are read from shared memory, not DRAM",
             "algorithmic_bytes_per_launch": alg_bytes,
             "bytes_rule": "(4 B x bins + 8 B) per (voxel, detector pair) term walked",
