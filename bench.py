@@ -616,11 +616,12 @@ def run_precision(dev, args, att):
     crystals, 33 TOF bins of 15 mm.  Full-size throughput of the plain launch
     and of the precision launch ("kahan": SSS_FLAG_KAHAN, Kahan-compensated
     scatter-point reduction and float-pair TOF offsets), then both against the
-    FP64 oracle on a sample of scatter points: relative L2,
-    largest bin error (over the largest reference bin) and the fitted scale
-    of the centre TOF bin (prompts drawn from the FP64 scatter).  The sample
-    is ``--precision-points`` scatter points spread evenly over the workload
-    in lattice order."""
+    FP64 GPU oracle (the C restatement's SSS run on the GPU, oracle/
+    sss_oracle_gpu.cu) on a sample of scatter points: relative L2, largest bin
+    error (over the largest reference bin) and the fitted scale of the centre
+    TOF bin (prompts drawn from the FP64 scatter).  The sample is one scatter
+    point in ``--precision-every``, spread evenly over the workload in
+    lattice order (1: the whole workload)."""
     import torch
 
     from opensss_gb300 import TofSSS, geometry as G, workloads as W
@@ -659,9 +660,17 @@ def run_precision(dev, args, att):
                          "steps": args.precision_steps, "warmup": args.precision_warmup}
     eng._ws = None
     # errors on a stratified sample (every sampled z-slice) against the FP64 oracle
-    idx, n_all = stratified_sample(pr, args.precision_points)
+    from oracle import oracle as O
+
+    n_all = len(O.scatter_points(pr.activity, pr.attenuation, pr.image_size, pr.sample_step)[0])
+    idx = W.stratified_points(n_all, max(1, n_all // max(1, args.precision_every)))
     n = len(idx)
-    ref, _ = oracle_sample(pr, att, idx, cpu_threads())
+    t0 = time.perf_counter()
+    ref = O.sss_compact(pr.activity, pr.attenuation, pr.image_size, pr.scanner.geometry, pr.scanner.normals,
+                        pr.scanner.detector_size_mm, att, pr.energy_resolution, pr.energy_threshold,
+                        pr.nr_rings_used, pr.nr_detectors_used, pr.sample_step, pr.tof_resolution, pr.tof_range,
+                        pr.nr_bins, points=idx, gpu=True)
+    oracle_s = time.perf_counter() - t0
     nru, ndu = pr.nr_rings_used, pr.nr_detectors_used
     outs = {k: eng.run_flat(act, mu, pr.grid, pr.image_size, points=idx, kahan=(k == "kahan"))
             for k in ("plain", "kahan")}
@@ -707,7 +716,9 @@ def run_precision(dev, args, att):
             "error_vs_fp64_oracle": err, "fp64_fitted_scale": s_ref, "fit_bin": b,
             "sample": f"{n} of {n_all} scatter points, evenly spread in lattice order "
                       f"({n * _pairs(nru, ndu) * pr.nr_bins:.3e} units)",
-            "fp64_oracle": "oracle/sss_oracle.c (FP64 C restatement), host cores",
+            "fp64_oracle": "oracle/sss_oracle_gpu.cu: the FP64 C restatement's SSS on this GPU (shared "
+                           "arithmetic in oracle/orc_core.h, no fused multiply-adds)",
+            "fp64_oracle_seconds": oracle_s,
             "kahan": "SSS_FLAG_KAHAN: Kahan-compensated scatter-point sums and TOF offsets from float-pair "
                      "distances and samples"}
 
@@ -1125,8 +1136,9 @@ def main():
     ap.add_argument("--batch-size", type=int, default=64, help="instances in the uneven batch")
     ap.add_argument("--batch-steps", type=int, default=3, help="timed replays of the batch (at most --steps)")
     ap.add_argument("--no-precision", action="store_true", help="skip the 33-bin precision study")
-    ap.add_argument("--precision-points", type=int, default=32,
-                    help="scatter points of the FP64 oracle sample in the precision study")
+    ap.add_argument("--precision-every", type=int, default=16,
+                    help="one scatter point in this many (evenly spread) enters the FP64 GPU oracle's check "
+                         "of the 33-bin instance (1: all points)")
     ap.add_argument("--precision-steps", type=int, default=1)
     ap.add_argument("--precision-warmup", type=int, default=1)
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")

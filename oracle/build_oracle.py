@@ -3,6 +3,9 @@
 * ``oracle/_build/libsssoracle.so`` — the FP64 C restatement
   (``oracle/sss_oracle.c``), built with OpenMP and ``-ffp-contract=off`` so
   that no multiply-add is fused, matching the reference's IEEE FP64 numerics.
+* ``oracle/_build/libsssoracle_gpu.so`` — the FP64 GPU oracle
+  (``oracle/sss_oracle_gpu.cu``): the same restatement's SSS on an sm_103a GPU,
+  built with ``-fmad=false`` so that no multiply-add is fused there either.
 * ``oracle/_ref/libref_rt3dtof.so`` and ``oracle/_ref/libref_rt3d.so`` — the
   reference's own MEX ray tracers (``Matlab/RayTracing3DTOF.cpp``,
   ``Matlab/RayTracing3D.cpp``) compiled unmodified from the reference checkout
@@ -40,8 +43,21 @@ def build_oracle(force=False):
     os.makedirs(out_dir, exist_ok=True)
     src = os.path.join(HERE, "sss_oracle.c")
     out = os.path.join(out_dir, "libsssoracle.so")
-    if force or _stale(out, [src]):
+    if force or _stale(out, [src, os.path.join(HERE, "orc_core.h")]):
         _run(["gcc", "-std=gnu11", *CFLAGS, "-fopenmp", src, "-o", out + ".tmp", "-lm"])
+        os.replace(out + ".tmp", out)
+    return out
+
+
+def build_oracle_gpu(force=False):
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    src = os.path.join(HERE, "sss_oracle_gpu.cu")
+    out = os.path.join(out_dir, "libsssoracle_gpu.so")
+    if force or _stale(out, [src, os.path.join(HERE, "orc_core.h")]):
+        nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+        _run([nvcc if os.path.exists(nvcc) else "nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+              "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-shared", src, "-o", out + ".tmp"])
         os.replace(out + ".tmp", out)
     return out
 
@@ -79,4 +95,5 @@ def build_ref(force=False):
 
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
+    print(build_oracle_gpu(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))

@@ -1,10 +1,12 @@
 """Python face of the oracle (test infrastructure only).
 
-ORACLE — only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
-baseline import this module, and only as the test oracle or the timed CPU
-reference arm.  It loads ``oracle/_build/libsssoracle.so`` (the FP64 C
+ORACLE — only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its
+CPU baseline and its error checks against FP64) import this module, and only
+as the test oracle or the timed CPU reference arm.  It loads ``oracle/_build/libsssoracle.so`` (the FP64 C
 restatement) and, where it was built, the reference's own MEX ray tracers from
-``oracle/_ref``.  The per-problem tables are rebuilt here independently of the
+``oracle/_ref``; ``sss_compact(..., gpu=True)`` runs the same restatement's
+SSS on the current CUDA device (``oracle/_build/libsssoracle_gpu.so``, the
+FP64 GPU oracle).  The per-problem tables are rebuilt here independently of the
 engine, with the same NumPy/SciPy calls the reference makes
 (``Python/openSSS/SingleScatterSimulationTOF.py:99-150``).
 """
@@ -208,15 +210,35 @@ def scatter_points(act, mu, image_size, step):
     return xyz, sl
 
 
+_gpu_lib = None
+
+
+def gpu_lib():
+    """The FP64 GPU oracle (``oracle/_build/libsssoracle_gpu.so``)."""
+    global _gpu_lib
+    if _gpu_lib is None:
+        path = os.path.join(HERE, "_build", "libsssoracle_gpu.so")
+        if not os.path.exists(path):
+            from oracle import build_oracle  # noqa: WPS433
+
+            build_oracle.build_oracle_gpu()
+        _gpu_lib = C.CDLL(path)
+        _gpu_lib.orc_sss_gpu.restype = C.c_int
+        _gpu_lib.orc_sss_gpu.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+    return _gpu_lib
+
+
 def sss_compact(act, mu, image_size, geometry, normals, det_size, att_table, energy_resolution,
                 energy_threshold, nru, ndu, step, tof_resolution, tof_range, nbins,
-                sp_begin=0, sp_end=-1, nthreads=0, tof=None, points=None):
+                sp_begin=0, sp_end=-1, nthreads=0, tof=None, points=None, gpu=False, leg_bytes=0):
     """FP64 SSS; returns compact [B, NRU*NRU, NDU, NDU] (pairs di1<=di2 filled).
     ``tof`` replaces the TOF table ([B, 8001], e.g. an emulation of another
     evaluation of the weights).  ``points`` (ascending scatter-point numbers
     in lattice order) restricts the sum to those points instead of the range
     [sp_begin, sp_end); each z-slice is then normalised over its listed
-    points, as the engine does for the same subset."""
+    points, as the engine does for the same subset.  ``gpu`` runs the same
+    restatement on the current CUDA device (``orc_sss_gpu``, the FP64 GPU
+    oracle), holding at most ``leg_bytes`` of voxel lists at once (0: 4 GB)."""
     tables = problem_tables(att_table, energy_threshold, energy_resolution, nbins, tof_range,
                             tof_resolution)
     if tof is not None:
@@ -226,7 +248,10 @@ def sss_compact(act, mu, image_size, geometry, normals, det_size, att_table, ene
     s, keep = _sss_struct(act, mu, image_size, geometry, normals, det_size, nru, ndu, step,
                           tables, sp_begin, sp_end, points)
     out = np.zeros((nbins, nru * nru, ndu, ndu))
-    st = lib().orc_sss(C.byref(s), _p(out), C.c_int(nthreads))
+    if gpu:
+        st = gpu_lib().orc_sss_gpu(C.addressof(s), _p(out), int(leg_bytes))
+    else:
+        st = lib().orc_sss(C.byref(s), _p(out), C.c_int(nthreads))
     if st != 0:
         raise RuntimeError(f"oracle SSS failed with status {st}")
     return out

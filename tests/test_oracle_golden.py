@@ -227,3 +227,9 @@ def test_oracle_mask_threshold_rule(case):
     assert np.all(loose >= exact)
     if mu.max() > 0:  # one fixture is the empty map, where every LOR is a tail either way
         assert loose.sum() > exact.sum()
+
+
+def test_gpu_oracle_library_builds_and_exports_its_entry_point():
+    """The FP64 GPU oracle (oracle/sss_oracle_gpu.cu) cross-compiles for
+    sm_103a here and loads without a GPU; its runs are the -m gpu tests."""
+    assert hasattr(O.gpu_lib(), "orc_sss_gpu")
