@@ -234,6 +234,15 @@ def gen_sss(R, which):
                          W.make_problem("wide-body-tof13", (17, 17, 4), 3.1, 2, 12, 13, 3.9, 214.0, seed=21,
                                         scanner=W.ring_scanner(48, 4, radius_cm=41.0, ring_pitch_cm=1.0,
                                                                phase=0.5), radius_cm=25.0)))
+    if "evenaniso" in which:
+        # an even bin count (no bin centred on offset 0), an odd sampled
+        # crystal count, a sampling step that differs per axis and more
+        # slices than columns (Nz > Nx = Ny)
+        problems.append(("sss_tiny_even_aniso",
+                         W.make_problem("tiny-even-aniso", (10, 10, 14), 1.6, 3, 7, 4, 2.5, 214.0, seed=23,
+                                        scanner=W.ring_scanner(48, 8, radius_cm=20.0, ring_pitch_cm=1.0,
+                                                               phase=0.5),
+                                        radius_cm=7.0, sample_step=(1, 2, 3))))
     if "edge" in which:
         # degenerate inputs: no scatter point (empty attenuation map, or a
         # sampling step past the volume), no activity, one sampled ring, and
@@ -676,7 +685,7 @@ def gen_support(R):
 
 
 ALL = ["rays", "tables", "sss_tiny", "sss_nontof_40x40x20", "sss_nxgt", "sss_tofrange", "sss_bins", "sss_widebody",
-       "sss_edge",
+       "sss_evenaniso", "sss_edge",
        "sss_tof13_slice", "upsample", "upsample_lut",
        "mask", "fit", "span", "listmode", "prep", "support"]
 

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 ORACLE_TOL = 1e-13
 
 GOLDENS = ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_tiny_nx14_ny10", "sss_tiny_wide", "sss_tiny_far",
-           "sss_wide_body_tof13", "sss_edge_empty_mu", "sss_edge_empty_act", "sss_edge_one_ring",
+           "sss_wide_body_tof13", "sss_tiny_even_aniso", "sss_edge_empty_mu", "sss_edge_empty_act", "sss_edge_one_ring",
            "sss_edge_one_crystal", "sss_edge_step_past_volume"]
 
 

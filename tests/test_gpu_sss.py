@@ -59,7 +59,7 @@ def _valid_mask(nru, ndu):
 
 
 @pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_nontof_40x40x20",
-                                  "sss_tiny_nx14_ny10", "sss_tiny_wide"])
+                                  "sss_tiny_nx14_ny10", "sss_tiny_wide", "sss_tiny_even_aniso"])
 def test_sss_matches_reference(cuda_ok, att_table, name):
     """sss_tiny_wide has bins 1.56 x the timing FWHM wide, so its weights take
     the per-bin 2^x evaluation; the other TOF cases take the factored one."""

@@ -51,7 +51,8 @@ EDGE = ["sss_edge_empty_mu", "sss_edge_empty_act", "sss_edge_one_ring", "sss_edg
 
 
 @pytest.mark.parametrize("name", ["sss_tiny_b1", "sss_tiny_b3", "sss_tiny_b5", "sss_tiny_nx14_ny10",
-                                  "sss_tiny_wide", "sss_tiny_far", "sss_wide_body_tof13"] + EDGE)
+                                  "sss_tiny_wide", "sss_tiny_far", "sss_wide_body_tof13", "sss_tiny_even_aniso"]
+                         + EDGE)
 def test_oracle_sss_matches_reference(name, att_table):
     g = golden(name)
     pr = problem_from_golden(g)
